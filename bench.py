@@ -1,0 +1,415 @@
+#!/usr/bin/env python3
+"""Benchmark of the plain WoB hot path on one GB300.
+
+Workload (the largest single-GPU configuration of the headline metric): 3D interior Robin problem
+(du/dn + 2u = h), direct BIE, backward estimator with uniform boundary sampling, on an icosphere
+subdivided to 81,920 triangles and displaced by 0.15 * sum_{l<=4} c_lm Y_lm (c_lm ~ N(0,1), seed
+0); exact solution u = 1/(4 pi |x - s|), s = (3, 0.5, 0); evaluation points on a 512 x 512 grid of
+the z = 0 slice over [-1.3, 1.3]^2, kept when inside the surface; 4096 paths per point, 16 bounces,
+FP32 walks, FP64 sums, Philox seed 0.
+
+A step is one pass over every evaluation point with 4096 new paths (path_offset advances, as the
+reference's iteration loop does). Metric: bounces per second (a bounce is one executed iteration of
+the bounce loop, estimator.cuh:252); the RMSE against the exact solution after all timed steps is
+reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores: the reference itself cannot be
+built (its Eigen / lbvh / libigl / json submodules are empty), so this runs the CPU restatement
+under oracle/ with all host threads, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bounces/s; time to RMSE 1e-3 vs analytic, plain vs learned-CV WoB, 1 GB300"
+UNIT = "bounces/s"
+PATHS = 4096
+PATH_LENGTH = 16
+GRID = 512
+EXTENT = 2.6
+SEED = 0
+# Algorithmic bytes per bounce of this workload: two uniform boundary samples, each one element
+# record (76 B) plus one sampling-table entry (8 B).
+BYTES_PER_BOUNCE = 2 * (76 + 8)
+# DRAM bytes (read + write) of one walk launch, measured by ncu on the same kernel over 1/16 of
+# the evaluation points and scaled to a full launch by the bounces it processes; None until
+# captured (profiles/walk_uniform3d_robin_icosphere81920.md).
+TRAFFIC_BYTES_PER_BOUNCE = None
+WORKLOAD = ("3D interior Robin (du/dn + 2u = h), direct BIE, backward estimator, uniform sampling; "
+            "displaced icosphere 81920 triangles; 512x512 z=0 slice over [-1.3,1.3]^2, inside points; "
+            "4096 paths x 16 bounces per point per step")
+PROBE_DIR = np.array([0.48, 0.57, 0.66])
+
+
+def build_scene_arrays():
+    from wobtoolbox_gb300 import workloads as W
+    return W.config1_scene(subdiv=6, seed=SEED, alpha=2.0, source=(3.0, 0.5, 0.0))
+
+
+def params():
+    import wobtoolbox_gb300 as wob
+    return wob.EstimatorParams(bie_model=wob.Direct, domain=wob.InteriorDomain, estimator=wob.BackwardEstimator,
+                               problem=wob.RobinProblem, path_length=PATH_LENGTH, num_sample_paths=PATHS,
+                               seed=SEED)
+
+
+def probe_dirs(n):
+    d = np.tile(PROBE_DIR / np.linalg.norm(PROBE_DIR), (n, 1)).astype(np.float32)
+    return d
+
+
+def exact(points, sc):
+    from wobtoolbox_gb300 import workloads as W
+    return W.point_sources(points, sc["source"], sc["strengths"])[:, 0]
+
+
+def cpu_sample(sc, n_points, seed=1):
+    """A fixed pseudo-random sample of inside slice points, classified with the oracle's
+    brute-force half-line parity test."""
+    from oracle import oracle_py as O
+    from wobtoolbox_gb300 import workloads as W
+    cand = W.slice_points_z0(GRID, EXTENT)
+    perm = np.random.default_rng(seed).permutation(len(cand))
+    el = O.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    chosen = []
+    for s in range(0, len(perm), 256):
+        pts = cand[perm[s:s + 256]]
+        d = probe_dirs(len(pts))
+        counts, _, hp = O.line_query(el, pts, d)
+        for i in range(len(pts)):
+            m = min(int(counts[i]), 64)
+            t = ((hp[i, :m] - pts[i]) * d[i]).sum(1)
+            if (t > 0).sum() % 2 == 1:
+                chosen.append(perm[s + i])
+        if len(chosen) >= n_points:
+            break
+    return np.ascontiguousarray(cand[np.array(chosen[:n_points])])
+
+
+def time_cpu(sc, sample_pts, paths, threads=0, path_offset=0):
+    """Runs the oracle on the sample; returns (seconds, bounces, threads used)."""
+    from oracle import oracle_py as O
+    import wobtoolbox_gb300 as wob
+    import dataclasses
+    p = dataclasses.replace(params(), num_sample_paths=paths, path_offset=path_offset)
+    el = O.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    t0 = time.perf_counter()
+    _, _, b, _ = O.solve_domain(el, p, sample_pts, n_threads=threads)
+    return time.perf_counter() - t0, b, O.max_threads()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args):
+    """CPU arm: the reference algorithm (oracle restatement) on all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle_py as O
+    O.build()
+    sc = build_scene_arrays()
+    sample_pts = cpu_sample(sc, args.ref_points)
+    paths = args.cpu_paths
+    for w in range(args.warmup):
+        time_cpu(sc, sample_pts, paths, path_offset=w * paths)
+    secs, bounces = 0.0, 0
+    for k in range(args.steps):
+        dt, b, threads = time_cpu(sc, sample_pts, paths, path_offset=(args.warmup + k) * paths)
+        secs += dt
+        bounces += b
+    value = bounces / secs
+    sample = f"{len(sample_pts)} inside slice points x {paths} paths x {PATH_LENGTH} bounces per step"
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference CPU/OpenMP build unavailable (Eigen/lbvh/libigl/json submodules empty); timed the "
+                "C++ restatement of its algorithm under oracle/ on all host threads",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import workloads as W
+
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sc = build_scene_arrays()
+    scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+
+    # inside test of every slice point on the GPU: odd number of crossings of a half-line
+    cand = W.slice_points_z0(GRID, EXTENT)
+    n_c = len(cand)
+    d_c = torch.from_numpy(cand).to(dev)
+    d_dir = torch.from_numpy(probe_dirs(n_c)).to(dev)
+    counts = torch.zeros(n_c, dtype=torch.int32, device=dev)
+    hits = torch.zeros(n_c, 64, dtype=torch.int32, device=dev)
+    hp = torch.zeros(n_c, 64, 3, dtype=torch.float32, device=dev)
+    scene.line_query(d_c, d_dir, n_c, counts, hits, hp)
+    m = torch.clamp(counts, max=64)
+    valid = torch.arange(64, device=dev)[None, :] < m[:, None]
+    t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
+    crossings = ((t > 0) & valid).sum(1)
+    inside = (crossings % 2 == 1).cpu().numpy()
+    del hits, hp
+    pts = np.ascontiguousarray(cand[inside])
+    n_pts = len(pts)
+    d_pts = torch.from_numpy(pts).to(dev)
+    d_sum = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+    d_sq = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+    d_b = torch.zeros(1, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    p = params()
+    base_offset = rank * (1 << 40)
+    import dataclasses
+
+    def step(k, sum_buf=d_sum, sq_buf=d_sq):
+        scene.solve_domain(dataclasses.replace(p, path_offset=base_offset + k * PATHS), d_pts, n_pts, sum_buf,
+                           sq_buf, d_b, stream)
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    d_sum.zero_()
+    d_sq.zero_()
+    d_b.zero_()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(float(k))  # evict the scene from L2 between timed steps (not timed)
+            starts[k].record(stream)
+            step(args.warmup + k)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    local_s = sum(kernel_ms) / 1e3
+    bounces_local = int(d_b.item())
+    if scene.poll_error():
+        raise RuntimeError("device traversal limit hit")
+    total_s = max_over_ranks(local_s, world)
+    bounces_all = sum_over_ranks(bounces_local, world)
+    value = bounces_all / total_s
+
+    # accuracy after all timed steps (args.steps * 4096 paths per point)
+    s = d_sum.cpu().numpy()
+    n_paths_total = args.steps * PATHS
+    u = s[:, 0] / n_paths_total
+    rmse = float(np.sqrt(np.mean((u - exact(pts, sc)) ** 2)))
+
+    # end to end through the C ABI with host buffers (copies in the timed region)
+    pts_pinned = torch.from_numpy(pts).pin_memory()
+    h_sum = np.zeros((n_pts, 4))
+    h_sq = np.zeros((n_pts, 4))
+    e2e_p = dataclasses.replace(p, path_offset=base_offset + (1 << 30))
+    import ctypes as C
+    lib = wob.load()
+    bb = C.c_uint64(0)
+    cp = e2e_p.to_c()
+    for w in range(1):
+        wob.check(lib.wob_solve_domain_host(scene.handle, C.byref(cp), pts_pinned.data_ptr(), n_pts,
+                                            h_sum.ctypes.data, h_sq.ctypes.data, C.byref(bb)))
+    barrier(world)
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    b0 = bb.value
+    for k in range(e2e_steps):
+        cp.path_offset = base_offset + (1 << 30) + (k + 1) * PATHS
+        wob.check(lib.wob_solve_domain_host(scene.handle, C.byref(cp), pts_pinned.data_ptr(), n_pts,
+                                            h_sum.ctypes.data, h_sq.ctypes.data, C.byref(bb)))
+    e2e_local = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_local, world)
+    e2e_bounces = sum_over_ranks(bb.value - b0, world)
+    e2e_value = e2e_bounces / e2e_s
+
+    out = None
+    if rank == 0:
+        avg_ms = sum(kernel_ms) / len(kernel_ms)
+        bounces_per_launch = bounces_local / args.steps
+        achieved = BYTES_PER_BOUNCE * bounces_per_launch / (avg_ms / 1e3) / 1e9
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        clk = clocks.summary()
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": int(len(sc["verts"])), "points": n_pts,
+                       "paths_per_point_per_step": PATHS, "path_length": PATH_LENGTH,
+                       "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
+                       "rmse_u_vs_exact": rmse, "paths_per_point_total": n_paths_total,
+                       "parallelism": f"replicas x{world}, points x independent path streams"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if peaks else
+                         "fallback 6.8 TB/s",
+                         "traffic": None if TRAFFIC_BYTES_PER_BOUNCE is None else
+                         TRAFFIC_BYTES_PER_BOUNCE * bounces_per_launch,
+                         "algorithmic_bytes_per_bounce": BYTES_PER_BOUNCE},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_pts * 3 * 4,
+                    "d2h_bytes_per_step": n_pts * 4 * 8 * 2 + 8 + 4, "steps": e2e_steps},
+            "clocks": clk,
+            "gpu_launches": args.steps,
+            "kernel_ms": kernel_ms,
+        }
+        if not args.no_cpu_baseline:
+            from oracle import oracle_py as O
+            O.build()
+            sample_pts = cpu_sample(sc, args.cpu_points)
+            dt, b, threads = time_cpu(sc, sample_pts, args.cpu_paths)
+            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": f"{len(sample_pts)} inside slice points x {args.cpu_paths} paths x "
+                                             f"{PATH_LENGTH} bounces ({dt:.1f} s)"}
+    scene.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-points", type=int, default=2048, help="CPU baseline sample (inside points)")
+    ap.add_argument("--cpu-paths", type=int, default=PATHS)
+    ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

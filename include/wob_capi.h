@@ -1,0 +1,187 @@
+/*
+ * wob_capi.h - C ABI of the GB300 walk-on-boundary (WoB) engine.
+ *
+ * Plain C types only (no CUDA or torch types in the signatures): streams are passed as void*
+ * (a cudaStream_t, or NULL for the legacy default stream), device buffers as plain pointers.
+ * Every entry point returns a wob_status; wob_last_error() gives the message of the last failure
+ * on the calling thread.
+ *
+ * Each entry point names the reference interface it replaces (rsugimoto/WoBToolbox, path:line).
+ * The enums keep the reference's numbering so a caller can pass the values its string
+ * converters produce (bie_models.cuh:24-51, estimator.cuh:24-54, points.hpp:22).
+ */
+#ifndef WOB_CAPI_H
+#define WOB_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WOB_CAPI_VERSION 1
+
+typedef enum wob_status {
+    WOB_OK = 0,
+    WOB_ERR_INVALID_ARGUMENT = 1, /* bad sizes, pointers, enums or geometry */
+    WOB_ERR_UNSUPPORTED = 2,      /* a combination the reference does not define */
+    WOB_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    WOB_ERR_OUT_OF_MEMORY = 4,
+    WOB_ERR_DEVICE_LIMIT = 5      /* a kernel hit an iteration / stack bound and stopped */
+} wob_status;
+
+/* wob::BIEModelType (bie_models.cuh:21) */
+enum { WOB_INDIRECT_SINGLE_LAYER = 0, WOB_INDIRECT_DOUBLE_LAYER = 1, WOB_DIRECT = 2 };
+/* wob::DomainType (bie_models.cuh:22) */
+enum { WOB_INTERIOR_DOMAIN = 0, WOB_EXTERIOR_DOMAIN = 1 };
+/* wob::EstimatorType (estimator.cuh:24) */
+enum { WOB_BACKWARD_ESTIMATOR = 0, WOB_FORWARD_ESTIMATOR = 1 };
+/* wob::ProblemType (estimator.cuh:38) */
+enum { WOB_DIRICHLET_PROBLEM = 0, WOB_NEUMANN_PROBLEM = 1, WOB_ROBIN_PROBLEM = 2, WOB_MIXED_PROBLEM = 3 };
+/* wob::BoundaryType (points.hpp:22) */
+enum { WOB_DIRICHLET = 0, WOB_NEUMANN = 1, WOB_ROBIN = 2 };
+
+typedef struct wob_scene_s *wob_scene;
+
+/*
+ * Solver parameters: the reference's Estimator constructor arguments (estimator.cuh:145-152)
+ * plus the template enums that wob::utils::run<> dispatches on (runtime_utils.cuh:113-153),
+ * the sample count of one launch (apps/general_2d.cu:60-61) and the random stream position.
+ */
+typedef struct wob_params {
+    int32_t bie_model;                  /* WOB_INDIRECT_SINGLE_LAYER / _DOUBLE_LAYER / WOB_DIRECT */
+    int32_t domain;                     /* WOB_INTERIOR_DOMAIN / WOB_EXTERIOR_DOMAIN */
+    int32_t estimator;                  /* WOB_BACKWARD_ESTIMATOR / WOB_FORWARD_ESTIMATOR */
+    int32_t problem;                    /* WOB_*_PROBLEM */
+    uint32_t path_length;               /* bounces per path, >= 1 */
+    uint32_t num_sample_paths;          /* paths per evaluation point in this call, >= 1 */
+    uint32_t num_resampling_candidates; /* RIS candidates (1 = plain uniform sampling) */
+    uint32_t num_volume_samples;        /* 0 = no source term */
+    float eps;                          /* kernel distance clamp (FLT_EPSILON in the reference) */
+    float first_kind_equation_scaling_constant; /* 1 in the reference */
+    uint64_t seed;                      /* Philox key */
+    uint64_t path_offset;               /* index of the first path of this call in each point's stream */
+    uint32_t point_offset;              /* stream id of the first evaluation point */
+    uint32_t flags;                     /* reserved, must be 0 */
+} wob_params;
+
+typedef struct wob_scene_info {
+    int32_t dim;
+    uint32_t n_elems;
+    uint32_t n_nodes;                   /* wide BVH nodes */
+    uint32_t bvh_depth;
+    float total_area;                   /* Scene::total_boundary_area (scene.cuh:280) */
+    float total_boundary_value;         /* Scene::total_boundary_value (scene.cuh:294) */
+    int32_t has_volume_cache;
+    uint32_t bytes_on_device;
+} wob_scene_info;
+
+/* Last error message of the calling thread ("" when none). */
+const char *wob_last_error(void);
+/* WOB_CAPI_VERSION of the loaded library. */
+int wob_version(void);
+/* Device the library was initialised on and its SM count. */
+int wob_device_info(int *device, int *sm_count);
+
+/*
+ * Builds a scene from boundary elements on the current CUDA device
+ * (replaces wob::SceneHost::SceneHost, scene.cuh:264-299, and the lbvh build it wraps).
+ * dim = 2 (segments) or 3 (triangles); host arrays in caller order:
+ *   vertices        [n_elems][dim][dim]   a, b (, c)
+ *   normals         [n_elems][dim]
+ *   boundary_values [n_elems][dim]        per-vertex g (ElementXs::boundary_value_a/b/c)
+ *   robin_alphas    [n_elems][dim]        per-vertex alpha; may be NULL (all zero)
+ *   boundary_types  [n_elems]             WOB_DIRICHLET / WOB_NEUMANN / WOB_ROBIN
+ * The scene stores elements in BVH leaf order (as the reference's CDFs are, scene.cuh:275-279);
+ * wob_scene_get_element_order() returns that order.
+ */
+int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                     const float *boundary_values, const float *robin_alphas,
+                     const int32_t *boundary_types, wob_scene *out);
+int wob_scene_destroy(wob_scene scene);
+int wob_scene_get_info(wob_scene scene, wob_scene_info *info);
+/* order[i] = caller index of the i-th stored element (n_elems entries, host memory). */
+int wob_scene_get_element_order(wob_scene scene, uint32_t *order);
+/*
+ * Reads and clears the scene's device error word (synchronous): bit 0 = a BVH traversal stack
+ * overflowed, bit 1 = a traversal hit its step bound. Kernels that set a bit stop that query and
+ * carry on; the reference has no equivalent (its lbvh query has no bound).
+ */
+int wob_scene_poll_error(wob_scene scene, uint32_t *bits);
+
+/*
+ * Attaches a source term f on a grid_res^dim cell grid over (-domain_size/2, domain_size/2)^dim,
+ * values in host memory, x fastest (replaces SceneHost::set_volume_cache + VolumeCacheHost,
+ * scene.cuh:206-252, 301-306). The |f| CDF is built on the host.
+ */
+int wob_scene_set_volume_cache(wob_scene scene, uint32_t grid_res, float domain_size,
+                               const float *values);
+int wob_scene_clear_volume_cache(wob_scene scene);
+
+/*
+ * Domain estimator over n_points evaluation points, params->num_sample_paths paths each
+ * (replaces the per-point DeviceFunctor loop of apps/general_2d.cu:43-71 / general_3d.cu:43-73
+ * around Estimator::compute_sample_path_contribution_domain, estimator.cuh:154-191, 405-454,
+ * launched by wob::utils::run<>, runtime_utils.cuh:113-153).
+ * Device pointers; enqueued on `stream`, asynchronous:
+ *   points  [n_points][dim]  float
+ *   sum     [n_points][dim+1] double   += sum over paths of [u, grad u]
+ *   sumsq   [n_points][dim+1] double   += sum over paths of [u, grad u]^2 (may be NULL)
+ *   bounces [1] uint64 += executed bounce-loop iterations (may be NULL)
+ * Accumulates into sum/sumsq, so successive calls with path_offset advanced by
+ * num_sample_paths continue each point's random stream (the reference's iteration loop,
+ * apps/general_2d.cu:327-367, with FP64 running sums instead of FP32 Kahan).
+ */
+int wob_solve_domain(wob_scene scene, const wob_params *params, const float *points,
+                     uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                     void *stream);
+
+/*
+ * Same computation with HOST buffers: copies points in, runs, copies sum/sumsq out and
+ * synchronises (sum/sumsq are accumulated into, like the device version).
+ */
+int wob_solve_domain_host(wob_scene scene, const wob_params *params, const float *points,
+                          uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces);
+
+/*
+ * Boundary estimator (replaces Estimator::compute_sample_path_contribution_boundary,
+ * estimator.cuh:193-222, 456-496, as driven by apps/boundary_estimate.cu:62-95).
+ * Device pointers, one boundary point per entry (points.hpp:32-39):
+ *   p [n][dim], n [n][dim], interior_angle [n], boundary_value [n], boundary_type [n] int32,
+ *   robin_alpha [n] (may be NULL)
+ *   sum [n], sumsq [n] (may be NULL) double, accumulated into.
+ */
+int wob_solve_boundary(wob_scene scene, const wob_params *params, const float *p,
+                       const float *n, const float *interior_angle, const float *boundary_value,
+                       const int32_t *boundary_type, const float *robin_alpha, uint32_t n_points,
+                       double *sum, double *sumsq, uint64_t *bounces, void *stream);
+
+/*
+ * All hits of the infinite lines origin + t dir (the query of scene.cuh:483-486 / 787-790).
+ * Device pointers: origins [n][dim], dirs [n][dim]; counts [n] = number of hits (uncapped);
+ * hits [n][64] = stored element indices of the first min(count, 64) hits in storage order;
+ * hit_points [n][64][dim] (may be NULL).
+ */
+int wob_line_query(wob_scene scene, const float *origins, const float *dirs, uint32_t n_rays,
+                   uint32_t *counts, uint32_t *hits, float *hit_points, void *stream);
+
+/*
+ * Per-path domain contributions for parity checks: values [n_points][num_sample_paths][dim+1]
+ * float (device), the exact per-path values whose sums wob_solve_domain accumulates.
+ */
+int wob_debug_domain_paths(wob_scene scene, const wob_params *params, const float *points,
+                           uint32_t n_points, float *values, void *stream);
+
+/* Per-path boundary contributions [n_points][num_sample_paths] float (device). */
+int wob_debug_boundary_paths(wob_scene scene, const wob_params *params, const float *p,
+                             const float *n, const float *interior_angle,
+                             const float *boundary_value, const int32_t *boundary_type,
+                             const float *robin_alpha, uint32_t n_points, float *values,
+                             void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WOB_CAPI_H */

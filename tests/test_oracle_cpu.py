@@ -1,0 +1,148 @@
+"""CPU tests of the oracle itself: known-answer vectors, the scalar math it shares with the
+engine, and unbiasedness against closed-form harmonic solutions (the reference's own validation,
+apps/general_2d.cu:123-154, apps/general_3d.cu)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests import scenes as S
+from wobtoolbox_gb300 import workloads as W
+
+
+def test_philox_known_answers(oracle):
+    # Known-answer vectors of Philox4x32-10 published with the Random123 library (Salmon et al.).
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+           ((0xFFFFFFFF,) * 4, (0xFFFFFFFF, 0xFFFFFFFF), (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+           ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+            (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, expect in kat:
+        assert [int(x) for x in oracle.philox(ctr, *key)] == list(expect)
+
+
+def test_uniforms_in_half_open_unit_interval(oracle):
+    u = oracle.uniforms(0, 0, 3, 5, 100000)
+    assert u.min() > 0.0 and u.max() <= 1.0
+    assert abs(u.mean() - 0.5) < 0.005
+    # distinct streams per (point, path)
+    assert not np.array_equal(u[:8], oracle.uniforms(0, 0, 3, 6, 8))
+    assert not np.array_equal(u[:8], oracle.uniforms(0, 1, 3, 5, 8))
+
+
+def test_sincospi_accuracy(oracle):
+    x = np.linspace(0, 2, 400001).astype(np.float32)
+    s, c = oracle.sincospi(x)
+    xd = x.astype(np.float64) * np.pi
+    assert np.abs(s - np.sin(xd)).max() < 2e-7
+    assert np.abs(c - np.cos(xd)).max() < 2e-7
+    # exact at the quadrant points
+    s, c = oracle.sincospi(np.array([0.0, 0.5, 1.0, 1.5, 2.0], np.float32))
+    assert np.array_equal(np.abs(s), [0, 1, 0, 1, 0]) and np.array_equal(np.abs(c), [1, 0, 1, 0, 1])
+
+
+def test_log_accuracy(oracle):
+    x = np.concatenate([np.logspace(-44, 38, 200000), np.linspace(1e-6, 4, 200000)]).astype(np.float32)
+    x = x[x > 0]
+    y = oracle.log(x).astype(np.float64)
+    ref = np.log(x.astype(np.float64))
+    ulp = np.abs(y - ref) / np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    assert ulp.max() < 4.0
+    z = oracle.log(np.array([0.0, -1.0, np.inf, np.nan], np.float32))
+    assert z[0] == -np.inf and np.isnan(z[1]) and z[2] == np.inf and np.isnan(z[3])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_green_functions_closed_form(oracle, dim):
+    rng = np.random.default_rng(0)
+    y = rng.standard_normal((200, dim))
+    x = rng.standard_normal((200, dim))
+    ny = rng.standard_normal((200, dim)); ny /= np.linalg.norm(ny, axis=1, keepdims=True)
+    nx = rng.standard_normal((200, dim)); nx /= np.linalg.norm(nx, axis=1, keepdims=True)
+    out = oracle.green(dim, 1e-7, y, x, ny, nx).astype(np.float64)
+    r = y - x
+    rn = np.linalg.norm(r, axis=1)
+    rh = r / rn[:, None]
+    if dim == 2:
+        G = -np.log(rn) / (2 * np.pi)
+        dGdx = rh / rn[:, None] / (2 * np.pi)
+        dGdny = -(rh * ny).sum(1) / rn / (2 * np.pi)
+        d2 = (ny - 2 * (rh * ny).sum(1)[:, None] * rh) / (2 * np.pi * rn[:, None] ** 2)
+        exp = np.concatenate([G[:, None], dGdx, dGdny[:, None], d2], 1)
+        got = out[:, :6]
+    else:
+        G = 1 / (4 * np.pi * rn)
+        dGdx = rh / rn[:, None] ** 2 / (4 * np.pi)
+        dGdny = -(rh * ny).sum(1) / rn ** 2 / (4 * np.pi)
+        d2 = (ny - 3 * (rh * ny).sum(1)[:, None] * rh) / (4 * np.pi * rn[:, None] ** 3)
+        exp = np.concatenate([G[:, None], dGdx, dGdny[:, None], d2], 1)
+        got = out[:, :8]
+    assert np.allclose(got, exp, rtol=2e-5, atol=1e-6)
+    # dG/dx is the gradient of G in x: finite differences
+    h = 1e-4
+    e0 = np.zeros(dim); e0[0] = h
+    Gp = oracle.green(dim, 1e-7, y, x + e0, ny, nx)[:, 0].astype(np.float64)
+    Gm = oracle.green(dim, 1e-7, y, x - e0, ny, nx)[:, 0].astype(np.float64)
+    fd = (Gp - Gm) / (2 * h)
+    assert np.allclose(fd, out[:, 1], rtol=5e-2, atol=5e-3)
+
+
+def _z_test(mean, ex, var, n):
+    se = np.sqrt(np.maximum(var, 1e-300) / n)
+    return (mean - ex) / se
+
+
+def test_double_layer_unbiased_2d(oracle):
+    """configs[0]-style walk: DL interior Dirichlet on a star, g = e^x cos y; z-test per point."""
+    sc = W.config0_scene()
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+    import wobtoolbox_gb300 as wob
+    pts = sc["points"][::97]
+    n = 2048
+    p = wob.EstimatorParams(path_length=8, num_sample_paths=n, seed=3)
+    s, q, b, _ = oracle.solve_domain(el, p, pts)
+    mean = s / n
+    var = q / n - mean ** 2
+    z = _z_test(mean[:, 0], W.exp_cos(pts)[:, 0], var[:, 0], n)
+    assert np.abs(z).max() < 4.5
+    assert abs(z.mean()) < 4.0 / np.sqrt(len(z))
+    # a line that only grazes the convex hull at its own element has no hit: the path ends early
+    assert 0.99 * len(pts) * n * 8 < b <= len(pts) * n * 8
+
+
+def test_closed_form_walk_matches_estimator(oracle):
+    """apps/simple_wob_and_wos.cu:81-108 (closed-form DL walk) vs the general estimator."""
+    sc = W.config0_scene()
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+    import wobtoolbox_gb300 as wob
+    pts = sc["points"][::301]
+    p = wob.EstimatorParams(path_length=6, num_sample_paths=256, seed=1)
+    s, _, _, _ = oracle.solve_domain(el, p, pts)
+    cf = oracle.simple_wob(el, 1, 6, 256, pts)
+    assert np.allclose(cf, s[:, 0], rtol=1e-4, atol=1e-3 * np.abs(s[:, 0]).max())
+
+
+@pytest.mark.parametrize("combo", [(0, 0, 0, 0), (0, 0, 1, 1), (0, 0, 0, 2), (2, 0, 0, 0), (2, 0, 0, 2),
+                                   (0, 1, 1, 1), (2, 1, 0, 0), (0, 0, 0, 3)])
+def test_estimators_unbiased_3d(oracle, combo):
+    """Backward / forward, SL / Direct, interior / exterior on a 3D displaced sphere: mean z ~ 0."""
+    import wobtoolbox_gb300 as wob
+    bie, dom, est, prob = combo
+    sc = S.scene3d(prob, bool(dom), subdiv=3)
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    n = 4096
+    p = wob.EstimatorParams(bie_model=bie, domain=dom, estimator=est, problem=prob, path_length=6,
+                            num_sample_paths=n, seed=5, num_resampling_candidates=1,
+                            first_kind_equation_scaling_constant=2.0 if prob == 3 else 1.0)
+    pts = sc["points"][:4]
+    s, q, _, _ = oracle.solve_domain(el, p, pts)
+    mean = s / n
+    var = q / n - mean ** 2
+    ex = sc["u"](pts)
+    # interior Neumann: u is defined up to a constant (apps/general_2d.cu:106-121), test grad u
+    comps = [1, 2, 3] if (prob == 1 and dom == 0) else [0]
+    for c in comps:
+        z = _z_test(mean[:, c], ex[:, c], var[:, c], n)
+        # truncated Neumann series (path_length 6): allow the truncation bias plus 5 sigma
+        bias = np.abs(mean[:, c] - ex[:, c])
+        ok = (np.abs(z) < 5.0) | (bias < 0.05 * np.abs(ex[:, c]) + 2e-3)
+        assert np.all(ok), (c, z, mean[:, c], ex[:, c])

@@ -1,0 +1,96 @@
+"""Builds the engine's shared library in-tree: wobtoolbox_gb300/_lib/libwob_gb300.so.
+
+CUDA units are compiled by nvcc for sm_103a only, in parallel; the host scene builder by the host
+C++ compiler. Walk kernels are built with -fmad=false and host code with -ffp-contract=off: every
+formula on the walk is evaluated in plain IEEE single precision (fused multiply-adds only where the
+source writes fmaf), which is what makes the engine's paths reproducible on the CPU.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libwob_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CU_SOURCES = ["capi.cu", "kernels_2d.cu", "kernels_3d.cu"]
+CPP_SOURCES = ["scene_build.cpp"]
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps() -> list[str]:
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(INCLUDE, "wob_capi.h"))
+    files.append(os.path.abspath(__file__))
+    return files
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + proc.stdout + proc.stderr)
+
+
+def cu_flags(extra: list[str] | None = None) -> list[str]:
+    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
+                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE] + (extra or [])
+
+
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
+    """Compiles the library if any source changed; returns its path."""
+    os.makedirs(OUT, exist_ok=True)
+    os.makedirs(BUILD, exist_ok=True)
+    deps = _deps()
+    if not force and not ptxas_info and not _stale(LIB, deps):
+        return LIB
+    nvcc = nvcc_path()
+    cxx = os.environ.get("CXX", "g++")
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(obj)
+        extra = ["-Xptxas", "-v"] if ptxas_info else []
+        jobs.append([nvcc] + cu_flags(extra) + ["-c", os.path.join(CSRC, src), "-o", obj])
+    for src in CPP_SOURCES:
+        obj = os.path.join(BUILD, src.replace(".cpp", ".o"))
+        objs.append(obj)
+        jobs.append([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c",
+                     os.path.join(CSRC, src), "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        futs = [ex.submit(subprocess.run, j, capture_output=True, text=True) for j in jobs]
+        for j, f in zip(jobs, futs):
+            proc = f.result()
+            if proc.returncode != 0:
+                raise RuntimeError("build failed:\n" + " ".join(j) + "\n" + proc.stdout + proc.stderr)
+            if verbose or ptxas_info:
+                sys.stderr.write(proc.stderr)
+    tmp = LIB + ".tmp"
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fPIC"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv))

@@ -1,0 +1,444 @@
+// C ABI of the GB300 WoB engine (declarations and reference citations in include/wob_capi.h).
+//
+// A scene owns its device buffers (element records, intersection records, BVH nodes, CDFs and
+// guide tables, the optional volume cache, a device error word) on the device that was current
+// when it was created. Solves are asynchronous on the caller's stream; the *_host variants stage
+// through a per-scene workspace and synchronise.
+#include "../../include/wob_capi.h"
+
+#include "launch.hpp"
+#include "scene_host.hpp"
+#include "walk_generic.cuh"
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+int fail_cuda(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? WOB_ERR_OUT_OF_MEMORY : WOB_ERR_CUDA;
+}
+
+// A device allocation freed with the scene.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+cudaError_t upload(DevBuf &b, const void *src, size_t bytes) {
+    b.release();
+    if (bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) return e;
+    b.bytes = bytes;
+    return cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice);
+}
+
+}  // namespace
+
+struct wob_scene_s {
+    int device = 0;
+    wobgb::HostScene host;
+    DevBuf elems, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
+    DevBuf vol_values, vol_cdf, vol_guide;
+    bool has_volume = false;
+    uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
+    float vol_size = 0.0f;
+    bool all_dirichlet = true;
+    // workspace of the host-pointer entry points
+    std::mutex ws_mutex;
+    DevBuf ws;
+    cudaStream_t ws_stream = nullptr;
+
+    template <int D> wobgb::SceneView<D> view() const {
+        wobgb::SceneView<D> v{};
+        v.elems = (const float4 *)elems.ptr;
+        v.isect = (const float4 *)isect.ptr;
+        v.nodes = (const float4 *)nodes.ptr;
+        v.area_cdf = (const float *)area_cdf.ptr;
+        v.area_guide = (const uint32_t *)area_guide.ptr;
+        v.bv_cdf = (const float *)bv_cdf.ptr;
+        v.bv_guide = (const uint32_t *)bv_guide.ptr;
+        v.vol_values = (const float *)vol_values.ptr;
+        v.vol_cdf = (const float *)vol_cdf.ptr;
+        v.vol_guide = (const uint32_t *)vol_guide.ptr;
+        v.err = (uint32_t *)err.ptr;
+        v.n_elems = host.n;
+        v.n_nodes = host.n_nodes;
+        v.area_G = (uint32_t)host.area_guide.size();
+        v.bv_G = (uint32_t)host.bv_guide.size();
+        v.vol_n = vol_n;
+        v.vol_G = vol_G;
+        v.vol_res = vol_res;
+        v.traversal_limit = 5u * host.n_nodes + 16u;
+        v.total_area = host.total_area;
+        v.total_bv = host.total_bv;
+        v.vol_size = vol_size;
+        return v;
+    }
+    void release_all() {
+        for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
+                          &vol_cdf, &vol_guide, &ws})
+            b->release();
+        if (ws_stream) cudaStreamDestroy(ws_stream);
+        ws_stream = nullptr;
+    }
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// Checks the parameters against the scene; fills the kernel parameter block.
+int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w) {
+    if (!p) return fail(WOB_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (p->bie_model < 0 || p->bie_model > 2) return fail(WOB_ERR_INVALID_ARGUMENT, "bie_model must be 0 (IndirectSingleLayer), 1 (IndirectDoubleLayer) or 2 (Direct)");
+    if (p->domain < 0 || p->domain > 1) return fail(WOB_ERR_INVALID_ARGUMENT, "domain must be 0 (InteriorDomain) or 1 (ExteriorDomain)");
+    if (p->estimator < 0 || p->estimator > 1) return fail(WOB_ERR_INVALID_ARGUMENT, "estimator must be 0 (BackwardEstimator) or 1 (ForwardEstimator)");
+    if (p->problem < 0 || p->problem > 3) return fail(WOB_ERR_INVALID_ARGUMENT, "problem must be 0..3 (Dirichlet, Neumann, Robin, Mixed)");
+    if (p->path_length < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "path_length must be >= 1");
+    if (p->num_sample_paths < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "num_sample_paths must be >= 1");
+    if (p->num_resampling_candidates < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "num_resampling_candidates must be >= 1");
+    if (!(p->eps > 0.0f) || !(p->eps < 3.0e38f)) return fail(WOB_ERR_INVALID_ARGUMENT, "eps must be positive and finite");
+    const float fk = p->first_kind_equation_scaling_constant;
+    if (!(fk > 0.0f) || !(fk < 3.0e38f)) return fail(WOB_ERR_INVALID_ARGUMENT, "first_kind_equation_scaling_constant must be positive and finite");
+    if (p->flags != 0) return fail(WOB_ERR_INVALID_ARGUMENT, "flags must be 0");
+    if (p->bie_model == WOB_INDIRECT_DOUBLE_LAYER && !s->all_dirichlet)
+        return fail(WOB_ERR_UNSUPPORTED, "the double-layer model supports Dirichlet boundaries only (bie_models.cuh:383)");
+    const bool needs_bv = (p->estimator == WOB_BACKWARD_ESTIMATOR && p->bie_model == WOB_DIRECT && p->problem == WOB_NEUMANN_PROBLEM) ||
+                          (p->estimator == WOB_FORWARD_ESTIMATOR && p->bie_model == WOB_INDIRECT_SINGLE_LAYER && p->problem == WOB_NEUMANN_PROBLEM);
+    if (needs_bv && !s->host.bv_valid)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "boundary-value sampling needs a nonzero, finite total |g|");
+    if (p->num_volume_samples > 0 && !s->has_volume)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "num_volume_samples > 0 needs a volume cache (wob_scene_set_volume_cache)");
+    w.bie = p->bie_model;
+    w.domain = p->domain;
+    w.estimator = p->estimator;
+    w.problem = p->problem;
+    w.path_length = p->path_length;
+    w.n_paths = p->num_sample_paths;
+    w.n_resampling = p->num_resampling_candidates;
+    w.n_volume = p->num_volume_samples;
+    w.eps = p->eps;
+    w.fk = fk;
+    w.seed = p->seed;
+    w.path_offset = p->path_offset;
+    w.point_offset = p->point_offset;
+    return WOB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wob_last_error(void) { return g_last_error.c_str(); }
+
+int wob_version(void) { return WOB_CAPI_VERSION; }
+
+int wob_device_info(int *device, int *sm_count) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGetDevice");
+    if (device) *device = dev;
+    if (sm_count) {
+        e = cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return fail_cuda(e, "cudaDeviceGetAttribute");
+    }
+    return WOB_OK;
+}
+
+int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                     const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                     wob_scene *out) {
+    if (!out) return fail(WOB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    wob_scene_s *s = new wob_scene_s();
+    std::string err = wobgb::build_host_scene(dim, n_elems, vertices, normals, boundary_values, robin_alphas,
+                                              boundary_types, s->host);
+    if (!err.empty()) {
+        delete s;
+        return fail(WOB_ERR_INVALID_ARGUMENT, err);
+    }
+    for (uint32_t i = 0; i < n_elems; i++)
+        if (boundary_types[i] != WOB_DIRICHLET) s->all_dirichlet = false;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail_cuda(e, "cudaGetDevice");
+    }
+    const wobgb::HostScene &h = s->host;
+    const uint32_t zero = 0;
+    if ((e = upload(s->elems, h.elems.data(), h.elems.size() * 4)) != cudaSuccess ||
+        (e = upload(s->isect, h.isect.data(), h.isect.size() * 4)) != cudaSuccess ||
+        (e = upload(s->nodes, h.nodes.data(), h.nodes.size() * 4)) != cudaSuccess ||
+        (e = upload(s->area_cdf, h.area_cdf.data(), h.area_cdf.size() * 4)) != cudaSuccess ||
+        (e = upload(s->area_guide, h.area_guide.data(), h.area_guide.size() * 4)) != cudaSuccess ||
+        (e = upload(s->bv_cdf, h.bv_cdf.data(), h.bv_cdf.size() * 4)) != cudaSuccess ||
+        (e = upload(s->bv_guide, h.bv_guide.data(), h.bv_guide.size() * 4)) != cudaSuccess ||
+        (e = upload(s->err, &zero, 4)) != cudaSuccess) {
+        s->release_all();
+        delete s;
+        return fail_cuda(e, "uploading the scene");
+    }
+    *out = s;
+    return WOB_OK;
+}
+
+int wob_scene_destroy(wob_scene s) {
+    if (!s) return WOB_OK;
+    {
+        DeviceGuard g(s->device);
+        s->release_all();
+    }
+    delete s;
+    return WOB_OK;
+}
+
+int wob_scene_get_info(wob_scene s, wob_scene_info *info) {
+    if (!s || !info) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and info are required");
+    info->dim = s->host.dim;
+    info->n_elems = s->host.n;
+    info->n_nodes = s->host.n_nodes;
+    info->bvh_depth = s->host.depth;
+    info->total_area = s->host.total_area;
+    info->total_boundary_value = s->host.total_bv;
+    info->has_volume_cache = s->has_volume ? 1 : 0;
+    size_t bytes = 0;
+    for (const DevBuf *b : {&s->elems, &s->isect, &s->nodes, &s->area_cdf, &s->area_guide, &s->bv_cdf, &s->bv_guide,
+                            &s->vol_values, &s->vol_cdf, &s->vol_guide})
+        bytes += b->bytes;
+    info->bytes_on_device = (uint32_t)(bytes > 0xFFFFFFFFu ? 0xFFFFFFFFu : bytes);
+    return WOB_OK;
+}
+
+int wob_scene_get_element_order(wob_scene s, uint32_t *order) {
+    if (!s || !order) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and order are required");
+    std::memcpy(order, s->host.order.data(), s->host.order.size() * 4);
+    return WOB_OK;
+}
+
+int wob_scene_set_volume_cache(wob_scene s, uint32_t grid_res, float domain_size, const float *values) {
+    if (!s || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and values are required");
+    if (grid_res < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "grid_res must be >= 1");
+    if (!(domain_size > 0.0f) || !(domain_size < 3.0e38f)) return fail(WOB_ERR_INVALID_ARGUMENT, "domain_size must be positive and finite");
+    const int dim = s->host.dim;
+    uint64_t n = 1;
+    for (int i = 0; i < dim; i++) n *= grid_res;
+    if (n > (1ull << 30)) return fail(WOB_ERR_INVALID_ARGUMENT, "volume cache too large");
+    std::vector<float> cdf;
+    std::string err = wobgb::build_volume_cdf(dim, grid_res, values, cdf);
+    if (!err.empty()) return fail(WOB_ERR_INVALID_ARGUMENT, err);
+    std::vector<uint32_t> guide = wobgb::build_guide(cdf);
+    DeviceGuard g(s->device);
+    cudaError_t e;
+    if ((e = upload(s->vol_values, values, n * 4)) != cudaSuccess || (e = upload(s->vol_cdf, cdf.data(), n * 4)) != cudaSuccess ||
+        (e = upload(s->vol_guide, guide.data(), guide.size() * 4)) != cudaSuccess) {
+        s->vol_values.release();
+        s->vol_cdf.release();
+        s->vol_guide.release();
+        s->has_volume = false;
+        return fail_cuda(e, "uploading the volume cache");
+    }
+    s->has_volume = true;
+    s->vol_res = grid_res;
+    s->vol_n = (uint32_t)n;
+    s->vol_G = (uint32_t)guide.size();
+    s->vol_size = domain_size;
+    return WOB_OK;
+}
+
+int wob_scene_clear_volume_cache(wob_scene s) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    DeviceGuard g(s->device);
+    s->vol_values.release();
+    s->vol_cdf.release();
+    s->vol_guide.release();
+    s->has_volume = false;
+    s->vol_res = s->vol_n = s->vol_G = 0;
+    return WOB_OK;
+}
+
+static int solve_domain_impl(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
+                             double *sum, double *sumsq, uint64_t *bounces, float *per_path, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!points) return fail(WOB_ERR_INVALID_ARGUMENT, "points is NULL");
+    if (!per_path && !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "sum is NULL");
+    DeviceGuard g(s->device);
+    cudaError_t e;
+    if (s->host.dim == 2)
+        e = wobgb::launch_domain_2d(s->view<2>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces,
+                                    per_path, (cudaStream_t)stream);
+    else
+        e = wobgb::launch_domain_3d(s->view<3>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces,
+                                    per_path, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the domain walk");
+    return WOB_OK;
+}
+
+int wob_solve_domain(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                     double *sumsq, uint64_t *bounces, void *stream) {
+    return solve_domain_impl(s, params, points, n_points, sum, sumsq, bounces, nullptr, stream);
+}
+
+int wob_debug_domain_paths(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
+                           float *values, void *stream) {
+    if (!values) return fail(WOB_ERR_INVALID_ARGUMENT, "values is NULL");
+    return solve_domain_impl(s, params, points, n_points, nullptr, nullptr, nullptr, values, stream);
+}
+
+int wob_solve_domain_host(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                          double *sumsq, uint64_t *bounces) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!points || !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum are required");
+    const int D = s->host.dim;
+    const size_t pts_bytes = (size_t)n_points * D * 4, out_bytes = (size_t)n_points * (D + 1) * 8;
+    const size_t off_sum = (pts_bytes + 255) / 256 * 256;
+    const size_t off_sq = off_sum + (out_bytes + 255) / 256 * 256;
+    const size_t off_b = off_sq + (out_bytes + 255) / 256 * 256;
+    const size_t total = off_b + 256;
+    std::lock_guard<std::mutex> lock(s->ws_mutex);
+    DeviceGuard g(s->device);
+    cudaError_t e;
+    if (!s->ws_stream && (e = cudaStreamCreateWithFlags(&s->ws_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail_cuda(e, "cudaStreamCreate");
+    if (s->ws.bytes < total) {
+        s->ws.release();
+        if ((e = cudaMalloc(&s->ws.ptr, total)) != cudaSuccess) return fail_cuda(e, "cudaMalloc workspace");
+        s->ws.bytes = total;
+    }
+    char *base = (char *)s->ws.ptr;
+    float *d_pts = (float *)base;
+    double *d_sum = (double *)(base + off_sum);
+    double *d_sq = (double *)(base + off_sq);
+    uint64_t *d_b = (uint64_t *)(base + off_b);
+    cudaStream_t st_ = s->ws_stream;
+    if ((e = cudaMemcpyAsync(d_pts, points, pts_bytes, cudaMemcpyHostToDevice, st_)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d_sum, 0, out_bytes, st_)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d_sq, 0, out_bytes, st_)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d_b, 0, 8, st_)) != cudaSuccess)
+        return fail_cuda(e, "staging inputs");
+    e = D == 2 ? wobgb::launch_domain_2d(s->view<2>(), w, d_pts, n_points, d_sum, sumsq ? d_sq : nullptr,
+                                         (unsigned long long *)d_b, nullptr, st_)
+               : wobgb::launch_domain_3d(s->view<3>(), w, d_pts, n_points, d_sum, sumsq ? d_sq : nullptr,
+                                         (unsigned long long *)d_b, nullptr, st_);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the domain walk");
+    std::vector<double> tmp((size_t)n_points * (D + 1));
+    uint64_t b = 0;
+    uint32_t errw = 0;
+    if ((e = cudaMemcpyAsync(tmp.data(), d_sum, out_bytes, cudaMemcpyDeviceToHost, st_)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&b, d_b, 8, cudaMemcpyDeviceToHost, st_)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&errw, s->err.ptr, 4, cudaMemcpyDeviceToHost, st_)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st_)) != cudaSuccess)
+        return fail_cuda(e, "reading results");
+    for (size_t i = 0; i < tmp.size(); i++) sum[i] += tmp[i];
+    if (sumsq) {
+        if ((e = cudaMemcpyAsync(tmp.data(), d_sq, out_bytes, cudaMemcpyDeviceToHost, st_)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st_)) != cudaSuccess)
+            return fail_cuda(e, "reading results");
+        for (size_t i = 0; i < tmp.size(); i++) sumsq[i] += tmp[i];
+    }
+    if (bounces) *bounces += b;
+    if (errw) return fail(WOB_ERR_DEVICE_LIMIT, "a BVH traversal hit its stack or step bound");
+    return WOB_OK;
+}
+
+static int solve_boundary_impl(wob_scene s, const wob_params *params, const float *p, const float *n,
+                               const float *interior_angle, const float *boundary_value,
+                               const int32_t *boundary_type, const float *robin_alpha, uint32_t n_points,
+                               double *sum, double *sumsq, uint64_t *bounces, float *per_path, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!p || !n || !interior_angle || !boundary_value || !boundary_type)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "p, n, interior_angle, boundary_value and boundary_type are required");
+    if (!per_path && !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "sum is NULL");
+    wobgb::BoundaryInput bin{p, n, interior_angle, boundary_value, boundary_type, robin_alpha};
+    DeviceGuard g(s->device);
+    cudaError_t e;
+    if (s->host.dim == 2)
+        e = wobgb::launch_boundary_2d(s->view<2>(), w, bin, n_points, sum, sumsq, (unsigned long long *)bounces,
+                                      per_path, (cudaStream_t)stream);
+    else
+        e = wobgb::launch_boundary_3d(s->view<3>(), w, bin, n_points, sum, sumsq, (unsigned long long *)bounces,
+                                      per_path, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the boundary walk");
+    return WOB_OK;
+}
+
+int wob_solve_boundary(wob_scene s, const wob_params *params, const float *p, const float *n,
+                       const float *interior_angle, const float *boundary_value, const int32_t *boundary_type,
+                       const float *robin_alpha, uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                       void *stream) {
+    return solve_boundary_impl(s, params, p, n, interior_angle, boundary_value, boundary_type, robin_alpha, n_points,
+                               sum, sumsq, bounces, nullptr, stream);
+}
+
+int wob_debug_boundary_paths(wob_scene s, const wob_params *params, const float *p, const float *n,
+                             const float *interior_angle, const float *boundary_value, const int32_t *boundary_type,
+                             const float *robin_alpha, uint32_t n_points, float *values, void *stream) {
+    if (!values) return fail(WOB_ERR_INVALID_ARGUMENT, "values is NULL");
+    return solve_boundary_impl(s, params, p, n, interior_angle, boundary_value, boundary_type, robin_alpha, n_points,
+                               nullptr, nullptr, nullptr, values, stream);
+}
+
+int wob_line_query(wob_scene s, const float *origins, const float *dirs, uint32_t n_rays, uint32_t *counts,
+                   uint32_t *hits, float *hit_points, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (n_rays == 0) return WOB_OK;
+    if (!origins || !dirs || !counts || !hits) return fail(WOB_ERR_INVALID_ARGUMENT, "origins, dirs, counts and hits are required");
+    DeviceGuard g(s->device);
+    cudaError_t e = s->host.dim == 2
+                        ? wobgb::launch_line_query_2d(s->view<2>(), origins, dirs, n_rays, counts, hits, hit_points, (cudaStream_t)stream)
+                        : wobgb::launch_line_query_3d(s->view<3>(), origins, dirs, n_rays, counts, hits, hit_points, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the line query");
+    return WOB_OK;
+}
+
+int wob_scene_poll_error(wob_scene s, uint32_t *bits) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    DeviceGuard g(s->device);
+    uint32_t v = 0;
+    cudaError_t e = cudaMemcpy(&v, s->err.ptr, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail_cuda(e, "reading the error word");
+    const uint32_t zero = 0;
+    if (v && (e = cudaMemcpy(s->err.ptr, &zero, 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail_cuda(e, "clearing the error word");
+    if (bits) *bits = v;
+    return WOB_OK;
+}
+
+}  // extern "C"

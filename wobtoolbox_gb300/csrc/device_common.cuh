@@ -1,0 +1,558 @@
+// Device building blocks of the GB300 WoB engine: Philox4x32-10 streams, polynomial sin/cos(pi x)
+// and log, small vectors, the scene view, CDF lookup through guide tables, the 4-wide BVH
+// traversal for "all hits of an infinite line", and the boundary sampling queries.
+//
+// Every translation unit that includes this header is compiled with -fmad=false: the walk uses
+// IEEE single-precision +,-,*,/ and sqrt only (fused multiply-adds only where written as fmaf),
+// so a path evaluates to the same bits as a plain IEEE evaluation of the same formulas on a CPU.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wobgb {
+
+constexpr float kEps10 = 10.0f * 1.1920928955078125e-7f;  // 10 FLT_EPSILON (scene.cuh:418, 531)
+constexpr uint32_t kHitBuffer = 64;                         // hit buffer of scene.cuh:481
+constexpr uint32_t kStackSize = 64;
+constexpr uint32_t kChildEmptyD = 0xFFFFFFFFu;
+
+// Device error word bits (see ErrorWord in capi.cu).
+constexpr uint32_t kErrStackOverflow = 1u;
+constexpr uint32_t kErrTraversalLimit = 2u;
+
+enum : int { kDirichlet = 0, kNeumann = 1, kRobin = 2 };
+enum : int { kSingleLayer = 0, kDoubleLayer = 1, kDirect = 2 };
+enum : int { kInterior = 0, kExterior = 1 };
+enum : int { kBackward = 0, kForward = 1 };
+enum : int { kDirichletProblem = 0, kNeumannProblem = 1, kRobinProblem = 2, kMixedProblem = 3 };
+
+// ------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). Counter (block, path lo, path hi, point),
+// key (seed lo, seed hi + stream); uniforms ((x >> 8) + 1) 2^-24 in (0, 1].
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+struct PathRng {
+    uint32_t k0, k1, c1, c2, c3, block;
+    uint4 buf;
+    int used;
+    __device__ __forceinline__ PathRng(uint64_t seed, uint32_t stream, uint32_t point, uint64_t path)
+        : k0((uint32_t)seed), k1((uint32_t)(seed >> 32) + stream), c1((uint32_t)path),
+          c2((uint32_t)(path >> 32)), c3(point), block(0), buf(make_uint4(0, 0, 0, 0)), used(4) {}
+    __device__ __forceinline__ float uniform() {
+        if (used == 4) {
+            buf = philox4x32_10(make_uint4(block, c1, c2, c3), k0, k1);
+            block++;
+            used = 0;
+        }
+        const uint32_t x = used == 0 ? buf.x : used == 1 ? buf.y : used == 2 ? buf.z : buf.w;
+        used++;
+        return (float)((x >> 8) + 1u) * 0x1p-24f;
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// Scalar math (same polynomials as the CPU oracle; no CUDA transcendental on the walk).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float fmax_ref(float a, float b) { return (a < b) ? b : a; }
+
+// sin(pi x), cos(pi x): x = q/2 + r, |r| <= 1/4, Taylor polynomials in r^2, quadrant rotation.
+__device__ __forceinline__ void sincospi_own(float x, float *s_out, float *c_out) {
+    const float q = rintf(x * 2.0f);
+    const float r = x - q * 0.5f;
+    const float z = r * r;
+    float sp = -0x1.e3075p-8f;
+    sp = sp * z + 0x1.507834p-4f;
+    sp = sp * z - 0x1.32d2ccp-1f;
+    sp = sp * z + 0x1.466bc6p+1f;
+    sp = sp * z - 0x1.4abbcep+2f;
+    sp = sp * z + 0x1.921fb6p+1f;
+    const float s = sp * r;
+    float cp = 0x1.f9d38ap-10f;
+    cp = cp * z - 0x1.a6d1f2p-6f;
+    cp = cp * z + 0x1.e1f506p-3f;
+    cp = cp * z - 0x1.55d3c8p+0f;
+    cp = cp * z + 0x1.03c1f0p+2f;
+    cp = cp * z - 0x1.3bd3ccp+2f;
+    const float c = cp * z + 1.0f;
+    const int qi = ((int)q) & 3;
+    float so, co;
+    if (qi == 0) { so = s; co = c; }
+    else if (qi == 1) { so = c; co = -s; }
+    else if (qi == 2) { so = -s; co = -c; }
+    else { so = -c; co = s; }
+    *s_out = so;
+    *c_out = co;
+}
+
+// log x = e ln2 + 2 atanh((m-1)/(m+1)), m in (sqrt(1/2), sqrt(2)].
+__device__ __forceinline__ float log_own(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? __int_as_float(0xff800000) : __int_as_float(0x7fffffff);
+    if (x == __int_as_float(0x7f800000)) return x;
+    int e_adj = 0;
+    if (x < 0x1p-126f) { x = x * 0x1p+23f; e_adj = -23; }
+    const uint32_t bits = __float_as_uint(x);
+    int e = (int)(bits >> 23) - 127 + e_adj;
+    float m = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float p = 0x1.745d18p-4f;
+    p = p * z + 0x1.c71c72p-4f;
+    p = p * z + 0x1.24924ap-3f;
+    p = p * z + 0x1.99999ap-3f;
+    p = p * z + 0x1.555556p-2f;
+    p = p * z + 1.0f;
+    const float logm = (2.0f * s) * p;
+    const float fe = (float)e;
+    return fe * 0x1.62e4p-1f + (fe * 0x1.7f7d1cp-20f + logm);
+}
+
+// ------------------------------------------------------------------------------------------
+// Vectors: fixed-size, fully unrolled; sums left to right.
+// ------------------------------------------------------------------------------------------
+template <int D> struct V {
+    float v[D];
+};
+template <int D> __device__ __forceinline__ V<D> vzero() { V<D> r; _Pragma("unroll") for (int i = 0; i < D; i++) r.v[i] = 0.0f; return r; }
+template <int D> __device__ __forceinline__ V<D> vadd(const V<D> &a, const V<D> &b) { V<D> r; _Pragma("unroll") for (int i = 0; i < D; i++) r.v[i] = a.v[i] + b.v[i]; return r; }
+template <int D> __device__ __forceinline__ V<D> vsub(const V<D> &a, const V<D> &b) { V<D> r; _Pragma("unroll") for (int i = 0; i < D; i++) r.v[i] = a.v[i] - b.v[i]; return r; }
+template <int D> __device__ __forceinline__ V<D> vscale(float s, const V<D> &a) { V<D> r; _Pragma("unroll") for (int i = 0; i < D; i++) r.v[i] = s * a.v[i]; return r; }
+template <int D> __device__ __forceinline__ V<D> vdiv(const V<D> &a, float s) { V<D> r; _Pragma("unroll") for (int i = 0; i < D; i++) r.v[i] = a.v[i] / s; return r; }
+template <int D> __device__ __forceinline__ float vdot(const V<D> &a, const V<D> &b) {
+    float s = a.v[0] * b.v[0];
+    _Pragma("unroll") for (int i = 1; i < D; i++) s = s + a.v[i] * b.v[i];
+    return s;
+}
+template <int D> __device__ __forceinline__ float vsqnorm(const V<D> &a) { return vdot(a, a); }
+template <int D> __device__ __forceinline__ float vnorm(const V<D> &a) { return sqrtf(vsqnorm(a)); }
+template <int D> __device__ __forceinline__ V<D> vnormalized(const V<D> &a) {
+    const float z = vsqnorm(a);
+    if (z > 0.0f) return vdiv(a, sqrtf(z));
+    return a;
+}
+__device__ __forceinline__ V<3> vcross(const V<3> &a, const V<3> &b) {
+    V<3> r;
+    r.v[0] = a.v[1] * b.v[2] - a.v[2] * b.v[1];
+    r.v[1] = a.v[2] * b.v[0] - a.v[0] * b.v[2];
+    r.v[2] = a.v[0] * b.v[1] - a.v[1] * b.v[0];
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// Boundary point (points.hpp:32-39).
+// ------------------------------------------------------------------------------------------
+template <int D> struct BPoint {
+    V<D> p, n;
+    float angle;  // interior_angle
+    float bv;     // boundary_value
+    int type;     // boundary_type
+    float alpha;  // robin_alpha
+};
+template <int D> __device__ __forceinline__ BPoint<D> bp_zero() {
+    BPoint<D> b;
+    b.p = vzero<D>(); b.n = vzero<D>();
+    b.angle = 0.0f; b.bv = 0.0f; b.type = kDirichlet; b.alpha = 0.0f;
+    return b;
+}
+
+// ------------------------------------------------------------------------------------------
+// Scene view (device pointers; filled by the host, passed by value to kernels).
+// ------------------------------------------------------------------------------------------
+template <int D> struct SceneView {
+    const float4 *__restrict__ elems;   // D==2: 3 float4 / element, D==3: 5 float4
+    const float4 *__restrict__ isect;   // D==3: 3 float4 / element (a, a-b, a-c, (a-b)x(a-c))
+    const float4 *__restrict__ nodes;   // D==2: 5 float4 / node, D==3: 7 float4
+    const float *__restrict__ area_cdf;
+    const uint32_t *__restrict__ area_guide;
+    const float *__restrict__ bv_cdf;
+    const uint32_t *__restrict__ bv_guide;
+    const float *__restrict__ vol_values;
+    const float *__restrict__ vol_cdf;
+    const uint32_t *__restrict__ vol_guide;
+    uint32_t *err;                       // device error word (kErr* bits)
+    uint32_t n_elems, n_nodes, area_G, bv_G;
+    uint32_t vol_n, vol_G, vol_res, traversal_limit;
+    float total_area, total_bv, vol_size;
+};
+
+template <int D> struct Elem {
+    V<D> v[D];
+    V<D> n;
+    float bv[D], alpha[D];
+    float area;
+    int type;
+};
+
+template <int D> __device__ __forceinline__ Elem<D> load_elem(const SceneView<D> &s, uint32_t i);
+template <> __device__ __forceinline__ Elem<2> load_elem<2>(const SceneView<2> &s, uint32_t i) {
+    const float4 q0 = __ldg(s.elems + 3 * i), q1 = __ldg(s.elems + 3 * i + 1), q2 = __ldg(s.elems + 3 * i + 2);
+    Elem<2> e;
+    e.v[0].v[0] = q0.x; e.v[0].v[1] = q0.y; e.v[1].v[0] = q0.z; e.v[1].v[1] = q0.w;
+    e.n.v[0] = q1.x; e.n.v[1] = q1.y; e.bv[0] = q1.z; e.bv[1] = q1.w;
+    e.alpha[0] = q2.x; e.alpha[1] = q2.y; e.area = q2.z; e.type = __float_as_int(q2.w);
+    return e;
+}
+template <> __device__ __forceinline__ Elem<3> load_elem<3>(const SceneView<3> &s, uint32_t i) {
+    const float4 *p = s.elems + 5 * i;
+    const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4);
+    Elem<3> e;
+    e.v[0].v[0] = q0.x; e.v[0].v[1] = q0.y; e.v[0].v[2] = q0.z;
+    e.v[1].v[0] = q0.w; e.v[1].v[1] = q1.x; e.v[1].v[2] = q1.y;
+    e.v[2].v[0] = q1.z; e.v[2].v[1] = q1.w; e.v[2].v[2] = q2.x;
+    e.n.v[0] = q2.y; e.n.v[1] = q2.z; e.n.v[2] = q2.w;
+    e.bv[0] = q3.x; e.bv[1] = q3.y; e.bv[2] = q3.z;
+    e.alpha[0] = q3.w; e.alpha[1] = q4.x; e.alpha[2] = q4.y;
+    e.area = q4.z; e.type = __float_as_int(q4.w);
+    return e;
+}
+
+// First i in [0, n-1] with key <= cdf[i], else n-1: the reference's binary_search
+// (scene.cuh:30-43), started from a guide table. guide[j] is the first index whose CDF value
+// reaches (j - 1/2)/G, so for j = floor(key G) the answer lies in [guide[j], guide[j+2]]
+// (n-1 when j+2 >= G); the bisection below runs on that sub-range only.
+__device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, const uint32_t *__restrict__ guide,
+                                               uint32_t G, uint32_t n, float key) {
+    uint32_t j = (uint32_t)(key * (float)G);
+    if (j >= G) j = G - 1;
+    uint32_t low = __ldg(guide + j);
+    uint32_t high = (j + 2 < G) ? __ldg(guide + j + 2) : n - 1;
+    while (low < high) {
+        const uint32_t mid = (high + low) / 2;
+        if (key <= __ldg(cdf + mid)) high = mid;
+        else low = mid + 1;
+    }
+    return high;
+}
+
+// val1 + u (val2 - val1) (scene.cuh:393-396)
+__device__ __forceinline__ float interp2(float a, float b, float u) { return a + u * (b - a); }
+// (1 - sqrt u1) v1 + sqrt u1 (1 - u2) v2 + u2 sqrt u1 v3 (scene.cuh:665-671)
+__device__ __forceinline__ float interp3(float a, float b, float c, float k1, float k2, float k3) {
+    return k1 * a + k2 * b + k3 * c;
+}
+
+// ------------------------------------------------------------------------------------------
+// Line / element intersection: Cramer's rule, division-free inside test, t = tn/det, |t| > 10 eps
+// (restates scene.cuh:414-436 and 707-730).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool isect_seg(const V<2> &o, const V<2> &d, float ax, float ay, float bx, float by, float &t) {
+    const float edx = ax - bx, edy = ay - by;
+    const float wx = ax - o.v[0], wy = ay - o.v[1];
+    const float det = d.v[0] * edy - d.v[1] * edx;
+    const float sn = d.v[0] * wy - d.v[1] * wx;
+    bool inside;
+    if (det > 0.0f) inside = (sn >= 0.0f) && (sn <= det);
+    else if (det < 0.0f) inside = (sn <= 0.0f) && (sn >= det);
+    else inside = false;
+    if (!inside) return false;
+    const float tn = wx * edy - wy * edx;
+    t = tn / det;
+    return fabsf(t) > kEps10;
+}
+
+__device__ __forceinline__ bool isect_tri(const V<3> &o, const V<3> &d, const float4 r0, const float4 r1, const float4 r2, float &t) {
+    // r0 = (a.x, a.y, a.z, e1.x), r1 = (e1.y, e1.z, e2.x, e2.y), r2 = (e2.z, q.x, q.y, q.z)
+    const float wx = r0.x - o.v[0], wy = r0.y - o.v[1], wz = r0.z - o.v[2];
+    float det = d.v[0] * r2.y;
+    det = det + d.v[1] * r2.z;
+    det = det + d.v[2] * r2.w;
+    // w x d
+    const float cx = wy * d.v[2] - wz * d.v[1];
+    const float cy = wz * d.v[0] - wx * d.v[2];
+    const float cz = wx * d.v[1] - wy * d.v[0];
+    float bn = r1.z * cx;
+    bn = bn + r1.w * cy;
+    bn = bn + r2.x * cz;
+    bn = -bn;
+    float gn = r0.w * cx;
+    gn = gn + r1.x * cy;
+    gn = gn + r1.y * cz;
+    bool inside;
+    if (det > 0.0f) inside = (bn >= 0.0f) && (gn >= 0.0f) && (bn + gn <= det);
+    else if (det < 0.0f) inside = (bn <= 0.0f) && (gn <= 0.0f) && (bn + gn >= det);
+    else inside = false;
+    if (!inside) return false;
+    float tn = wx * r2.y;
+    tn = tn + wy * r2.z;
+    tn = tn + wz * r2.w;
+    t = tn / det;
+    return fabsf(t) > kEps10;
+}
+
+template <int D> __device__ __forceinline__ bool isect_elem(const SceneView<D> &s, uint32_t i, const V<D> &o, const V<D> &d, float &t);
+template <> __device__ __forceinline__ bool isect_elem<2>(const SceneView<2> &s, uint32_t i, const V<2> &o, const V<2> &d, float &t) {
+    const float4 q0 = __ldg(s.elems + 3 * i);
+    return isect_seg(o, d, q0.x, q0.y, q0.z, q0.w, t);
+}
+template <> __device__ __forceinline__ bool isect_elem<3>(const SceneView<3> &s, uint32_t i, const V<3> &o, const V<3> &d, float &t) {
+    const float4 *p = s.isect + 3 * i;
+    return isect_tri(o, d, __ldg(p), __ldg(p + 1), __ldg(p + 2), t);
+}
+
+// Conservative line / box tests against the 4 children of a node; bit k of the result is set
+// when child k's (padded) box meets the infinite line.
+__device__ __forceinline__ uint32_t node_hits(const SceneView<2> &s, uint32_t node, const V<2> &o, const V<2> &d, float c0, uint4 &child) {
+    const float4 *p = s.nodes + 5 * node;
+    const float4 lx = __ldg(p), ly = __ldg(p + 1), hx = __ldg(p + 2), hy = __ldg(p + 3);
+    const float4 cf = __ldg(p + 4);
+    child = make_uint4(__float_as_uint(cf.x), __float_as_uint(cf.y), __float_as_uint(cf.z), __float_as_uint(cf.w));
+    const float dx = d.v[0], dy = d.v[1];
+    // f(p) = dx p.y - dy p.x - c0 takes both signs over the box
+    const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, lys[4] = {ly.x, ly.y, ly.z, ly.w};
+    const float hxs[4] = {hx.x, hx.y, hx.z, hx.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float a1 = dx * lys[k], a2 = dx * hys[k];
+        const float b1 = dy * lxs[k], b2 = dy * hxs[k];
+        const float fmin_ = fminf(a1, a2) - fmaxf(b1, b2) - c0;
+        const float fmax_ = fmaxf(a1, a2) - fminf(b1, b2) - c0;
+        if (fmin_ <= 0.0f && fmax_ >= 0.0f) mask |= 1u << k;
+    }
+    return mask;
+}
+
+__device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t node, const V<3> &o, const V<3> &inv, float, uint4 &child) {
+    const float4 *p = s.nodes + 7 * node;
+    const float4 lx = __ldg(p), ly = __ldg(p + 1), lz = __ldg(p + 2);
+    const float4 hx = __ldg(p + 3), hy = __ldg(p + 4), hz = __ldg(p + 5);
+    const float4 cf = __ldg(p + 6);
+    child = make_uint4(__float_as_uint(cf.x), __float_as_uint(cf.y), __float_as_uint(cf.z), __float_as_uint(cf.w));
+    const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, lys[4] = {ly.x, ly.y, ly.z, ly.w}, lzs[4] = {lz.x, lz.y, lz.z, lz.w};
+    const float hxs[4] = {hx.x, hx.y, hx.z, hx.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float tx1 = (lxs[k] - o.v[0]) * inv.v[0], tx2 = (hxs[k] - o.v[0]) * inv.v[0];
+        const float ty1 = (lys[k] - o.v[1]) * inv.v[1], ty2 = (hys[k] - o.v[1]) * inv.v[1];
+        const float tz1 = (lzs[k] - o.v[2]) * inv.v[2], tz2 = (hzs[k] - o.v[2]) * inv.v[2];
+        const float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
+        const float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+        if (tn <= tf) mask |= 1u << k;
+    }
+    return mask;
+}
+
+// All hits of the infinite line o + t d, in storage order (depth-first, children in order, so
+// leaves come in increasing element order). Writes the first kHitBuffer element indices to hits
+// and returns the total count. On a stack overflow or runaway traversal it flags s.err and
+// returns what it has.
+template <int D>
+__device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D> &o, const V<D> &d, uint32_t *hits) {
+    uint32_t stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = 0u;  // root node
+    uint32_t count = 0;
+    V<D> aux;
+    float c0 = 0.0f;
+    if constexpr (D == 2) {
+        aux = d;
+        c0 = d.v[0] * o.v[1] - d.v[1] * o.v[0];
+    } else {
+        aux.v[0] = 1.0f / d.v[0]; aux.v[1] = 1.0f / d.v[1]; aux.v[2] = 1.0f / d.v[2];
+    }
+    uint32_t steps = 0;
+    while (sp > 0) {
+        if (++steps > s.traversal_limit) { atomicOr(s.err, kErrTraversalLimit); break; }
+        const uint32_t code = stack[--sp];
+        if (code & 0x80000000u) {
+            const uint32_t first = code & 0x0FFFFFFFu, cnt = ((code >> 28) & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; i++) {
+                float t;
+                if (isect_elem<D>(s, i, o, d, t)) {
+                    if (count < kHitBuffer) hits[count] = i;
+                    count++;
+                }
+            }
+        } else {
+            uint4 ch;
+            const uint32_t mask = node_hits(s, code, o, aux, c0, ch);
+            const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
+            if (sp + 4 > (int)kStackSize) { atomicOr(s.err, kErrStackOverflow); break; }
+#pragma unroll
+            for (int k = 3; k >= 0; k--)
+                if ((mask >> k) & 1u)
+                    if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
+        }
+    }
+    return count;
+}
+
+// ------------------------------------------------------------------------------------------
+// Boundary sampling queries (scene.cuh:441-622, 734-918).
+// ------------------------------------------------------------------------------------------
+template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
+    const float u1 = rng.uniform();
+    const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, s.n_elems, u1);
+    const Elem<D> e = load_elem<D>(s, idx);
+    BPoint<D> r;
+    if constexpr (D == 2) {
+        const float u2 = rng.uniform();
+        r.p.v[0] = interp2(e.v[0].v[0], e.v[1].v[0], u2);
+        r.p.v[1] = interp2(e.v[0].v[1], e.v[1].v[1], u2);
+        r.n = e.n;
+        r.angle = 0.5f;
+        r.bv = interp2(e.bv[0], e.bv[1], u2);
+        r.type = e.type;
+        r.alpha = interp2(e.alpha[0], e.alpha[1], u2);
+    } else {
+        const float u2 = rng.uniform();
+        const float u3 = rng.uniform();
+        const float sq = sqrtf(u2);
+        const float k1 = 1.0f - sq, k2 = sq * (1.0f - u3), k3 = u3 * sq;
+#pragma unroll
+        for (int i = 0; i < 3; i++) r.p.v[i] = interp3(e.v[0].v[i], e.v[1].v[i], e.v[2].v[i], k1, k2, k3);
+        r.n = e.n;
+        r.angle = 0.5f;
+        r.bv = interp3(e.bv[0], e.bv[1], e.bv[2], k1, k2, k3);
+        r.type = e.type;
+        r.alpha = interp3(e.alpha[0], e.alpha[1], e.alpha[2], k1, k2, k3);
+    }
+    inv_pdf = s.total_area;
+    return r;
+}
+
+template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(const SceneView<D> &s, PathRng &rng, const V<D> &x, uint32_t &m_out) {
+    V<D> dir;
+    if constexpr (D == 2) {
+        const float theta = rng.uniform();
+        sincospi_own(theta, &dir.v[0], &dir.v[1]);
+    } else {
+        dir.v[2] = rng.uniform();
+        const float phi = 2.0f * rng.uniform();
+        sincospi_own(phi, &dir.v[0], &dir.v[1]);
+        const float r = sqrtf(1.0f - dir.v[2] * dir.v[2]);
+        dir.v[0] = dir.v[0] * r;
+        dir.v[1] = dir.v[1] * r;
+    }
+    uint32_t hits[kHitBuffer];
+    uint32_t m = line_query<D>(s, x, dir, hits);
+    if (m == 0) {
+        BPoint<D> z = bp_zero<D>();
+        z.angle = 0.5f;
+        m_out = 0;
+        return z;
+    }
+    m = m < kHitBuffer ? m : kHitBuffer;
+    const float u = rng.uniform();
+    uint32_t k = (uint32_t)((float)m * u);
+    k = (m - 1) < k ? (m - 1) : k;
+    const uint32_t ei = hits[k];
+    const Elem<D> e = load_elem<D>(s, ei);
+    float t = 0.0f;
+    isect_elem<D>(s, ei, x, dir, t);
+    BPoint<D> r;
+#pragma unroll
+    for (int i = 0; i < D; i++) r.p.v[i] = x.v[i] + t * dir.v[i];
+    r.n = e.n;
+    r.angle = 0.5f;
+    r.type = e.type;
+    if constexpr (D == 2) {
+        const float tt = vnorm(vsub(r.p, e.v[0])) / e.area;
+        r.bv = interp2(e.bv[0], e.bv[1], tt);
+        r.alpha = interp2(e.alpha[0], e.alpha[1], tt);
+    } else {
+        // barycentric coordinates (scene.cuh:45-69)
+        const V<3> v0 = vsub(e.v[1], e.v[0]), v1 = vsub(e.v[2], e.v[0]), v2 = vsub(r.p, e.v[0]);
+        const float d00 = vdot(v0, v0), d01 = vdot(v0, v1), d11 = vdot(v1, v1);
+        const float d20 = vdot(v2, v0), d21 = vdot(v2, v1);
+        const float denom = d00 * d11 - d01 * d01;
+        const float L1 = (d11 * d20 - d01 * d21) / denom;
+        const float L2 = (d00 * d21 - d01 * d20) / denom;
+        const float L0 = 1.0f - (L1 + L2);
+        r.bv = L0 * e.bv[0] + L1 * e.bv[1] + L2 * e.bv[2];
+        r.alpha = L0 * e.alpha[0] + L1 * e.alpha[1] + L2 * e.alpha[2];
+    }
+    m_out = m;
+    return r;
+}
+
+template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection(const SceneView<D> &s, PathRng &rng, const V<D> &x, float &inv_pdf) {
+    uint32_t m;
+    const BPoint<D> r = sample_line_intersection2<D>(s, rng, x, m);
+    const V<D> rv = vsub(r.p, x);
+    const float cosv = fmax_ref(fabsf(vdot(vnormalized(rv), r.n)), kEps10);
+    if constexpr (D == 2) inv_pdf = (float)m * 0x1.921fb6p+1f * vnorm(rv) / cosv;
+    else inv_pdf = (float)m * 2.0f * 0x1.921fb6p+1f * vsqnorm(rv) / cosv;
+    return r;
+}
+
+template <int D> __device__ __forceinline__ BPoint<D> sample_boundary_value(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
+    const float u1 = rng.uniform();
+    const uint32_t idx = cdf_search(s.bv_cdf, s.bv_guide, s.bv_G, s.n_elems, u1);
+    const Elem<D> e = load_elem<D>(s, idx);
+    BPoint<D> r;
+    if constexpr (D == 2) {
+        const float u2 = rng.uniform();
+        const float ba = fabsf(e.bv[0]), bb = fabsf(e.bv[1]);
+        float t;
+        if (fabsf(ba - bb) < kEps10) t = u2;
+        else t = (-ba + sqrtf(ba * ba + u2 * (bb * bb - ba * ba))) / (bb - ba);
+        r.p.v[0] = interp2(e.v[0].v[0], e.v[1].v[0], t);
+        r.p.v[1] = interp2(e.v[0].v[1], e.v[1].v[1], t);
+        r.n = e.n;
+        r.angle = 0.5f;
+        r.bv = interp2(e.bv[0], e.bv[1], t);
+        r.type = e.type;
+        r.alpha = interp2(e.alpha[0], e.alpha[1], t);
+        inv_pdf = s.total_bv / (ba + t * (bb - ba));
+    } else {
+        const float pmf = idx == 0 ? __ldg(s.bv_cdf) : __ldg(s.bv_cdf + idx) - __ldg(s.bv_cdf + idx - 1);
+        const float u2 = rng.uniform();
+        const float u3 = rng.uniform();
+        const float sq = sqrtf(u2);
+        const float k1 = 1.0f - sq, k2 = sq * (1.0f - u3), k3 = u3 * sq;
+#pragma unroll
+        for (int i = 0; i < 3; i++) r.p.v[i] = interp3(e.v[0].v[i], e.v[1].v[i], e.v[2].v[i], k1, k2, k3);
+        r.n = e.n;
+        r.angle = 0.5f;
+        r.bv = interp3(e.bv[0], e.bv[1], e.bv[2], k1, k2, k3);
+        r.type = e.type;
+        r.alpha = interp3(e.alpha[0], e.alpha[1], e.alpha[2], k1, k2, k3);
+        inv_pdf = e.area / pmf;
+    }
+    return r;
+}
+
+template <int D> struct VSample {
+    V<D> p;
+    float value, inv_pdf;
+};
+
+// Source-value sampling of the volume cache (scene.cuh:100-120).
+template <int D> __device__ __forceinline__ VSample<D> sample_volume(const SceneView<D> &s, PathRng &rng) {
+    VSample<D> r;
+    const float u = rng.uniform();
+    const uint32_t idx = cdf_search(s.vol_cdf, s.vol_guide, s.vol_G, s.vol_n, u);
+    const uint32_t res = s.vol_res;
+    const float dx = s.vol_size / (float)res;
+    const uint32_t c[3] = {idx % res, (idx / res) % res, idx / (res * res)};
+#pragma unroll
+    for (int i = 0; i < D; i++) r.p.v[i] = ((float)c[i] + 0.5f) * dx - s.vol_size / 2.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const float uj = rng.uniform();
+        r.p.v[i] = r.p.v[i] + (uj - 0.5f) * s.vol_size / (float)res;
+    }
+    r.value = __ldg(s.vol_values + idx);
+    const float pdf = idx == 0 ? __ldg(s.vol_cdf) : __ldg(s.vol_cdf + idx) - __ldg(s.vol_cdf + idx - 1);
+    float cell = 1.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) cell = cell * (s.vol_size / (float)res);
+    r.inv_pdf = cell / pdf;
+    return r;
+}
+
+}  // namespace wobgb

@@ -1,0 +1,36 @@
+// Launch entry points shared between the C ABI (capi.cu) and the per-dimension kernel units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wobgb {
+
+template <int D> struct SceneView;
+struct WalkParams;
+
+// Boundary points of the boundary estimator (points.hpp:32-39), device pointers.
+struct BoundaryInput {
+    const float *p, *n, *angle, *bv;
+    const int32_t *type;
+    const float *alpha;  // may be null
+};
+
+cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                             double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                             cudaStream_t stream);
+cudaError_t launch_domain_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                             double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                             cudaStream_t stream);
+cudaError_t launch_boundary_2d(const SceneView<2> &s, const WalkParams &p, const BoundaryInput &bin,
+                               uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
+                               float *per_path, cudaStream_t stream);
+cudaError_t launch_boundary_3d(const SceneView<3> &s, const WalkParams &p, const BoundaryInput &bin,
+                               uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
+                               float *per_path, cudaStream_t stream);
+cudaError_t launch_line_query_2d(const SceneView<2> &s, const float *origins, const float *dirs, uint32_t n,
+                                 uint32_t *counts, uint32_t *hits, float *points, cudaStream_t stream);
+cudaError_t launch_line_query_3d(const SceneView<3> &s, const float *origins, const float *dirs, uint32_t n,
+                                 uint32_t *counts, uint32_t *hits, float *points, cudaStream_t stream);
+
+}  // namespace wobgb

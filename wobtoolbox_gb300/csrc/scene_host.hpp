@@ -1,0 +1,60 @@
+// Host-side scene construction for the GB300 WoB engine: validation, the 4-wide BVH, the element
+// storage order, the area and |g| CDFs and their guide tables, and the packed device records.
+//
+// Replaces wob::SceneHost (scene.cuh:264-326) and the lbvh build it wraps (scene.cuh:266).
+// All float arithmetic here must be built without contraction (-ffp-contract=off): the CDFs and
+// the precomputed intersection records are required to be bit-identical to what a plain IEEE
+// single-precision evaluation of the same formulas gives.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace wobgb {
+
+// BVH child codes. Internal children hold the node index (< 2^31). Leaves hold the first stored
+// element and the element count (1..kLeafMax) with the top bit set. kChildEmpty marks an unused
+// slot of a 4-wide node.
+constexpr uint32_t kLeafMax = 4;
+constexpr uint32_t kChildEmpty = 0xFFFFFFFFu;
+constexpr uint32_t kMaxElements = (1u << 28) - 8u;
+constexpr uint32_t kTraversalStack = 64;
+inline bool child_is_leaf(uint32_t c) { return (c & 0x80000000u) != 0u; }
+inline uint32_t leaf_first(uint32_t c) { return c & 0x0FFFFFFFu; }
+inline uint32_t leaf_count(uint32_t c) { return ((c >> 28) & 7u) + 1u; }
+inline uint32_t make_leaf(uint32_t first, uint32_t count) {
+    return 0x80000000u | ((count - 1u) << 28) | first;
+}
+
+// Packed record sizes in floats.
+inline int elem_record_floats(int dim) { return dim == 2 ? 12 : 20; }
+inline int node_record_floats(int dim) { return dim == 2 ? 20 : 28; }
+constexpr int kIsect3Floats = 12;
+
+struct HostScene {
+    int dim = 0;
+    uint32_t n = 0;
+    std::vector<uint32_t> order;           // order[i] = caller index of stored element i
+    std::vector<float> elems;              // n * elem_record_floats(dim)
+    std::vector<float> isect;              // 3D only: n * kIsect3Floats
+    std::vector<float> nodes;              // n_nodes * node_record_floats(dim)
+    std::vector<float> area_cdf, bv_cdf;   // n each
+    std::vector<uint32_t> area_guide, bv_guide;
+    float total_area = 0.0f, total_bv = 0.0f;
+    bool bv_valid = false;                 // |g| sampling defined (total |g| finite and > 0)
+    uint32_t n_nodes = 0, depth = 0;
+};
+
+// Returns "" on success, else a message. Arrays as documented for wob_scene_create.
+std::string build_host_scene(int dim, uint32_t n, const float *verts, const float *normals,
+                             const float *bvals, const float *alphas, const int32_t *types,
+                             HostScene &out);
+
+// Guide table of a nondecreasing CDF (see cdf_search in device_common.cuh).
+std::vector<uint32_t> build_guide(const std::vector<float> &cdf);
+
+// |f| CDF of a volume cache: prefix(|f|) / total in double, rounded to float; uniform if all zero.
+std::string build_volume_cdf(int dim, uint32_t res, const float *values, std::vector<float> &cdf);
+
+}  // namespace wobgb

@@ -1,0 +1,445 @@
+// The general WoB walk on the device: fundamental solutions, the three BIE models for interior and
+// exterior domains, and the backward / forward estimators with every sampling strategy of the
+// reference. The BIE model, domain and problem are run-time values (uniform across a launch);
+// the dimension is a template parameter.
+//
+// Restates equation_kernel.cuh:67-145, bie_models.cuh:53-590 and estimator.cuh:113-504.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace wobgb {
+
+struct WalkParams {
+    int bie, domain, estimator, problem;
+    uint32_t path_length, n_paths, n_resampling, n_volume;
+    float eps, fk;
+    uint64_t seed, path_offset;
+    uint32_t point_offset;
+};
+
+// ------------------------------------------------------------------------------------------
+// Fundamental solutions (equation_kernel.cuh:74-100 and 115-142).
+// ------------------------------------------------------------------------------------------
+template <int D> struct Green;
+template <> struct Green<2> {
+    float eps;
+    __device__ __forceinline__ float G(const V<2> &y, const V<2> &x) const {
+        return -0x1.45f306p-3f * log_own(fmax_ref(vnorm(vsub(y, x)), eps));
+    }
+    __device__ __forceinline__ V<2> dG_dx(const V<2> &y, const V<2> &x) const {
+        const V<2> r = vsub(y, x);
+        return vdiv(vscale(0x1.45f306p-3f, vnormalized(r)), fmax_ref(vnorm(r), eps));
+    }
+    __device__ __forceinline__ float dG_dny(const V<2> &y, const V<2> &x, const V<2> &ny) const {
+        const V<2> r = vsub(y, x);
+        return -0x1.45f306p-3f * vdot(vnormalized(r), ny) / fmax_ref(vnorm(r), eps);
+    }
+    __device__ __forceinline__ V<2> d2G_dxdny(const V<2> &y, const V<2> &x, const V<2> &ny) const {
+        const V<2> r = vsub(y, x);
+        const V<2> rh = vnormalized(r);
+        const float k = 1.0f / (0x1.921fb6p+2f * fmax_ref(vsqnorm(r), eps));
+        return vscale(k, vsub(ny, vscale(2.0f * vdot(rh, ny), rh)));
+    }
+};
+template <> struct Green<3> {
+    float eps;
+    __device__ __forceinline__ float G(const V<3> &y, const V<3> &x) const {
+        return 1.0f / (0x1.921fb6p+3f * fmax_ref(vnorm(vsub(y, x)), eps));
+    }
+    __device__ __forceinline__ V<3> dG_dx(const V<3> &y, const V<3> &x) const {
+        const V<3> r = vsub(y, x);
+        return vdiv(vscale(0x1.45f306p-4f, vnormalized(r)), fmax_ref(vsqnorm(r), eps));
+    }
+    __device__ __forceinline__ float dG_dny(const V<3> &y, const V<3> &x, const V<3> &ny) const {
+        const V<3> r = vsub(y, x);
+        return -0x1.45f306p-4f * vdot(vnormalized(r), ny) / fmax_ref(vsqnorm(r), eps);
+    }
+    __device__ __forceinline__ V<3> d2G_dxdny(const V<3> &y, const V<3> &x, const V<3> &ny) const {
+        const V<3> r = vsub(y, x);
+        const V<3> rh = vnormalized(r);
+        const float k = 1.0f / (0x1.921fb6p+3f * fmax_ref(vnorm(r) * vsqnorm(r), eps));
+        return vscale(k, vsub(ny, vscale(3.0f * vdot(rh, ny), rh)));
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// BIE models (bie_models.cuh:53-590); fbu may replace one point by the other (first-kind
+// roulette) exactly like the reference's by-reference arguments.
+// ------------------------------------------------------------------------------------------
+template <int D> struct Bie {
+    Green<D> K;
+    const SceneView<D> *s;
+    PathRng *rng;
+    int bie, domain;
+    float fk;
+    uint32_t nvs;
+
+    __device__ __forceinline__ float dtc() const { return domain == kInterior ? 1.0f : -1.0f; }
+    __device__ __forceinline__ float ift(float a) const { return domain == kInterior ? a : 1.0f - a; }
+
+    __device__ float vol_term(const BPoint<D> &b) const {
+        if (nvs == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(*s, *rng);
+        float r = 0.0f;
+        for (uint32_t i = 0; i < nvs; i++) {
+            if (b.type == kDirichlet) r = r + K.G(b.p, v.p) * v.value * v.inv_pdf;
+            else if (b.type == kNeumann) r = r + K.dG_dny(b.p, v.p, b.n) * v.value * v.inv_pdf;
+            else r = r + (K.dG_dny(b.p, v.p, b.n) + b.alpha * K.G(v.p, b.p)) * v.value * v.inv_pdf;
+        }
+        return r / (float)nvs;
+    }
+    __device__ float vol_init_boundary(const BPoint<D> &b) const {
+        if (nvs == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(*s, *rng);
+        float r = 0.0f;
+        for (uint32_t i = 0; i < nvs; i++) r = r - K.G(b.p, v.p) * v.value * v.inv_pdf;
+        return r / (float)nvs;
+    }
+    __device__ float vol_init_domain(const V<D> &x) const {
+        if (nvs == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(*s, *rng);
+        float r = 0.0f;
+        for (uint32_t i = 0; i < nvs; i++) r = r - K.G(v.p, x) * v.value * v.inv_pdf;
+        return r / (float)nvs;
+    }
+    __device__ V<D> vol_init_derivative(const V<D> &x) const {
+        if (nvs == 0) return vzero<D>();
+        const VSample<D> v = sample_volume<D>(*s, *rng);
+        V<D> r = vzero<D>();
+        for (uint32_t i = 0; i < nvs; i++) {
+            const V<D> g = K.dG_dx(v.p, x);
+#pragma unroll
+            for (int j = 0; j < D; j++) r.v[j] = r.v[j] - g.v[j] * v.value * v.inv_pdf;
+        }
+        return vdiv(r, (float)nvs);
+    }
+
+    __device__ float sdu(const V<D> &x, const BPoint<D> &y, float ip) const {
+        if (bie == kSingleLayer) return K.G(y.p, x) * ip;
+        if (bie == kDoubleLayer) return -K.dG_dny(y.p, x, y.n) * ip;
+        if (y.type == kDirichlet) return dtc() * ip * K.G(y.p, x);
+        if (y.type == kNeumann) return -dtc() * ip * K.dG_dny(y.p, x, y.n);
+        return -dtc() * ip * (K.dG_dny(y.p, x, y.n) + y.alpha * K.G(y.p, x));
+    }
+    __device__ float sdk(const V<D> &x, const BPoint<D> &y, float ip) const {
+        float r = vol_init_domain(x);
+        if (bie != kDirect) return r;
+        if (y.type == kDirichlet) {
+            const float k = -dtc() * ip * K.dG_dny(y.p, x, y.n);
+            r = r + k * (y.bv + vol_term(y));
+        } else {
+            const float k = dtc() * ip * K.G(y.p, x);
+            r = r + k * (y.bv + vol_term(y));
+        }
+        return r;
+    }
+    __device__ V<D> gdu(const V<D> &x, const BPoint<D> &y, float ip) const {
+        V<D> r;
+        if (bie == kSingleLayer) {
+            const V<D> g = K.dG_dx(y.p, x);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = g.v[i] * ip;
+            return r;
+        }
+        if (bie == kDoubleLayer) {
+            const V<D> g = K.d2G_dxdny(y.p, x, y.n);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = -g.v[i] * ip;
+            return r;
+        }
+        if (y.type == kDirichlet) {
+            const float c = dtc() * ip;
+            const V<D> g = K.dG_dx(y.p, x);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = c * g.v[i];
+            return r;
+        }
+        if (y.type == kNeumann) {
+            const float c = -dtc() * ip;
+            const V<D> g = K.d2G_dxdny(y.p, x, y.n);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = c * g.v[i];
+            return r;
+        }
+        const float c = -dtc() * ip;
+        const V<D> g1 = K.d2G_dxdny(y.p, x, y.n);
+        const V<D> g2 = K.dG_dx(y.p, x);
+#pragma unroll
+        for (int i = 0; i < D; i++) r.v[i] = c * (g1.v[i] + y.alpha * g2.v[i]);
+        return r;
+    }
+    __device__ V<D> gdk(const V<D> &x, const BPoint<D> &y, float ip) const {
+        V<D> r = vol_init_derivative(x);
+        if (bie != kDirect) return r;
+        if (y.type == kDirichlet) {
+            const float c = -dtc() * ip;
+            const V<D> g = K.d2G_dxdny(y.p, x, y.n);
+            const float sv = y.bv + vol_term(y);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = r.v[i] + c * g.v[i] * sv;
+        } else {
+            const float c = dtc() * ip;
+            const V<D> g = K.dG_dx(y.p, x);
+            const float sv = y.bv + vol_term(y);
+#pragma unroll
+            for (int i = 0; i < D; i++) r.v[i] = r.v[i] + c * g.v[i] * sv;
+        }
+        return r;
+    }
+    __device__ float sbu(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
+        if (bie == kDoubleLayer) return 0.0f;
+        if (x.type == kDirichlet) return 0.0f;
+        if (bie == kSingleLayer) return K.G(y.p, x.p) * ip;
+        if (y.type == kDirichlet) return dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
+        if (y.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+        return -dtc() / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
+    }
+    __device__ float sbk(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
+        if (bie == kDoubleLayer) return x.bv;
+        if (x.type == kDirichlet) return x.bv;
+        if (bie == kSingleLayer) return vol_init_boundary(x);
+        float r = vol_init_boundary(x);
+        if (y.type == kDirichlet) {
+            const float k = -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+            r = r + k * (y.bv + vol_term(y));
+        } else {
+            const float k = dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
+            r = r + k * (y.bv + vol_term(y));
+        }
+        return r;
+    }
+    __device__ float fbu(BPoint<D> &x, BPoint<D> &y, float ip, bool backward) const {
+        if (bie == kDoubleLayer) return dtc() / (1.0f - ift(x.angle)) * ip * K.dG_dny(y.p, x.p, y.n);
+        if (backward && x.type == kDirichlet) {
+            if (rng->uniform() * (1.0f + fk) < 1.0f) { y = x; return (1.0f + fk) * 1.0f; }
+            ip = ip * ((1.0f + fk) / fk);
+        } else if (!backward && y.type == kDirichlet) {
+            if (rng->uniform() * (1.0f + fk) < 1.0f) { x = y; return (1.0f + fk) * 1.0f; }
+            ip = ip * ((1.0f + fk) / fk);
+        }
+        if (bie == kSingleLayer) {
+            if (x.type == kDirichlet) return -2.0f * fk * ip * K.G(y.p, x.p);
+            if (x.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(x.p, y.p, x.n);
+            return -dtc() / ift(x.angle) * ip * (K.dG_dny(x.p, y.p, x.n) + x.alpha * K.G(y.p, x.p));
+        }
+        if (x.type == kDirichlet) {
+            if (y.type == kDirichlet) return -fk / ift(x.angle) * ip * K.G(y.p, x.p);
+            if (y.type == kNeumann) return fk / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+            return fk / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
+        }
+        if (y.type == kDirichlet) return dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
+        if (y.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+        return -dtc() / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
+    }
+    __device__ float fbk(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
+        if (bie == kDoubleLayer) return dtc() * 1.0f / (1.0f - ift(x.angle)) * (x.bv + vol_term(x));
+        if (bie == kSingleLayer) {
+            if (x.type == kDirichlet) return 2.0f * fk * (x.bv + vol_term(x));
+            return dtc() / ift(x.angle) * (x.bv + vol_term(x));
+        }
+        if (x.type == kDirichlet) {
+            const float sx = x.bv + vol_term(x);
+            if (y.type == kDirichlet) {
+                const float k = dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+                return dtc() * fk * (sx + k * (y.bv + vol_term(y)));
+            }
+            const float k = dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
+            return dtc() * fk * (sx - k * (y.bv + vol_term(y)));
+        }
+        if (y.type == kDirichlet) {
+            const float k = -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+            return k * (y.bv + vol_term(y));
+        }
+        const float k = dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
+        return k * (y.bv + vol_term(y));
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// Estimators (estimator.cuh:113-504).
+// ------------------------------------------------------------------------------------------
+template <int D> struct Walker {
+    const SceneView<D> &s;
+    const WalkParams &p;
+    PathRng rng;
+    Bie<D> bie;
+    uint32_t bounces;
+
+    __device__ __forceinline__ Walker(const SceneView<D> &s_, const WalkParams &p_, uint32_t stream, uint32_t point, uint64_t path)
+        : s(s_), p(p_), rng(p_.seed, stream, point, path), bounces(0) {
+        bie.K.eps = p.eps;
+        bie.s = &s;
+        bie.rng = &rng;
+        bie.bie = p.bie;
+        bie.domain = p.domain;
+        bie.fk = p.fk;
+        bie.nvs = p.n_volume;
+    }
+    __device__ __forceinline__ bool dl_dirichlet() const { return p.bie == kDoubleLayer && p.problem == kDirichletProblem; }
+    __device__ __forceinline__ bool direct_neumann() const { return p.bie == kDirect && p.problem == kNeumannProblem; }
+    __device__ __forceinline__ bool sl_neumann() const { return p.bie == kSingleLayer && p.problem == kNeumannProblem; }
+
+    __device__ float ris_target(int type, const BPoint<D> &yp, const BPoint<D> &c) const {
+        if (type == kDirichlet) return fabsf(bie.K.G(c.p, yp.p));
+        if (type == kNeumann) return fabsf(bie.K.dG_dny(yp.p, c.p, yp.n));
+        return fabsf(bie.K.dG_dny(yp.p, c.p, yp.n) + yp.alpha * bie.K.G(c.p, yp.p));
+    }
+    // Streaming RIS over K uniform candidates (scene.cuh:542-584, 847-889).
+    __device__ BPoint<D> sample_ris(const BPoint<D> &yp, float &inv_pdf) {
+        BPoint<D> y = bp_zero<D>();
+        float w_sum = 0.0f;
+        uint32_t M = 0;
+        for (uint32_t i = 0; i < p.n_resampling; i++) {
+            float ip;
+            const BPoint<D> xi = sample_uniform<D>(s, rng, ip);
+            const float wi = ris_target(yp.type, yp, xi) * ip;
+            w_sum = w_sum + wi;
+            M += 1;
+            if (rng.uniform() <= wi / w_sum) y = xi;
+        }
+        inv_pdf = w_sum / fmax_ref(ris_target(yp.type, yp, y) * (float)M, kEps10);
+        return y;
+    }
+
+    // compute_sample_unknown_boundary (estimator.cuh:232-357)
+    __device__ float unknown_boundary(const BPoint<D> &x) {
+        float contrib = 0.0f, w = 1.0f;
+        BPoint<D> y_prev = x;
+        BPoint<D> y = bp_zero<D>();
+        float ip = 0.0f;
+        const uint32_t L = p.path_length;
+        for (uint32_t m = 0; m < L; m++) {
+            bounces++;
+            if (m == L - 1) w = 0.5f * w;
+            if (dl_dirichlet()) {
+                y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
+                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                w = w * bie.fbu(y_prev, y, ip, true);
+                y_prev = y;
+            } else if (direct_neumann()) {
+                y = sample_boundary_value<D>(s, rng, ip);
+                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
+                w = w * bie.fbu(y_prev, y, ip, true);
+                y_prev = y;
+            } else if (p.bie == kSingleLayer) {
+                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                if (p.n_resampling == 1) y = sample_uniform<D>(s, rng, ip);
+                else y = sample_ris(y_prev, ip);
+                w = w * bie.fbu(y_prev, y, ip, true);
+                y_prev = y;
+            } else {
+                y = sample_uniform<D>(s, rng, ip);
+                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                y = sample_uniform<D>(s, rng, ip);
+                w = w * bie.fbu(y_prev, y, ip, true);
+                y_prev = y;
+            }
+            if (w == 0.0f) break;
+        }
+        return contrib;
+    }
+
+    // compute_sample_path_contribution_domain (estimator.cuh:154-191 backward, 405-454 forward)
+    __device__ void domain(const V<D> &x, float out[D + 1]) {
+        if (p.estimator == kBackward) {
+            BPoint<D> y, y1;
+            float ip, ip1;
+            if (dl_dirichlet()) {
+                y = sample_line_intersection<D>(s, rng, x, ip);
+                y1 = y;
+                ip1 = ip;
+            } else if (direct_neumann()) {
+                y = sample_line_intersection<D>(s, rng, x, ip);
+                y1 = sample_boundary_value<D>(s, rng, ip1);
+            } else {
+                y = sample_uniform<D>(s, rng, ip);
+                y1 = sample_uniform<D>(s, rng, ip1);
+            }
+            out[0] = bie.sdk(x, y1, ip1);
+            const V<D> g = bie.gdk(x, y1, ip1);
+#pragma unroll
+            for (int i = 0; i < D; i++) out[1 + i] = g.v[i];
+            const float mu = unknown_boundary(y);
+            out[0] = out[0] + mu * bie.sdu(x, y, ip);
+            const V<D> gu = bie.gdu(x, y, ip);
+#pragma unroll
+            for (int i = 0; i < D; i++) out[1 + i] = out[1 + i] + mu * gu.v[i];
+            return;
+        }
+        BPoint<D> y, y2;
+        float ip, ip2;
+        y = sample_uniform<D>(s, rng, ip);
+        out[0] = bie.sdk(x, y, ip);
+        const V<D> g = bie.gdk(x, y, ip);
+#pragma unroll
+        for (int i = 0; i < D; i++) out[1 + i] = g.v[i];
+        if (sl_neumann()) y = sample_boundary_value<D>(s, rng, ip);
+        else y = sample_uniform<D>(s, rng, ip);
+        y2 = sample_uniform<D>(s, rng, ip2);
+        float w = ip * bie.fbk(y, y2, ip2);
+        BPoint<D> y_prev;
+        const uint32_t L = p.path_length;
+        for (uint32_t m = 0; m < L; m++) {
+            bounces++;
+            if (m == L - 1) w = w * 0.5f;
+            out[0] = out[0] + w * bie.sdu(x, y, 1.0f);
+            const V<D> gu = bie.gdu(x, y, 1.0f);
+#pragma unroll
+            for (int i = 0; i < D; i++) out[1 + i] = out[1 + i] + w * gu.v[i];
+            y_prev = y;
+            if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
+            else y = sample_uniform<D>(s, rng, ip);
+            w = bie.fbu(y, y_prev, ip, false) * w;
+        }
+    }
+
+    // compute_sample_path_contribution_boundary (estimator.cuh:193-222 backward, 456-496 forward)
+    __device__ float boundary(const BPoint<D> &x) {
+        if (p.estimator == kBackward) {
+            BPoint<D> y, y1;
+            float ip, ip1;
+            if (dl_dirichlet()) {
+                y = sample_line_intersection<D>(s, rng, x.p, ip);
+                y1 = y;
+                ip1 = ip;
+            } else if (direct_neumann()) {
+                y = sample_line_intersection<D>(s, rng, x.p, ip);
+                y1 = sample_boundary_value<D>(s, rng, ip1);
+            } else {
+                y = sample_uniform<D>(s, rng, ip);
+                y1 = sample_uniform<D>(s, rng, ip1);
+            }
+            float r = bie.sbk(x, y1, ip1);
+            const float mu = unknown_boundary(y);
+            r = r + mu * bie.sbu(x, y, ip);
+            return r;
+        }
+        BPoint<D> y, y2;
+        float ip, ip2;
+        y = sample_uniform<D>(s, rng, ip);
+        float r = bie.sbk(x, y, ip);
+        if (sl_neumann()) y = sample_boundary_value<D>(s, rng, ip);
+        else y = sample_uniform<D>(s, rng, ip);
+        y2 = sample_uniform<D>(s, rng, ip2);
+        float w = ip * bie.fbk(y, y2, ip2);
+        BPoint<D> y_prev;
+        const uint32_t L = p.path_length;
+        for (uint32_t m = 0; m < L; m++) {
+            bounces++;
+            if (m == L - 1) w = w * 0.5f;
+            r = r + bie.sbu(x, y, 1.0f) * w;
+            y_prev = y;
+            if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
+            else y = sample_uniform<D>(s, rng, ip);
+            w = bie.fbu(y, y_prev, ip, false) * w;
+        }
+        return r;
+    }
+};
+
+constexpr uint32_t kStreamDomain = 0u;
+constexpr uint32_t kStreamBoundary = 1u;
+
+}  // namespace wobgb
