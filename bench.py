@@ -22,6 +22,7 @@ under oracle/ with all host threads, on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -268,6 +269,10 @@ def run_ours(args):
     inside = (crossings % 2 == 1).cpu().numpy()
     del hits, hp
     pts = np.ascontiguousarray(cand[inside])
+    paths = PATHS
+    if args.small:  # profiling case: every 16th point, 512 paths
+        pts = np.ascontiguousarray(pts[::16])
+        paths = 512
     n_pts = len(pts)
     d_pts = torch.from_numpy(pts).to(dev)
     d_sum = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
@@ -275,12 +280,11 @@ def run_ours(args):
     d_b = torch.zeros(1, dtype=torch.int64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream()
-    p = params()
+    p = dataclasses.replace(params(), num_sample_paths=paths)
     base_offset = rank * (1 << 40)
-    import dataclasses
 
     def step(k, sum_buf=d_sum, sq_buf=d_sq):
-        scene.solve_domain(dataclasses.replace(p, path_offset=base_offset + k * PATHS), d_pts, n_pts, sum_buf,
+        scene.solve_domain(dataclasses.replace(p, path_offset=base_offset + k * paths), d_pts, n_pts, sum_buf,
                            sq_buf, d_b, stream)
 
     for w in range(args.warmup):
@@ -312,7 +316,7 @@ def run_ours(args):
 
     # accuracy after all timed steps (args.steps * 4096 paths per point)
     s = d_sum.cpu().numpy()
-    n_paths_total = args.steps * PATHS
+    n_paths_total = args.steps * paths
     u = s[:, 0] / n_paths_total
     rmse = float(np.sqrt(np.mean((u - exact(pts, sc)) ** 2)))
 
@@ -333,7 +337,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     b0 = bb.value
     for k in range(e2e_steps):
-        cp.path_offset = base_offset + (1 << 30) + (k + 1) * PATHS
+        cp.path_offset = base_offset + (1 << 30) + (k + 1) * paths
         wob.check(lib.wob_solve_domain_host(scene.handle, C.byref(cp), pts_pinned.data_ptr(), n_pts,
                                             h_sum.ctypes.data, h_sq.ctypes.data, C.byref(bb)))
     e2e_local = time.perf_counter() - t0
@@ -359,7 +363,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "triangles": int(len(sc["verts"])), "points": n_pts,
-                       "paths_per_point_per_step": PATHS, "path_length": PATH_LENGTH,
+                       "paths_per_point_per_step": paths, "path_length": PATH_LENGTH,
                        "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
                        "rmse_u_vs_exact": rmse, "paths_per_point_total": n_paths_total,
                        "parallelism": f"replicas x{world}, points x independent path streams"},
@@ -402,6 +406,7 @@ def main():
     ap.add_argument("--cpu-paths", type=int, default=PATHS)
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

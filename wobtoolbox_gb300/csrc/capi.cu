@@ -71,17 +71,17 @@ struct wob_scene_s {
         v.isect = (const float4 *)isect.ptr;
         v.nodes = (const float4 *)nodes.ptr;
         v.area_cdf = (const float *)area_cdf.ptr;
-        v.area_guide = (const uint32_t *)area_guide.ptr;
+        v.area_guide = (const uint4 *)area_guide.ptr;
         v.bv_cdf = (const float *)bv_cdf.ptr;
-        v.bv_guide = (const uint32_t *)bv_guide.ptr;
+        v.bv_guide = (const uint4 *)bv_guide.ptr;
         v.vol_values = (const float *)vol_values.ptr;
         v.vol_cdf = (const float *)vol_cdf.ptr;
-        v.vol_guide = (const uint32_t *)vol_guide.ptr;
+        v.vol_guide = (const uint4 *)vol_guide.ptr;
         v.err = (uint32_t *)err.ptr;
         v.n_elems = host.n;
         v.n_nodes = host.n_nodes;
-        v.area_G = (uint32_t)host.area_guide.size();
-        v.bv_G = (uint32_t)host.bv_guide.size();
+        v.area_G = (uint32_t)(host.area_guide.size() / 4);
+        v.bv_G = (uint32_t)(host.bv_guide.size() / 4);
         v.vol_n = vol_n;
         v.vol_G = vol_G;
         v.vol_res = vol_res;
@@ -266,7 +266,7 @@ int wob_scene_set_volume_cache(wob_scene s, uint32_t grid_res, float domain_size
     s->has_volume = true;
     s->vol_res = grid_res;
     s->vol_n = (uint32_t)n;
-    s->vol_G = (uint32_t)guide.size();
+    s->vol_G = (uint32_t)(guide.size() / 4);
     s->vol_size = domain_size;
     return WOB_OK;
 }

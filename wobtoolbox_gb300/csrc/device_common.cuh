@@ -175,12 +175,12 @@ template <int D> struct SceneView {
     const float4 *__restrict__ isect;   // D==3: 3 float4 / element (a, a-b, a-c, (a-b)x(a-c))
     const float4 *__restrict__ nodes;   // D==2: 5 float4 / node, D==3: 7 float4
     const float *__restrict__ area_cdf;
-    const uint32_t *__restrict__ area_guide;
+    const uint4 *__restrict__ area_guide;
     const float *__restrict__ bv_cdf;
-    const uint32_t *__restrict__ bv_guide;
+    const uint4 *__restrict__ bv_guide;
     const float *__restrict__ vol_values;
     const float *__restrict__ vol_cdf;
-    const uint32_t *__restrict__ vol_guide;
+    const uint4 *__restrict__ vol_guide;
     uint32_t *err;                       // device error word (kErr* bits)
     uint32_t n_elems, n_nodes, area_G, bv_G;
     uint32_t vol_n, vol_G, vol_res, traversal_limit;
@@ -219,15 +219,23 @@ template <> __device__ __forceinline__ Elem<3> load_elem<3>(const SceneView<3> &
 }
 
 // First i in [0, n-1] with key <= cdf[i], else n-1: the reference's binary_search
-// (scene.cuh:30-43), started from a guide table. guide[j] is the first index whose CDF value
-// reaches (j - 1/2)/G, so for j = floor(key G) the answer lies in [guide[j], guide[j+2]]
-// (n-1 when j+2 >= G); the bisection below runs on that sub-range only.
-__device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, const uint32_t *__restrict__ guide,
-                                               uint32_t G, uint32_t n, float key) {
+// (scene.cuh:30-43), started from a guide table. Entry j of the table holds lo = the first index
+// whose CDF value reaches (j - 1/2)/G, hi = the lo of entry j + 2 (n - 1 for the last two) and
+// the CDF values at lo and lo + 1. For j = floor(key G) every index below lo has a CDF value
+// under (j - 1/2)/G < key and cdf[hi] >= (j + 3/2)/G > key, so the answer lies in [lo, hi]; the
+// two stored values settle it with one 16-byte load in almost every case, the bisection below
+// covers the rest of the sub-range.
+__device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, const uint4 *__restrict__ guide,
+                                               uint32_t G, float key) {
     uint32_t j = (uint32_t)(key * (float)G);
     if (j >= G) j = G - 1;
-    uint32_t low = __ldg(guide + j);
-    uint32_t high = (j + 2 < G) ? __ldg(guide + j + 2) : n - 1;
+    const uint4 g = __ldg(guide + j);
+    const uint32_t lo = g.x, hi = g.y;
+    if (lo >= hi) return hi;
+    if (key <= __uint_as_float(g.z)) return lo;
+    if (lo + 1 == hi) return hi;
+    if (key <= __uint_as_float(g.w)) return lo + 1;
+    uint32_t low = lo + 2, high = hi;
     while (low < high) {
         const uint32_t mid = (high + low) / 2;
         if (key <= __ldg(cdf + mid)) high = mid;
@@ -395,7 +403,7 @@ __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D>
 // ------------------------------------------------------------------------------------------
 template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
     const float u1 = rng.uniform();
-    const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, s.n_elems, u1);
+    const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, u1);
     const Elem<D> e = load_elem<D>(s, idx);
     BPoint<D> r;
     if constexpr (D == 2) {
@@ -491,7 +499,7 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection(c
 
 template <int D> __device__ __forceinline__ BPoint<D> sample_boundary_value(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
     const float u1 = rng.uniform();
-    const uint32_t idx = cdf_search(s.bv_cdf, s.bv_guide, s.bv_G, s.n_elems, u1);
+    const uint32_t idx = cdf_search(s.bv_cdf, s.bv_guide, s.bv_G, u1);
     const Elem<D> e = load_elem<D>(s, idx);
     BPoint<D> r;
     if constexpr (D == 2) {
@@ -535,7 +543,7 @@ template <int D> struct VSample {
 template <int D> __device__ __forceinline__ VSample<D> sample_volume(const SceneView<D> &s, PathRng &rng) {
     VSample<D> r;
     const float u = rng.uniform();
-    const uint32_t idx = cdf_search(s.vol_cdf, s.vol_guide, s.vol_G, s.vol_n, u);
+    const uint32_t idx = cdf_search(s.vol_cdf, s.vol_guide, s.vol_G, u);
     const uint32_t res = s.vol_res;
     const float dx = s.vol_size / (float)res;
     const uint32_t c[3] = {idx % res, (idx / res) % res, idx / (res * res)};

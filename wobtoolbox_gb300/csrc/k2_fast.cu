@@ -1,0 +1,7 @@
+// 2D specialisations: double-layer Dirichlet with line-intersection sampling; direct Neumann.
+#include "kernels.cuh"
+
+namespace wobgb {
+template cudaError_t launch_domain_variant<2, kDoubleLayer, kStratLineIntersection, false>(const SceneView<2> &, const WalkParams &, const float *, uint32_t, double *, double *, unsigned long long *, float *, cudaStream_t);
+template cudaError_t launch_domain_variant<2, kDirect, kStratDirectNeumann, false>(const SceneView<2> &, const WalkParams &, const float *, uint32_t, double *, double *, unsigned long long *, float *, cudaStream_t);
+}  // namespace wobgb

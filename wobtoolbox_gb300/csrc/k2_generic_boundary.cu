@@ -1,0 +1,6 @@
+// 2D general boundary walk (run-time BIE model and strategy).
+#include "kernels.cuh"
+
+namespace wobgb {
+template cudaError_t launch_boundary_variant<2, -1, kStratRuntime, true>(const SceneView<2> &, const WalkParams &, const BoundaryInput &, uint32_t, double *, double *, unsigned long long *, float *, cudaStream_t);
+}  // namespace wobgb

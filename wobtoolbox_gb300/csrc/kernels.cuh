@@ -26,7 +26,7 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
-template <int D, bool kPerPath>
+template <int D, int kBie, int kStrat, bool kVol, bool kPerPath>
 __global__ void __launch_bounds__(kBlock) domain_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                         uint32_t n_points, double *__restrict__ sum,
                                                         double *__restrict__ sumsq,
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kBlock) domain_kernel(SceneView<D> s, WalkPara
             V<D> x;
 #pragma unroll
             for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)pt * D + i);
-            Walker<D> w(s, p, kStreamDomain, p.point_offset + pt, p.path_offset + path);
+            Walker<D, kBie, kStrat, kVol> w(s, p, kStreamDomain, p.point_offset + pt, p.path_offset + path);
             w.domain(x, out);
             my_bounces += w.bounces;
             if (kPerPath) {
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kBlock) domain_kernel(SceneView<D> s, WalkPara
     }
 }
 
-template <int D, bool kPerPath>
+template <int D, int kBie, int kStrat, bool kVol, bool kPerPath>
 __global__ void __launch_bounds__(kBlock) boundary_kernel(SceneView<D> s, WalkParams p, BoundaryInput bin,
                                                           uint32_t n_points, double *__restrict__ sum,
                                                           double *__restrict__ sumsq,
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kBlock) boundary_kernel(SceneView<D> s, WalkPa
             x.bv = __ldg(bin.bv + pt);
             x.type = __ldg(bin.type + pt);
             x.alpha = bin.alpha ? __ldg(bin.alpha + pt) : 0.0f;
-            Walker<D> w(s, p, kStreamBoundary, p.point_offset + pt, p.path_offset + path);
+            Walker<D, kBie, kStrat, kVol> w(s, p, kStreamBoundary, p.point_offset + pt, p.path_offset + path);
             out = w.boundary(x);
             my_bounces += w.bounces;
             if (kPerPath) per_path[(size_t)pt * p.n_paths + path] = out;
@@ -160,10 +160,9 @@ __global__ void __launch_bounds__(kBlock) line_query_kernel(SceneView<D> s, cons
 
 template <class K>
 inline int persistent_grid(K kernel, uint64_t work_warps) {
-    static int sm_count = 0;
-    int dev = 0;
+    int dev = 0, sm_count = 0;
     cudaGetDevice(&dev);
-    if (sm_count == 0) cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
     if (per_sm < 1) per_sm = 1;
@@ -174,32 +173,32 @@ inline int persistent_grid(K kernel, uint64_t work_warps) {
     return (int)g;
 }
 
-template <int D>
-cudaError_t launch_domain_impl(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
-                               double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
-                               cudaStream_t stream) {
+template <int D, int kBie, int kStrat, bool kVol>
+cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                  double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                  cudaStream_t stream) {
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
     if (per_path) {
-        const int g = persistent_grid(domain_kernel<D, true>, units);
-        domain_kernel<D, true><<<g, kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);
+        auto k = domain_kernel<D, kBie, kStrat, kVol, true>;
+        k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);
     } else {
-        const int g = persistent_grid(domain_kernel<D, false>, units);
-        domain_kernel<D, false><<<g, kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, nullptr);
+        auto k = domain_kernel<D, kBie, kStrat, kVol, false>;
+        k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, nullptr);
     }
     return cudaGetLastError();
 }
 
-template <int D>
-cudaError_t launch_boundary_impl(const SceneView<D> &s, const WalkParams &p, const BoundaryInput &bin,
-                                 uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
-                                 float *per_path, cudaStream_t stream) {
+template <int D, int kBie, int kStrat, bool kVol>
+cudaError_t launch_boundary_variant(const SceneView<D> &s, const WalkParams &p, const BoundaryInput &bin,
+                                    uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
+                                    float *per_path, cudaStream_t stream) {
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
     if (per_path) {
-        const int g = persistent_grid(boundary_kernel<D, true>, units);
-        boundary_kernel<D, true><<<g, kBlock, 0, stream>>>(s, p, bin, n_points, sum, sumsq, bounces, per_path);
+        auto k = boundary_kernel<D, kBie, kStrat, kVol, true>;
+        k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, bin, n_points, sum, sumsq, bounces, per_path);
     } else {
-        const int g = persistent_grid(boundary_kernel<D, false>, units);
-        boundary_kernel<D, false><<<g, kBlock, 0, stream>>>(s, p, bin, n_points, sum, sumsq, bounces, nullptr);
+        auto k = boundary_kernel<D, kBie, kStrat, kVol, false>;
+        k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, bin, n_points, sum, sumsq, bounces, nullptr);
     }
     return cudaGetLastError();
 }

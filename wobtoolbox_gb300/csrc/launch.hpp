@@ -16,6 +16,21 @@ struct BoundaryInput {
     const float *alpha;  // may be null
 };
 
+// Variants of the walk kernels: kBie / kStrat fix the BIE model and sampling strategy at compile
+// time (-1 = run-time), kVol = false drops the source term. Instantiated in the k*_*.cu units.
+template <int D, int kBie, int kStrat, bool kVol>
+cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                  double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                  cudaStream_t stream);
+template <int D, int kBie, int kStrat, bool kVol>
+cudaError_t launch_boundary_variant(const SceneView<D> &s, const WalkParams &p, const BoundaryInput &bin,
+                                    uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
+                                    float *per_path, cudaStream_t stream);
+template <int D>
+cudaError_t launch_line_query_impl(const SceneView<D> &s, const float *origins, const float *dirs, uint32_t n,
+                                   uint32_t *counts, uint32_t *hits, float *points, cudaStream_t stream);
+
+// Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                              double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                              cudaStream_t stream);

@@ -146,14 +146,23 @@ std::vector<uint32_t> build_guide(const std::vector<float> &cdf) {
     const uint32_t n = (uint32_t)cdf.size();
     uint32_t G = std::min<uint32_t>(n, 1u << 22);
     if (G == 0) G = 1;
-    std::vector<uint32_t> guide(G);
+    std::vector<uint32_t> first(G);
     uint32_t i = 0;
     for (uint32_t j = 0; j < G; j++) {
         const double thr = ((double)j - 0.5) / (double)G;
         while (i + 1 < n && (double)cdf[i] < thr) i++;
-        guide[j] = i;
+        first[j] = i;
     }
-    return guide;
+    std::vector<uint32_t> rec(4 * (size_t)G);
+    for (uint32_t j = 0; j < G; j++) {
+        const uint32_t lo = first[j];
+        const uint32_t hi = (j + 2 < G) ? first[j + 2] : (n ? n - 1 : 0);
+        rec[4 * (size_t)j + 0] = lo;
+        rec[4 * (size_t)j + 1] = hi;
+        rec[4 * (size_t)j + 2] = n ? f2u(cdf[lo]) : 0u;
+        rec[4 * (size_t)j + 3] = n ? f2u(cdf[std::min(lo + 1, n - 1)]) : 0u;
+    }
+    return rec;
 }
 
 std::string build_volume_cdf(int dim, uint32_t res, const float *values, std::vector<float> &cdf) {
@@ -308,8 +317,7 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
     kahan_cdf(bvw, out.bv_cdf, out.total_bv);
     out.bv_valid = out.total_bv > 0.0f && std::isfinite(out.total_bv);
     if (out.bv_valid) out.bv_guide = build_guide(out.bv_cdf);
-    else out.bv_guide.assign(1, 0u);
-    (void)f2u;
+    else out.bv_guide.assign(4, 0u);
     return "";
 }
 

@@ -40,7 +40,7 @@ struct HostScene {
     std::vector<float> isect;              // 3D only: n * kIsect3Floats
     std::vector<float> nodes;              // n_nodes * node_record_floats(dim)
     std::vector<float> area_cdf, bv_cdf;   // n each
-    std::vector<uint32_t> area_guide, bv_guide;
+    std::vector<uint32_t> area_guide, bv_guide;  // packed guide records (4 words each)
     float total_area = 0.0f, total_bv = 0.0f;
     bool bv_valid = false;                 // |g| sampling defined (total |g| finite and > 0)
     uint32_t n_nodes = 0, depth = 0;
@@ -51,7 +51,10 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
                              const float *bvals, const float *alphas, const int32_t *types,
                              HostScene &out);
 
-// Guide table of a nondecreasing CDF (see cdf_search in device_common.cuh).
+// Guide table of a nondecreasing CDF with G = min(n, 2^22) entries of 4 words each:
+// {lo, hi, bits(cdf[lo]), bits(cdf[lo + 1])}, where lo is the first index whose CDF value reaches
+// (j - 1/2)/G and hi the lo of entry j + 2 (n - 1 for the last two). See cdf_search in
+// device_common.cuh for why the answer for a key in bin j lies in [lo, hi].
 std::vector<uint32_t> build_guide(const std::vector<float> &cdf);
 
 // |f| CDF of a volume cache: prefix(|f|) / total in double, rounded to float; uniform if all zero.

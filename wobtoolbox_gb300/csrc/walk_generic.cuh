@@ -67,64 +67,102 @@ template <> struct Green<3> {
 // BIE models (bie_models.cuh:53-590); fbu may replace one point by the other (first-kind
 // roulette) exactly like the reference's by-reference arguments.
 // ------------------------------------------------------------------------------------------
-template <int D> struct Bie {
+// The BIE models (bie_models.cuh:53-590) are member functions of the walker below: kBie >= 0
+// fixes the model at compile time (-1: run-time value), kVol = false drops the source-term code.
+// fbu may replace one point by the other (first-kind roulette) exactly like the reference's
+// by-reference arguments.
+
+// ------------------------------------------------------------------------------------------
+// Estimators (estimator.cuh:113-504).
+// ------------------------------------------------------------------------------------------
+// Sampling strategies of the estimators (the if-constexpr chains of estimator.cuh:158-168, 255-347,
+// 423-427, 445-448). kStrat fixes one at compile time; kStratRuntime picks it from the parameters.
+enum : int {
+    kStratRuntime = -1,
+    kStratLineIntersection = 0,  // backward, double layer + Dirichlet
+    kStratDirectNeumann = 1,     // backward, direct + Neumann
+    kStratSingleLayer = 2,       // backward, single layer (uniform or RIS)
+    kStratUniform = 3,           // backward, every other case: two uniform samples per bounce
+    kStratFwdSlNeumann = 4,      // forward, single layer + Neumann
+    kStratFwdUniform = 5         // forward, every other case
+};
+
+__host__ __device__ __forceinline__ int strategy_of(int bie, int est, int problem) {
+    if (est == kBackward) {
+        if (bie == kDoubleLayer && problem == kDirichletProblem) return kStratLineIntersection;
+        if (bie == kDirect && problem == kNeumannProblem) return kStratDirectNeumann;
+        if (bie == kSingleLayer) return kStratSingleLayer;
+        return kStratUniform;
+    }
+    return (bie == kSingleLayer && problem == kNeumannProblem) ? kStratFwdSlNeumann : kStratFwdUniform;
+}
+
+// The scene view and parameters are held by value: a kernel parameter whose address is taken
+// is copied to local memory, a by-value copy stays in registers / the parameter bank.
+template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> struct Walker {
+    const SceneView<D> s;
+    const WalkParams p;
+    PathRng rng;
     Green<D> K;
-    const SceneView<D> *s;
-    PathRng *rng;
-    int bie, domain;
-    float fk;
-    uint32_t nvs;
+    uint32_t bounces;
 
-    __device__ __forceinline__ float dtc() const { return domain == kInterior ? 1.0f : -1.0f; }
-    __device__ __forceinline__ float ift(float a) const { return domain == kInterior ? a : 1.0f - a; }
+    __device__ __forceinline__ Walker(const SceneView<D> &s_, const WalkParams &p_, uint32_t stream, uint32_t point, uint64_t path)
+        : s(s_), p(p_), rng(p_.seed, stream, point, path), bounces(0) {
+        K.eps = p.eps;
+    }
 
-    __device__ float vol_term(const BPoint<D> &b) const {
-        if (nvs == 0) return 0.0f;
-        const VSample<D> v = sample_volume<D>(*s, *rng);
+    // ---------------- BIE models
+    __device__ __forceinline__ int model() const { return kBie >= 0 ? kBie : p.bie; }
+    __device__ __forceinline__ float dtc() const { return p.domain == kInterior ? 1.0f : -1.0f; }
+    __device__ __forceinline__ float ift(float a) const { return p.domain == kInterior ? a : 1.0f - a; }
+
+    __device__ __forceinline__ float vol_term(const BPoint<D> &b) {
+        if (!kVol || p.n_volume == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(s, rng);
         float r = 0.0f;
-        for (uint32_t i = 0; i < nvs; i++) {
+        for (uint32_t i = 0; i < p.n_volume; i++) {
             if (b.type == kDirichlet) r = r + K.G(b.p, v.p) * v.value * v.inv_pdf;
             else if (b.type == kNeumann) r = r + K.dG_dny(b.p, v.p, b.n) * v.value * v.inv_pdf;
             else r = r + (K.dG_dny(b.p, v.p, b.n) + b.alpha * K.G(v.p, b.p)) * v.value * v.inv_pdf;
         }
-        return r / (float)nvs;
+        return r / (float)p.n_volume;
     }
-    __device__ float vol_init_boundary(const BPoint<D> &b) const {
-        if (nvs == 0) return 0.0f;
-        const VSample<D> v = sample_volume<D>(*s, *rng);
+    __device__ __forceinline__ float vol_init_boundary(const BPoint<D> &b) {
+        if (!kVol || p.n_volume == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(s, rng);
         float r = 0.0f;
-        for (uint32_t i = 0; i < nvs; i++) r = r - K.G(b.p, v.p) * v.value * v.inv_pdf;
-        return r / (float)nvs;
+        for (uint32_t i = 0; i < p.n_volume; i++) r = r - K.G(b.p, v.p) * v.value * v.inv_pdf;
+        return r / (float)p.n_volume;
     }
-    __device__ float vol_init_domain(const V<D> &x) const {
-        if (nvs == 0) return 0.0f;
-        const VSample<D> v = sample_volume<D>(*s, *rng);
+    __device__ __forceinline__ float vol_init_domain(const V<D> &x) {
+        if (!kVol || p.n_volume == 0) return 0.0f;
+        const VSample<D> v = sample_volume<D>(s, rng);
         float r = 0.0f;
-        for (uint32_t i = 0; i < nvs; i++) r = r - K.G(v.p, x) * v.value * v.inv_pdf;
-        return r / (float)nvs;
+        for (uint32_t i = 0; i < p.n_volume; i++) r = r - K.G(v.p, x) * v.value * v.inv_pdf;
+        return r / (float)p.n_volume;
     }
-    __device__ V<D> vol_init_derivative(const V<D> &x) const {
-        if (nvs == 0) return vzero<D>();
-        const VSample<D> v = sample_volume<D>(*s, *rng);
+    __device__ __forceinline__ V<D> vol_init_derivative(const V<D> &x) {
+        if (!kVol || p.n_volume == 0) return vzero<D>();
+        const VSample<D> v = sample_volume<D>(s, rng);
         V<D> r = vzero<D>();
-        for (uint32_t i = 0; i < nvs; i++) {
+        for (uint32_t i = 0; i < p.n_volume; i++) {
             const V<D> g = K.dG_dx(v.p, x);
 #pragma unroll
             for (int j = 0; j < D; j++) r.v[j] = r.v[j] - g.v[j] * v.value * v.inv_pdf;
         }
-        return vdiv(r, (float)nvs);
+        return vdiv(r, (float)p.n_volume);
     }
 
-    __device__ float sdu(const V<D> &x, const BPoint<D> &y, float ip) const {
-        if (bie == kSingleLayer) return K.G(y.p, x) * ip;
-        if (bie == kDoubleLayer) return -K.dG_dny(y.p, x, y.n) * ip;
+    __device__ __forceinline__ float sdu(const V<D> &x, const BPoint<D> &y, float ip) {
+        if (model() == kSingleLayer) return K.G(y.p, x) * ip;
+        if (model() == kDoubleLayer) return -K.dG_dny(y.p, x, y.n) * ip;
         if (y.type == kDirichlet) return dtc() * ip * K.G(y.p, x);
         if (y.type == kNeumann) return -dtc() * ip * K.dG_dny(y.p, x, y.n);
         return -dtc() * ip * (K.dG_dny(y.p, x, y.n) + y.alpha * K.G(y.p, x));
     }
-    __device__ float sdk(const V<D> &x, const BPoint<D> &y, float ip) const {
+    __device__ __forceinline__ float sdk(const V<D> &x, const BPoint<D> &y, float ip) {
         float r = vol_init_domain(x);
-        if (bie != kDirect) return r;
+        if (model() != kDirect) return r;
         if (y.type == kDirichlet) {
             const float k = -dtc() * ip * K.dG_dny(y.p, x, y.n);
             r = r + k * (y.bv + vol_term(y));
@@ -134,15 +172,15 @@ template <int D> struct Bie {
         }
         return r;
     }
-    __device__ V<D> gdu(const V<D> &x, const BPoint<D> &y, float ip) const {
+    __device__ __forceinline__ V<D> gdu(const V<D> &x, const BPoint<D> &y, float ip) {
         V<D> r;
-        if (bie == kSingleLayer) {
+        if (model() == kSingleLayer) {
             const V<D> g = K.dG_dx(y.p, x);
 #pragma unroll
             for (int i = 0; i < D; i++) r.v[i] = g.v[i] * ip;
             return r;
         }
-        if (bie == kDoubleLayer) {
+        if (model() == kDoubleLayer) {
             const V<D> g = K.d2G_dxdny(y.p, x, y.n);
 #pragma unroll
             for (int i = 0; i < D; i++) r.v[i] = -g.v[i] * ip;
@@ -169,9 +207,9 @@ template <int D> struct Bie {
         for (int i = 0; i < D; i++) r.v[i] = c * (g1.v[i] + y.alpha * g2.v[i]);
         return r;
     }
-    __device__ V<D> gdk(const V<D> &x, const BPoint<D> &y, float ip) const {
+    __device__ __forceinline__ V<D> gdk(const V<D> &x, const BPoint<D> &y, float ip) {
         V<D> r = vol_init_derivative(x);
-        if (bie != kDirect) return r;
+        if (model() != kDirect) return r;
         if (y.type == kDirichlet) {
             const float c = -dtc() * ip;
             const V<D> g = K.d2G_dxdny(y.p, x, y.n);
@@ -187,18 +225,18 @@ template <int D> struct Bie {
         }
         return r;
     }
-    __device__ float sbu(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
-        if (bie == kDoubleLayer) return 0.0f;
+    __device__ __forceinline__ float sbu(const BPoint<D> &x, const BPoint<D> &y, float ip) {
+        if (model() == kDoubleLayer) return 0.0f;
         if (x.type == kDirichlet) return 0.0f;
-        if (bie == kSingleLayer) return K.G(y.p, x.p) * ip;
+        if (model() == kSingleLayer) return K.G(y.p, x.p) * ip;
         if (y.type == kDirichlet) return dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
         if (y.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
         return -dtc() / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
     }
-    __device__ float sbk(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
-        if (bie == kDoubleLayer) return x.bv;
+    __device__ __forceinline__ float sbk(const BPoint<D> &x, const BPoint<D> &y, float ip) {
+        if (model() == kDoubleLayer) return x.bv;
         if (x.type == kDirichlet) return x.bv;
-        if (bie == kSingleLayer) return vol_init_boundary(x);
+        if (model() == kSingleLayer) return vol_init_boundary(x);
         float r = vol_init_boundary(x);
         if (y.type == kDirichlet) {
             const float k = -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
@@ -209,43 +247,43 @@ template <int D> struct Bie {
         }
         return r;
     }
-    __device__ float fbu(BPoint<D> &x, BPoint<D> &y, float ip, bool backward) const {
-        if (bie == kDoubleLayer) return dtc() / (1.0f - ift(x.angle)) * ip * K.dG_dny(y.p, x.p, y.n);
+    __device__ __forceinline__ float fbu(BPoint<D> &x, BPoint<D> &y, float ip, bool backward) {
+        if (model() == kDoubleLayer) return dtc() / (1.0f - ift(x.angle)) * ip * K.dG_dny(y.p, x.p, y.n);
         if (backward && x.type == kDirichlet) {
-            if (rng->uniform() * (1.0f + fk) < 1.0f) { y = x; return (1.0f + fk) * 1.0f; }
-            ip = ip * ((1.0f + fk) / fk);
+            if (rng.uniform() * (1.0f + p.fk) < 1.0f) { y = x; return (1.0f + p.fk) * 1.0f; }
+            ip = ip * ((1.0f + p.fk) / p.fk);
         } else if (!backward && y.type == kDirichlet) {
-            if (rng->uniform() * (1.0f + fk) < 1.0f) { x = y; return (1.0f + fk) * 1.0f; }
-            ip = ip * ((1.0f + fk) / fk);
+            if (rng.uniform() * (1.0f + p.fk) < 1.0f) { x = y; return (1.0f + p.fk) * 1.0f; }
+            ip = ip * ((1.0f + p.fk) / p.fk);
         }
-        if (bie == kSingleLayer) {
-            if (x.type == kDirichlet) return -2.0f * fk * ip * K.G(y.p, x.p);
+        if (model() == kSingleLayer) {
+            if (x.type == kDirichlet) return -2.0f * p.fk * ip * K.G(y.p, x.p);
             if (x.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(x.p, y.p, x.n);
             return -dtc() / ift(x.angle) * ip * (K.dG_dny(x.p, y.p, x.n) + x.alpha * K.G(y.p, x.p));
         }
         if (x.type == kDirichlet) {
-            if (y.type == kDirichlet) return -fk / ift(x.angle) * ip * K.G(y.p, x.p);
-            if (y.type == kNeumann) return fk / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
-            return fk / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
+            if (y.type == kDirichlet) return -p.fk / ift(x.angle) * ip * K.G(y.p, x.p);
+            if (y.type == kNeumann) return p.fk / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
+            return p.fk / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
         }
         if (y.type == kDirichlet) return dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
         if (y.type == kNeumann) return -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
         return -dtc() / ift(x.angle) * ip * (K.dG_dny(y.p, x.p, y.n) + y.alpha * K.G(y.p, x.p));
     }
-    __device__ float fbk(const BPoint<D> &x, const BPoint<D> &y, float ip) const {
-        if (bie == kDoubleLayer) return dtc() * 1.0f / (1.0f - ift(x.angle)) * (x.bv + vol_term(x));
-        if (bie == kSingleLayer) {
-            if (x.type == kDirichlet) return 2.0f * fk * (x.bv + vol_term(x));
+    __device__ __forceinline__ float fbk(const BPoint<D> &x, const BPoint<D> &y, float ip) {
+        if (model() == kDoubleLayer) return dtc() * 1.0f / (1.0f - ift(x.angle)) * (x.bv + vol_term(x));
+        if (model() == kSingleLayer) {
+            if (x.type == kDirichlet) return 2.0f * p.fk * (x.bv + vol_term(x));
             return dtc() / ift(x.angle) * (x.bv + vol_term(x));
         }
         if (x.type == kDirichlet) {
             const float sx = x.bv + vol_term(x);
             if (y.type == kDirichlet) {
                 const float k = dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
-                return dtc() * fk * (sx + k * (y.bv + vol_term(y)));
+                return dtc() * p.fk * (sx + k * (y.bv + vol_term(y)));
             }
             const float k = dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
-            return dtc() * fk * (sx - k * (y.bv + vol_term(y)));
+            return dtc() * p.fk * (sx - k * (y.bv + vol_term(y)));
         }
         if (y.type == kDirichlet) {
             const float k = -dtc() / ift(x.angle) * ip * K.dG_dny(y.p, x.p, y.n);
@@ -254,39 +292,21 @@ template <int D> struct Bie {
         const float k = dtc() / ift(x.angle) * ip * K.G(y.p, x.p);
         return k * (y.bv + vol_term(y));
     }
-};
 
-// ------------------------------------------------------------------------------------------
-// Estimators (estimator.cuh:113-504).
-// ------------------------------------------------------------------------------------------
-template <int D> struct Walker {
-    const SceneView<D> &s;
-    const WalkParams &p;
-    PathRng rng;
-    Bie<D> bie;
-    uint32_t bounces;
+    // ---------------- estimators
+    __device__ __forceinline__ int strat() const { return kStrat != kStratRuntime ? kStrat : strategy_of(model(), p.estimator, p.problem); }
+    __device__ __forceinline__ bool backward() const { return strat() <= kStratUniform; }
+    __device__ __forceinline__ bool dl_dirichlet() const { return strat() == kStratLineIntersection; }
+    __device__ __forceinline__ bool direct_neumann() const { return strat() == kStratDirectNeumann; }
+    __device__ __forceinline__ bool sl_neumann() const { return strat() == kStratFwdSlNeumann; }
 
-    __device__ __forceinline__ Walker(const SceneView<D> &s_, const WalkParams &p_, uint32_t stream, uint32_t point, uint64_t path)
-        : s(s_), p(p_), rng(p_.seed, stream, point, path), bounces(0) {
-        bie.K.eps = p.eps;
-        bie.s = &s;
-        bie.rng = &rng;
-        bie.bie = p.bie;
-        bie.domain = p.domain;
-        bie.fk = p.fk;
-        bie.nvs = p.n_volume;
-    }
-    __device__ __forceinline__ bool dl_dirichlet() const { return p.bie == kDoubleLayer && p.problem == kDirichletProblem; }
-    __device__ __forceinline__ bool direct_neumann() const { return p.bie == kDirect && p.problem == kNeumannProblem; }
-    __device__ __forceinline__ bool sl_neumann() const { return p.bie == kSingleLayer && p.problem == kNeumannProblem; }
-
-    __device__ float ris_target(int type, const BPoint<D> &yp, const BPoint<D> &c) const {
-        if (type == kDirichlet) return fabsf(bie.K.G(c.p, yp.p));
-        if (type == kNeumann) return fabsf(bie.K.dG_dny(yp.p, c.p, yp.n));
-        return fabsf(bie.K.dG_dny(yp.p, c.p, yp.n) + yp.alpha * bie.K.G(c.p, yp.p));
+    __device__ __forceinline__ float ris_target(int type, const BPoint<D> &yp, const BPoint<D> &c) const {
+        if (type == kDirichlet) return fabsf(K.G(c.p, yp.p));
+        if (type == kNeumann) return fabsf(K.dG_dny(yp.p, c.p, yp.n));
+        return fabsf(K.dG_dny(yp.p, c.p, yp.n) + yp.alpha * K.G(c.p, yp.p));
     }
     // Streaming RIS over K uniform candidates (scene.cuh:542-584, 847-889).
-    __device__ BPoint<D> sample_ris(const BPoint<D> &yp, float &inv_pdf) {
+    __device__ __forceinline__ BPoint<D> sample_ris(const BPoint<D> &yp, float &inv_pdf) {
         BPoint<D> y = bp_zero<D>();
         float w_sum = 0.0f;
         uint32_t M = 0;
@@ -303,7 +323,7 @@ template <int D> struct Walker {
     }
 
     // compute_sample_unknown_boundary (estimator.cuh:232-357)
-    __device__ float unknown_boundary(const BPoint<D> &x) {
+    __device__ __forceinline__ float unknown_boundary(const BPoint<D> &x) {
         float contrib = 0.0f, w = 1.0f;
         BPoint<D> y_prev = x;
         BPoint<D> y = bp_zero<D>();
@@ -314,26 +334,26 @@ template <int D> struct Walker {
             if (m == L - 1) w = 0.5f * w;
             if (dl_dirichlet()) {
                 y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
-                contrib = contrib + w * bie.fbk(y_prev, y, ip);
-                w = w * bie.fbu(y_prev, y, ip, true);
+                contrib = contrib + w * fbk(y_prev, y, ip);
+                w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             } else if (direct_neumann()) {
                 y = sample_boundary_value<D>(s, rng, ip);
-                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                contrib = contrib + w * fbk(y_prev, y, ip);
                 y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
-                w = w * bie.fbu(y_prev, y, ip, true);
+                w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
-            } else if (p.bie == kSingleLayer) {
-                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+            } else if (strat() == kStratSingleLayer) {
+                contrib = contrib + w * fbk(y_prev, y, ip);
                 if (p.n_resampling == 1) y = sample_uniform<D>(s, rng, ip);
                 else y = sample_ris(y_prev, ip);
-                w = w * bie.fbu(y_prev, y, ip, true);
+                w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             } else {
                 y = sample_uniform<D>(s, rng, ip);
-                contrib = contrib + w * bie.fbk(y_prev, y, ip);
+                contrib = contrib + w * fbk(y_prev, y, ip);
                 y = sample_uniform<D>(s, rng, ip);
-                w = w * bie.fbu(y_prev, y, ip, true);
+                w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             }
             if (w == 0.0f) break;
@@ -342,8 +362,8 @@ template <int D> struct Walker {
     }
 
     // compute_sample_path_contribution_domain (estimator.cuh:154-191 backward, 405-454 forward)
-    __device__ void domain(const V<D> &x, float out[D + 1]) {
-        if (p.estimator == kBackward) {
+    __device__ __forceinline__ void domain(const V<D> &x, float out[D + 1]) {
+        if (backward()) {
             BPoint<D> y, y1;
             float ip, ip1;
             if (dl_dirichlet()) {
@@ -357,13 +377,13 @@ template <int D> struct Walker {
                 y = sample_uniform<D>(s, rng, ip);
                 y1 = sample_uniform<D>(s, rng, ip1);
             }
-            out[0] = bie.sdk(x, y1, ip1);
-            const V<D> g = bie.gdk(x, y1, ip1);
+            out[0] = sdk(x, y1, ip1);
+            const V<D> g = gdk(x, y1, ip1);
 #pragma unroll
             for (int i = 0; i < D; i++) out[1 + i] = g.v[i];
             const float mu = unknown_boundary(y);
-            out[0] = out[0] + mu * bie.sdu(x, y, ip);
-            const V<D> gu = bie.gdu(x, y, ip);
+            out[0] = out[0] + mu * sdu(x, y, ip);
+            const V<D> gu = gdu(x, y, ip);
 #pragma unroll
             for (int i = 0; i < D; i++) out[1 + i] = out[1 + i] + mu * gu.v[i];
             return;
@@ -371,33 +391,33 @@ template <int D> struct Walker {
         BPoint<D> y, y2;
         float ip, ip2;
         y = sample_uniform<D>(s, rng, ip);
-        out[0] = bie.sdk(x, y, ip);
-        const V<D> g = bie.gdk(x, y, ip);
+        out[0] = sdk(x, y, ip);
+        const V<D> g = gdk(x, y, ip);
 #pragma unroll
         for (int i = 0; i < D; i++) out[1 + i] = g.v[i];
         if (sl_neumann()) y = sample_boundary_value<D>(s, rng, ip);
         else y = sample_uniform<D>(s, rng, ip);
         y2 = sample_uniform<D>(s, rng, ip2);
-        float w = ip * bie.fbk(y, y2, ip2);
+        float w = ip * fbk(y, y2, ip2);
         BPoint<D> y_prev;
         const uint32_t L = p.path_length;
         for (uint32_t m = 0; m < L; m++) {
             bounces++;
             if (m == L - 1) w = w * 0.5f;
-            out[0] = out[0] + w * bie.sdu(x, y, 1.0f);
-            const V<D> gu = bie.gdu(x, y, 1.0f);
+            out[0] = out[0] + w * sdu(x, y, 1.0f);
+            const V<D> gu = gdu(x, y, 1.0f);
 #pragma unroll
             for (int i = 0; i < D; i++) out[1 + i] = out[1 + i] + w * gu.v[i];
             y_prev = y;
             if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
             else y = sample_uniform<D>(s, rng, ip);
-            w = bie.fbu(y, y_prev, ip, false) * w;
+            w = fbu(y, y_prev, ip, false) * w;
         }
     }
 
     // compute_sample_path_contribution_boundary (estimator.cuh:193-222 backward, 456-496 forward)
-    __device__ float boundary(const BPoint<D> &x) {
-        if (p.estimator == kBackward) {
+    __device__ __forceinline__ float boundary(const BPoint<D> &x) {
+        if (backward()) {
             BPoint<D> y, y1;
             float ip, ip1;
             if (dl_dirichlet()) {
@@ -411,29 +431,29 @@ template <int D> struct Walker {
                 y = sample_uniform<D>(s, rng, ip);
                 y1 = sample_uniform<D>(s, rng, ip1);
             }
-            float r = bie.sbk(x, y1, ip1);
+            float r = sbk(x, y1, ip1);
             const float mu = unknown_boundary(y);
-            r = r + mu * bie.sbu(x, y, ip);
+            r = r + mu * sbu(x, y, ip);
             return r;
         }
         BPoint<D> y, y2;
         float ip, ip2;
         y = sample_uniform<D>(s, rng, ip);
-        float r = bie.sbk(x, y, ip);
+        float r = sbk(x, y, ip);
         if (sl_neumann()) y = sample_boundary_value<D>(s, rng, ip);
         else y = sample_uniform<D>(s, rng, ip);
         y2 = sample_uniform<D>(s, rng, ip2);
-        float w = ip * bie.fbk(y, y2, ip2);
+        float w = ip * fbk(y, y2, ip2);
         BPoint<D> y_prev;
         const uint32_t L = p.path_length;
         for (uint32_t m = 0; m < L; m++) {
             bounces++;
             if (m == L - 1) w = w * 0.5f;
-            r = r + bie.sbu(x, y, 1.0f) * w;
+            r = r + sbu(x, y, 1.0f) * w;
             y_prev = y;
             if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
             else y = sample_uniform<D>(s, rng, ip);
-            w = bie.fbu(y, y_prev, ip, false) * w;
+            w = fbu(y, y_prev, ip, false) * w;
         }
         return r;
     }
