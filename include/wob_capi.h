@@ -145,6 +145,27 @@ int wob_solve_domain_host(wob_scene scene, const wob_params *params, const float
                           uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces);
 
 /*
+ * Host-buffer domain solve that allocates nothing. No counterpart in the reference: it is for
+ * callers that may not allocate device memory (for example a host application that owns the GPU
+ * memory budget and forbids plugin allocations, or a real-time loop that must not allocate).
+ * Same arguments and accumulate-into semantics as wob_solve_domain_host, plus the stream to run
+ * on (NULL = legacy default stream); synchronises that stream before returning.
+ *
+ * It stages points, running sums and the bounce counter through a 16 MiB static device array
+ * that every GPU loading the library holds until the process exits, so n_points is limited to
+ * wob_noalloc_max_points(dim) (about 220k points in 3D, 300k in 2D); larger requests fail with
+ * WOB_ERR_INVALID_ARGUMENT. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. All calls on a device
+ * share the one array: calls are serialised within a process, calls from several processes or
+ * threads that overlap on the GPU race on it. It calls no cudaMalloc / cudaFree.
+ */
+int wob_solve_domain_host_noalloc(wob_scene scene, const wob_params *params, const float *points,
+                                  uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                                  void *stream);
+/* Largest n_points wob_solve_domain_host_noalloc accepts for dim 2 or 3. */
+int wob_noalloc_max_points(int dim, uint32_t *max_points);
+
+/*
  * Boundary estimator (replaces Estimator::compute_sample_path_contribution_boundary,
  * estimator.cuh:193-222, 456-496, as driven by apps/boundary_estimate.cu:62-95).
  * Device pointers, one boundary point per entry (points.hpp:32-39):

@@ -27,7 +27,7 @@ EXPORTED = [
     "wob_scene_get_info", "wob_scene_get_element_order", "wob_scene_poll_error",
     "wob_scene_set_volume_cache", "wob_scene_clear_volume_cache", "wob_solve_domain",
     "wob_solve_domain_host", "wob_solve_boundary", "wob_line_query", "wob_debug_domain_paths",
-    "wob_debug_boundary_paths",
+    "wob_debug_boundary_paths", "wob_solve_domain_host_noalloc", "wob_noalloc_max_points",
 ]
 
 
@@ -86,6 +86,8 @@ def load() -> C.CDLL:
         "wob_line_query": (C.c_int, [vp, vp, vp, u32, vp, vp, vp, vp]),
         "wob_debug_domain_paths": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp]),
         "wob_debug_boundary_paths": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+        "wob_solve_domain_host_noalloc": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp, vp, vp]),
+        "wob_noalloc_max_points": (C.c_int, [C.c_int, P(u32)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

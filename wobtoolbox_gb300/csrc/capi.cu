@@ -151,6 +151,57 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     return WOB_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// Allocation-free staging for wob_solve_domain_host_noalloc.
+//
+// Callers that may not allocate device memory (a host application that owns the GPU memory
+// budget and forbids allocations by plugins, a real-time loop that must not allocate) still need
+// the host-buffer solve. That entry point stages its points, running sums and bounce counter
+// through this fixed array instead of a cudaMalloc'd workspace. It is a file-scope static device
+// array, so every GPU that loads the library holds it until the process exits.
+// ------------------------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;                        // serialises the entry point within a process
+void *g_noalloc_addr[kNoAllocMaxDevices] = {};     // device address of the array, per device
+
+inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Layout for n points of dimension D: points | sums | sums of squares | bounce counter.
+size_t noalloc_bytes(int D, uint64_t n, size_t off[4]) {
+    off[0] = 0;
+    off[1] = align256(n * (uint64_t)D * 4);
+    off[2] = off[1] + align256(n * (uint64_t)(D + 1) * 8);
+    off[3] = off[2] + align256(n * (uint64_t)(D + 1) * 8);
+    return off[3] + 256;
+}
+
+uint32_t noalloc_max_points(int D) {
+    uint64_t lo = 0, hi = kNoAllocScratchBytes;
+    size_t off[4];
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) / 2;
+        if (noalloc_bytes(D, mid, off) <= kNoAllocScratchBytes) lo = mid;
+        else hi = mid - 1;
+    }
+    return (uint32_t)lo;
+}
+
+// Device address of the scratch array on `device` (which must be current). The host-side name
+// g_noalloc_scratch is only a stand-in: its address has to be looked up once per device.
+int noalloc_scratch(int device, void **out) {
+    if (device < 0 || device >= kNoAllocMaxDevices) return fail(WOB_ERR_UNSUPPORTED, "device index out of range for the no-allocation scratch");
+    if (!g_noalloc_addr[device]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress(no-allocation scratch)");
+        g_noalloc_addr[device] = ptr;
+    }
+    *out = g_noalloc_addr[device];
+    return WOB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -438,6 +489,65 @@ int wob_scene_poll_error(wob_scene s, uint32_t *bits) {
     if (v && (e = cudaMemcpy(s->err.ptr, &zero, 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail_cuda(e, "clearing the error word");
     if (bits) *bits = v;
+    return WOB_OK;
+}
+
+int wob_noalloc_max_points(int dim, uint32_t *max_points) {
+    if ((dim != 2 && dim != 3) || !max_points) return fail(WOB_ERR_INVALID_ARGUMENT, "dim must be 2 or 3 and max_points non-NULL");
+    *max_points = noalloc_max_points(dim);
+    return WOB_OK;
+}
+
+int wob_solve_domain_host_noalloc(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
+                                  double *sum, double *sumsq, uint64_t *bounces, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!points || !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum are required");
+    const int D = s->host.dim;
+    const uint32_t max_points = noalloc_max_points(D);
+    if (n_points > max_points)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "n_points = " + std::to_string(n_points) + " exceeds the no-allocation limit of " +
+                                                  std::to_string(max_points) + " points for dim " + std::to_string(D) +
+                                                  " (16 MiB static device scratch); split the points or use wob_solve_domain_host");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    DeviceGuard g(s->device);
+    void *base_v = nullptr;
+    if ((st = noalloc_scratch(s->device, &base_v)) != WOB_OK) return st;
+    char *base = (char *)base_v;
+    size_t off[4];
+    noalloc_bytes(D, n_points, off);
+    float *d_pts = (float *)(base + off[0]);
+    double *d_sum = (double *)(base + off[1]);
+    double *d_sq = (double *)(base + off[2]);
+    uint64_t *d_b = (uint64_t *)(base + off[3]);
+    const size_t pts_bytes = (size_t)n_points * D * 4, out_bytes = (size_t)n_points * (D + 1) * 8;
+    cudaStream_t cs = (cudaStream_t)stream;
+    cudaError_t e;
+    // The array keeps the previous call's contents: the sums are loaded from the caller's arrays
+    // (the solve accumulates into them) and the bounce counter is cleared.
+    if ((e = cudaMemcpyAsync(d_pts, points, pts_bytes, cudaMemcpyHostToDevice, cs)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_sum, sum, out_bytes, cudaMemcpyHostToDevice, cs)) != cudaSuccess ||
+        (sumsq && (e = cudaMemcpyAsync(d_sq, sumsq, out_bytes, cudaMemcpyHostToDevice, cs)) != cudaSuccess) ||
+        (e = cudaMemsetAsync(d_b, 0, 8, cs)) != cudaSuccess)
+        return fail_cuda(e, "staging inputs in the no-allocation scratch");
+    e = D == 2 ? wobgb::launch_domain_2d(s->view<2>(), w, d_pts, n_points, d_sum, sumsq ? d_sq : nullptr,
+                                         (unsigned long long *)d_b, nullptr, cs)
+               : wobgb::launch_domain_3d(s->view<3>(), w, d_pts, n_points, d_sum, sumsq ? d_sq : nullptr,
+                                         (unsigned long long *)d_b, nullptr, cs);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the domain walk");
+    uint64_t b = 0;
+    uint32_t errw = 0;
+    if ((e = cudaMemcpyAsync(sum, d_sum, out_bytes, cudaMemcpyDeviceToHost, cs)) != cudaSuccess ||
+        (sumsq && (e = cudaMemcpyAsync(sumsq, d_sq, out_bytes, cudaMemcpyDeviceToHost, cs)) != cudaSuccess) ||
+        (e = cudaMemcpyAsync(&b, d_b, 8, cudaMemcpyDeviceToHost, cs)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&errw, s->err.ptr, 4, cudaMemcpyDeviceToHost, cs)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(cs)) != cudaSuccess)
+        return fail_cuda(e, "reading results from the no-allocation scratch");
+    if (bounces) *bounces += b;
+    if (errw) return fail(WOB_ERR_DEVICE_LIMIT, "a BVH traversal hit its stack or step bound");
     return WOB_OK;
 }
 
