@@ -54,6 +54,9 @@ WORKLOAD = ("3D interior Robin (du/dn + 2u = h), direct BIE, backward estimator,
             "displaced icosphere 81920 triangles; 512x512 z=0 slice over [-1.3,1.3]^2, inside points; "
             "4096 paths x 16 bounces per point per step")
 PROBE_DIR = np.array([0.48, 0.57, 0.66])
+DL2D_WORKLOAD = ("2D interior Dirichlet, double-layer BIE, backward estimator, line-intersection sampling; star "
+                 "r = 1 + 0.3 cos 5t, 1024 segments, g = e^x cos y; 128x128 grid over [-1.3,1.3]^2, 7960 interior "
+                 "points; 1024 paths x 8 bounces per point per step")
 
 
 def build_scene_arrays():
@@ -250,43 +253,62 @@ def run_ours(args):
     rank, world, local = dist_init(args)
     wob.load()
     dev = torch.device("cuda", torch.cuda.current_device())
-    sc = build_scene_arrays()
-    scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
-
-    # inside test of every slice point on the GPU: odd number of crossings of a half-line
-    cand = W.slice_points_z0(GRID, EXTENT)
-    n_c = len(cand)
-    d_c = torch.from_numpy(cand).to(dev)
-    d_dir = torch.from_numpy(probe_dirs(n_c)).to(dev)
-    counts = torch.zeros(n_c, dtype=torch.int32, device=dev)
-    hits = torch.zeros(n_c, 64, dtype=torch.int32, device=dev)
-    hp = torch.zeros(n_c, 64, 3, dtype=torch.float32, device=dev)
-    scene.line_query(d_c, d_dir, n_c, counts, hits, hp)
-    m = torch.clamp(counts, max=64)
-    valid = torch.arange(64, device=dev)[None, :] < m[:, None]
-    t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
-    crossings = ((t > 0) & valid).sum(1)
-    inside = (crossings % 2 == 1).cpu().numpy()
-    del hits, hp
-    pts = np.ascontiguousarray(cand[inside])
-    paths = PATHS
+    if args.workload == "dl2d":
+        sc = W.config0_scene()
+        scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+        pts = sc["points"]
+        paths = 1024
+        p = wob.EstimatorParams(bie_model=wob.IndirectDoubleLayer, domain=wob.InteriorDomain,
+                                estimator=wob.BackwardEstimator, problem=wob.DirichletProblem, path_length=8,
+                                num_sample_paths=paths, seed=SEED)
+        exact_u = W.exp_cos(pts)[:, 0]
+        workload = DL2D_WORKLOAD
+        bytes_per_bounce = None
+    else:
+        sc = build_scene_arrays()
+        scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+        # inside test of every slice point on the GPU: odd number of crossings of a half-line
+        cand = W.slice_points_z0(GRID, EXTENT)
+        n_c = len(cand)
+        d_c = torch.from_numpy(cand).to(dev)
+        d_dir = torch.from_numpy(probe_dirs(n_c)).to(dev)
+        counts = torch.zeros(n_c, dtype=torch.int32, device=dev)
+        hits = torch.zeros(n_c, 64, dtype=torch.int32, device=dev)
+        hp = torch.zeros(n_c, 64, 3, dtype=torch.float32, device=dev)
+        scene.line_query(d_c, d_dir, n_c, counts, hits, hp)
+        m = torch.clamp(counts, max=64)
+        valid = torch.arange(64, device=dev)[None, :] < m[:, None]
+        t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
+        crossings = ((t > 0) & valid).sum(1)
+        inside = (crossings % 2 == 1).cpu().numpy()
+        del hits, hp
+        pts = np.ascontiguousarray(cand[inside])
+        paths = PATHS
+        p = params()
+        exact_u = None
+        workload = WORKLOAD
+        bytes_per_bounce = BYTES_PER_BOUNCE
     if args.small:  # profiling case: every 16th point, 512 paths
         pts = np.ascontiguousarray(pts[::16])
         paths = 512
+        if exact_u is not None:
+            exact_u = exact_u[::16]
     n_pts = len(pts)
+    D = pts.shape[1]
     d_pts = torch.from_numpy(pts).to(dev)
-    d_sum = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
-    d_sq = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+    d_sum = torch.zeros(n_pts, D + 1, dtype=torch.float64, device=dev)
+    d_sq = torch.zeros(n_pts, D + 1, dtype=torch.float64, device=dev)
     d_b = torch.zeros(1, dtype=torch.int64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream()
-    p = dataclasses.replace(params(), num_sample_paths=paths)
+    p = dataclasses.replace(p, num_sample_paths=paths)
     base_offset = rank * (1 << 40)
 
     def step(k, sum_buf=d_sum, sq_buf=d_sq):
         scene.solve_domain(dataclasses.replace(p, path_offset=base_offset + k * paths), d_pts, n_pts, sum_buf,
                            sq_buf, d_b, stream)
 
+    tuned = scene.autotune_domain(p, d_pts, n_pts, stream)
     for w in range(args.warmup):
         step(w)
     torch.cuda.synchronize()
@@ -318,12 +340,14 @@ def run_ours(args):
     s = d_sum.cpu().numpy()
     n_paths_total = args.steps * paths
     u = s[:, 0] / n_paths_total
-    rmse = float(np.sqrt(np.mean((u - exact(pts, sc)) ** 2)))
+    if exact_u is None:
+        exact_u = exact(pts, sc)
+    rmse = float(np.sqrt(np.mean((u - exact_u) ** 2)))
 
     # end to end through the C ABI with host buffers (copies in the timed region)
     pts_pinned = torch.from_numpy(pts).pin_memory()
-    h_sum = np.zeros((n_pts, 4))
-    h_sq = np.zeros((n_pts, 4))
+    h_sum = np.zeros((n_pts, D + 1))
+    h_sq = np.zeros((n_pts, D + 1))
     e2e_p = dataclasses.replace(p, path_offset=base_offset + (1 << 30))
     import ctypes as C
     lib = wob.load()
@@ -349,7 +373,7 @@ def run_ours(args):
     if rank == 0:
         avg_ms = sum(kernel_ms) / len(kernel_ms)
         bounces_per_launch = bounces_local / args.steps
-        achieved = BYTES_PER_BOUNCE * bounces_per_launch / (avg_ms / 1e3) / 1e9
+        achieved = (bytes_per_bounce or 0) * bounces_per_launch / (avg_ms / 1e3) / 1e9
         peaks = {}
         try:
             with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -362,25 +386,26 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles": int(len(sc["verts"])), "points": n_pts,
-                       "paths_per_point_per_step": paths, "path_length": PATH_LENGTH,
+            "config": {"workload": workload, "elements": int(len(sc["verts"])), "points": n_pts,
+                       "paths_per_point_per_step": paths, "path_length": p.path_length,
                        "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
                        "rmse_u_vs_exact": rmse, "paths_per_point_total": n_paths_total,
-                       "parallelism": f"replicas x{world}, points x independent path streams"},
+                       "parallelism": f"replicas x{world}, points x independent path streams",
+                       "autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if peaks else
                          "fallback 6.8 TB/s",
                          "traffic": None if TRAFFIC_BYTES_PER_BOUNCE is None else
                          TRAFFIC_BYTES_PER_BOUNCE * bounces_per_launch,
-                         "algorithmic_bytes_per_bounce": BYTES_PER_BOUNCE},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_pts * 3 * 4,
-                    "d2h_bytes_per_step": n_pts * 4 * 8 * 2 + 8 + 4, "steps": e2e_steps},
+                         "algorithmic_bytes_per_bounce": bytes_per_bounce},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_pts * D * 4,
+                    "d2h_bytes_per_step": n_pts * (D + 1) * 8 * 2 + 8 + 4, "steps": e2e_steps},
             "clocks": clk,
             "gpu_launches": args.steps,
             "kernel_ms": kernel_ms,
         }
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and args.workload == "robin3d":
             from oracle import oracle_py as O
             O.build()
             sample_pts = cpu_sample(sc, args.cpu_points)
@@ -407,6 +432,8 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
+    ap.add_argument("--workload", choices=["robin3d", "dl2d"], default="robin3d",
+                    help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

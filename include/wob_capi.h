@@ -145,6 +145,25 @@ int wob_solve_domain_host(wob_scene scene, const wob_params *params, const float
                           uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces);
 
 /*
+ * Autotuner (no counterpart in the reference, whose launch shape is fixed by thrust::for_each):
+ * the specialised walk kernels are compiled for several occupancy targets; this times each on
+ * the first points (device pointer, about 2^21 paths) with the given parameters and makes the
+ * fastest the one used for that kernel variant from then on (process-wide). chosen = index of
+ * the chosen configuration (-1: these parameters use no tunable kernel), ms_per_config[k] = time
+ * of configuration k (room for 8), n_configs = number of configurations. Allocates a temporary
+ * output buffer and synchronises `stream`.
+ */
+int wob_autotune_domain(wob_scene scene, const wob_params *params, const float *points,
+                        uint32_t n_points, int32_t *chosen, float *ms_per_config, int32_t *n_configs,
+                        void *stream);
+
+/* The tunable kernel variant a solve with these parameters uses (-1: none). */
+int wob_tunable_variant(wob_scene scene, const wob_params *params, int32_t *variant);
+/* Fix / read the configuration of a tunable variant (e.g. to reuse an earlier tuning result). */
+int wob_set_domain_config(int32_t variant, int32_t config);
+int wob_get_domain_config(int32_t variant, int32_t *config);
+
+/*
  * Host-buffer domain solve that allocates nothing. No counterpart in the reference: it is for
  * callers that may not allocate device memory (for example a host application that owns the GPU
  * memory budget and forbids plugin allocations, or a real-time loop that must not allocate).

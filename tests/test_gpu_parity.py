@@ -212,3 +212,31 @@ def test_invalid_arguments_raise(engine, cuda):
     with pytest.raises(engine.WobError):
         scene.solve_domain_host(_params(engine, 0, 0, 0, 1, path_length=0), pts)
     scene.close()
+
+
+@pytest.mark.parametrize("case", ["uniform3d", "li2d"])
+def test_every_tuned_configuration_is_bit_identical(engine, oracle, cuda, case):
+    """The occupancy configurations the autotuner chooses among give the same paths."""
+    import ctypes as C
+    lib = engine.load()
+    if case == "uniform3d":
+        sc = S.scene3d(2, False)
+        p = _params(engine, 2, 0, 0, 2, path_length=6, num_sample_paths=64)
+    else:
+        sc = S.scene2d(0, False)
+        p = _params(engine, 1, 0, 0, 0, path_length=6, num_sample_paths=64)
+    scene = _make(engine, sc)
+    v = C.c_int32(-1)
+    engine.check(lib.wob_tunable_variant(scene.handle, C.byref(p.to_c()), C.byref(v)))
+    assert v.value >= 0
+    old = C.c_int32(0)
+    engine.check(lib.wob_get_domain_config(v.value, C.byref(old)))
+    try:
+        for cfg in range(3):
+            engine.check(lib.wob_set_domain_config(v.value, cfg))
+            _check_domain(engine, oracle, cuda, sc, p)
+        chosen, ms = scene.autotune_domain(p, cuda.from_numpy(sc["points"]).cuda(), len(sc["points"]))
+        assert 0 <= chosen < 3 and len(ms) == 3 and all(m > 0 for m in ms)
+    finally:
+        lib.wob_set_domain_config(v.value, old.value)
+    scene.close()

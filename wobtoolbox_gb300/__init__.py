@@ -239,6 +239,17 @@ class SceneHost:
                                               _ptr(boundary_value), _ptr(boundary_type), _ptr(robin_alpha),
                                               int(n_points), _ptr(values), _stream_ptr(stream)))
 
+    def autotune_domain(self, params: EstimatorParams, points, n_points: int, stream=None):
+        """Times the compiled configurations of the kernel these parameters use and keeps the
+        fastest. Returns (chosen index or -1, [ms per configuration])."""
+        p = params.to_c()
+        chosen = C.c_int32(-1)
+        n = C.c_int32(0)
+        ms = (C.c_float * 8)()
+        check(load().wob_autotune_domain(self._h, C.byref(p), _ptr(points), int(n_points), C.byref(chosen), ms,
+                                         C.byref(n), _stream_ptr(stream)))
+        return int(chosen.value), [float(ms[i]) for i in range(n.value)]
+
     def line_query(self, origins, dirs, n_rays: int, counts, hits, hit_points=None, stream=None) -> None:
         check(load().wob_line_query(self._h, _ptr(origins), _ptr(dirs), int(n_rays), _ptr(counts), _ptr(hits),
                                     _ptr(hit_points), _stream_ptr(stream)))

@@ -28,6 +28,7 @@ EXPORTED = [
     "wob_scene_set_volume_cache", "wob_scene_clear_volume_cache", "wob_solve_domain",
     "wob_solve_domain_host", "wob_solve_boundary", "wob_line_query", "wob_debug_domain_paths",
     "wob_debug_boundary_paths", "wob_solve_domain_host_noalloc", "wob_noalloc_max_points",
+    "wob_autotune_domain", "wob_tunable_variant", "wob_set_domain_config", "wob_get_domain_config",
 ]
 
 
@@ -88,6 +89,10 @@ def load() -> C.CDLL:
         "wob_debug_boundary_paths": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp]),
         "wob_solve_domain_host_noalloc": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp, vp, vp]),
         "wob_noalloc_max_points": (C.c_int, [C.c_int, P(u32)]),
+        "wob_autotune_domain": (C.c_int, [vp, P(wob_params), vp, u32, P(i32), vp, P(i32), vp]),
+        "wob_tunable_variant": (C.c_int, [vp, P(wob_params), P(i32)]),
+        "wob_set_domain_config": (C.c_int, [i32, i32]),
+        "wob_get_domain_config": (C.c_int, [i32, P(i32)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

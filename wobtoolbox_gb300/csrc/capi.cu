@@ -551,4 +551,80 @@ int wob_solve_domain_host_noalloc(wob_scene s, const wob_params *params, const f
     return WOB_OK;
 }
 
+int wob_autotune_domain(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
+                        int32_t *chosen, float *ms_per_config, int32_t *n_configs, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    const int D = s->host.dim;
+    const int v = wobgb::tunable_domain_variant(D, w);
+    if (chosen) *chosen = -1;
+    if (n_configs) *n_configs = 0;
+    if (v < 0 || n_points == 0) return WOB_OK;
+    if (!points) return fail(WOB_ERR_INVALID_ARGUMENT, "points is NULL");
+    // Time each configuration on enough points for about 2^21 paths (or all points).
+    const uint64_t want = ((1ull << 21) + w.n_paths - 1) / w.n_paths;
+    const uint32_t n_sub = (uint32_t)(want < n_points ? want : n_points);
+    DeviceGuard g(s->device);
+    cudaStream_t cs = (cudaStream_t)stream;
+    double *tmp = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&tmp, (size_t)n_sub * (D + 1) * 8)) != cudaSuccess) return fail_cuda(e, "cudaMalloc (autotune)");
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaFree(tmp);
+        return fail_cuda(e, "cudaEventCreate");
+    }
+    const wobgb::SceneView<2> v2 = s->view<2>();
+    const wobgb::SceneView<3> v3 = s->view<3>();
+    const void *view = D == 2 ? (const void *)&v2 : (const void *)&v3;
+    int best = 0;
+    float best_ms = 3.0e38f;
+    for (int c = 0; c < wobgb::kTuneConfigs && e == cudaSuccess; c++) {
+        e = wobgb::launch_domain_config(D, v, c, view, w, points, n_sub, tmp, nullptr, nullptr, nullptr, cs);
+        if (e != cudaSuccess) break;
+        cudaEventRecord(e0, cs);
+        for (int r = 0; r < 2 && e == cudaSuccess; r++)
+            e = wobgb::launch_domain_config(D, v, c, view, w, points, n_sub, tmp, nullptr, nullptr, nullptr, cs);
+        cudaEventRecord(e1, cs);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        ms *= 0.5f;
+        if (ms_per_config) ms_per_config[c] = ms;
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail_cuda(e, "autotuning");
+    wobgb::set_domain_config(v, best);
+    if (chosen) *chosen = best;
+    if (n_configs) *n_configs = wobgb::kTuneConfigs;
+    return WOB_OK;
+}
+
+int wob_set_domain_config(int32_t variant, int32_t config) {
+    if (variant < 0 || variant >= wobgb::kNumTunable || config < 0 || config >= wobgb::kTuneConfigs)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "variant or config out of range");
+    wobgb::set_domain_config(variant, config);
+    return WOB_OK;
+}
+
+int wob_get_domain_config(int32_t variant, int32_t *config) {
+    if (variant < 0 || variant >= wobgb::kNumTunable || !config) return fail(WOB_ERR_INVALID_ARGUMENT, "variant out of range or config NULL");
+    *config = wobgb::domain_config(variant);
+    return WOB_OK;
+}
+
+int wob_tunable_variant(wob_scene s, const wob_params *params, int32_t *variant) {
+    if (!s || !variant) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and variant are required");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    *variant = wobgb::tunable_domain_variant(s->host.dim, w);
+    return WOB_OK;
+}
+
 }  // extern "C"

@@ -225,11 +225,11 @@ template <> __device__ __forceinline__ Elem<3> load_elem<3>(const SceneView<3> &
 // under (j - 1/2)/G < key and cdf[hi] >= (j + 3/2)/G > key, so the answer lies in [lo, hi]; the
 // two stored values settle it with one 16-byte load in almost every case, the bisection below
 // covers the rest of the sub-range.
-__device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, const uint4 *__restrict__ guide,
-                                               uint32_t G, float key) {
+__device__ __forceinline__ uint32_t guide_bin(uint32_t G, float key) {
     uint32_t j = (uint32_t)(key * (float)G);
-    if (j >= G) j = G - 1;
-    const uint4 g = __ldg(guide + j);
+    return j >= G ? G - 1 : j;
+}
+__device__ __forceinline__ uint32_t cdf_resolve(const float *__restrict__ cdf, const uint4 g, float key) {
     const uint32_t lo = g.x, hi = g.y;
     if (lo >= hi) return hi;
     if (key <= __uint_as_float(g.z)) return lo;
@@ -242,6 +242,10 @@ __device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, co
         else low = mid + 1;
     }
     return high;
+}
+__device__ __forceinline__ uint32_t cdf_search(const float *__restrict__ cdf, const uint4 *__restrict__ guide,
+                                               uint32_t G, float key) {
+    return cdf_resolve(cdf, __ldg(guide + guide_bin(G, key)), key);
 }
 
 // val1 + u (val2 - val1) (scene.cuh:393-396)
@@ -401,13 +405,12 @@ __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D>
 // ------------------------------------------------------------------------------------------
 // Boundary sampling queries (scene.cuh:441-622, 734-918).
 // ------------------------------------------------------------------------------------------
-template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
-    const float u1 = rng.uniform();
-    const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, u1);
-    const Elem<D> e = load_elem<D>(s, idx);
+// The point of a uniform boundary sample on element e from its draws u[0..D-1] (u[0] picked the
+// element): linear interpolation in 2D, the sqrt-barycentric map in 3D.
+template <int D> __device__ __forceinline__ BPoint<D> uniform_point(const Elem<D> &e, const float *u) {
     BPoint<D> r;
     if constexpr (D == 2) {
-        const float u2 = rng.uniform();
+        const float u2 = u[1];
         r.p.v[0] = interp2(e.v[0].v[0], e.v[1].v[0], u2);
         r.p.v[1] = interp2(e.v[0].v[1], e.v[1].v[1], u2);
         r.n = e.n;
@@ -416,8 +419,7 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const Scene
         r.type = e.type;
         r.alpha = interp2(e.alpha[0], e.alpha[1], u2);
     } else {
-        const float u2 = rng.uniform();
-        const float u3 = rng.uniform();
+        const float u2 = u[1], u3 = u[2];
         const float sq = sqrtf(u2);
         const float k1 = 1.0f - sq, k2 = sq * (1.0f - u3), k3 = u3 * sq;
 #pragma unroll
@@ -428,8 +430,38 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const Scene
         r.type = e.type;
         r.alpha = interp3(e.alpha[0], e.alpha[1], e.alpha[2], k1, k2, k3);
     }
-    inv_pdf = s.total_area;
     return r;
+}
+
+template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
+    float u[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) u[i] = rng.uniform();
+    const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, u[0]);
+    inv_pdf = s.total_area;
+    return uniform_point<D>(load_elem<D>(s, idx), u);
+}
+
+// Two consecutive uniform samples: the draws of both are taken first, in the order two
+// sample_uniform calls take them, and both guide and element loads are issued before either is
+// used, so the two dependent load chains overlap. Same values as two sample_uniform calls.
+template <int D> __device__ __forceinline__ void sample_uniform_pair(const SceneView<D> &s, PathRng &rng, BPoint<D> &ya,
+                                                                    float &ipa, BPoint<D> &yb, float &ipb) {
+    float ua[D], ub[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) ua[i] = rng.uniform();
+#pragma unroll
+    for (int i = 0; i < D; i++) ub[i] = rng.uniform();
+    const uint4 ga = __ldg(s.area_guide + guide_bin(s.area_G, ua[0]));
+    const uint4 gb = __ldg(s.area_guide + guide_bin(s.area_G, ub[0]));
+    const uint32_t ia = cdf_resolve(s.area_cdf, ga, ua[0]);
+    const uint32_t ib = cdf_resolve(s.area_cdf, gb, ub[0]);
+    const Elem<D> ea = load_elem<D>(s, ia);
+    const Elem<D> eb = load_elem<D>(s, ib);
+    ya = uniform_point<D>(ea, ua);
+    yb = uniform_point<D>(eb, ub);
+    ipa = s.total_area;
+    ipb = s.total_area;
 }
 
 template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(const SceneView<D> &s, PathRng &rng, const V<D> &x, uint32_t &m_out) {

@@ -26,8 +26,10 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
-template <int D, int kBie, int kStrat, bool kVol, bool kPerPath>
-__global__ void __launch_bounds__(kBlock) domain_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
+// kMinB: minimum resident blocks per SM requested from the register allocator (1 = no limit);
+// the autotuner chooses among the compiled values.
+template <int D, int kBie, int kStrat, bool kVol, bool kPerPath, int kMinB = 1>
+__global__ void __launch_bounds__(kBlock, kMinB) domain_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                         uint32_t n_points, double *__restrict__ sum,
                                                         double *__restrict__ sumsq,
                                                         unsigned long long *__restrict__ bounces,
@@ -173,16 +175,16 @@ inline int persistent_grid(K kernel, uint64_t work_warps) {
     return (int)g;
 }
 
-template <int D, int kBie, int kStrat, bool kVol>
+template <int D, int kBie, int kStrat, bool kVol, int kMinB>
 cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                   double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                   cudaStream_t stream) {
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
     if (per_path) {
-        auto k = domain_kernel<D, kBie, kStrat, kVol, true>;
+        auto k = domain_kernel<D, kBie, kStrat, kVol, true, kMinB>;
         k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);
     } else {
-        auto k = domain_kernel<D, kBie, kStrat, kVol, false>;
+        auto k = domain_kernel<D, kBie, kStrat, kVol, false, kMinB>;
         k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, nullptr);
     }
     return cudaGetLastError();

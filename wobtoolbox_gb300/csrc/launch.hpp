@@ -18,7 +18,7 @@ struct BoundaryInput {
 
 // Variants of the walk kernels: kBie / kStrat fix the BIE model and sampling strategy at compile
 // time (-1 = run-time), kVol = false drops the source term. Instantiated in the k*_*.cu units.
-template <int D, int kBie, int kStrat, bool kVol>
+template <int D, int kBie, int kStrat, bool kVol, int kMinB = 1>
 cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                   double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                   cudaStream_t stream);
@@ -29,6 +29,19 @@ cudaError_t launch_boundary_variant(const SceneView<D> &s, const WalkParams &p, 
 template <int D>
 cudaError_t launch_line_query_impl(const SceneView<D> &s, const float *origins, const float *dirs, uint32_t n,
                                    uint32_t *counts, uint32_t *hits, float *points, cudaStream_t stream);
+
+// Autotuned variants: the hot specialisations are compiled for several occupancy targets.
+// tunable_domain_variant() names the tunable variant a solve would use (-1: none);
+// set_domain_config() / domain_config() select the compiled configuration used from then on.
+constexpr int kNumTunable = 3;
+constexpr int kTuneConfigs = 3;
+int tunable_domain_variant(int dim, const WalkParams &p);
+int domain_config(int variant);
+void set_domain_config(int variant, int config);
+const char *domain_config_name(int variant, int config);
+cudaError_t launch_domain_config(int dim, int variant, int config, const void *scene_view, const WalkParams &p,
+                                 const float *pts, uint32_t n_points, double *sum, double *sumsq,
+                                 unsigned long long *bounces, float *per_path, cudaStream_t stream);
 
 // Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,

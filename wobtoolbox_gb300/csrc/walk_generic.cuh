@@ -349,6 +349,14 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
                 else y = sample_ris(y_prev, ip);
                 w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
+            } else if (!kVol || p.n_volume == 0) {
+                // no draw between the two samples (fbk draws only for a source term): take both at once
+                BPoint<D> ya;
+                float ipa;
+                sample_uniform_pair<D>(s, rng, ya, ipa, y, ip);
+                contrib = contrib + w * fbk(y_prev, ya, ipa);
+                w = w * fbu(y_prev, y, ip, true);
+                y_prev = y;
             } else {
                 y = sample_uniform<D>(s, rng, ip);
                 contrib = contrib + w * fbk(y_prev, y, ip);
@@ -374,8 +382,7 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
                 y = sample_line_intersection<D>(s, rng, x, ip);
                 y1 = sample_boundary_value<D>(s, rng, ip1);
             } else {
-                y = sample_uniform<D>(s, rng, ip);
-                y1 = sample_uniform<D>(s, rng, ip1);
+                sample_uniform_pair<D>(s, rng, y, ip, y1, ip1);
             }
             out[0] = sdk(x, y1, ip1);
             const V<D> g = gdk(x, y1, ip1);
