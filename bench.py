@@ -421,6 +421,104 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batch(args):
+    """Batched workload: 256 seeded 2D scenes (lobes U{3..9}, amplitude U[0.1, 0.35], segments
+    log-uniform in [64, 16384], points U[1k, 64k]; interior / exterior x Neumann / Robin, Gaussian
+    sources in the interior scenes) in one persistent launch, against the same 256 solves launched
+    one after another (eagerly and replayed from a captured CUDA graph)."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    paths = args.batch_paths
+    specs = W.batch_scenes(256, seed=SEED, paths=paths, path_length=8)
+    scenes, plist = [], []
+    for sc in specs:
+        s = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+        if sc["volume"] is not None:
+            s.set_volume_cache(*sc["volume"])
+        scenes.append(s)
+        plist.append(wob.EstimatorParams(seed=SEED, **sc["params"]))
+    n_pts = [len(sc["points"]) for sc in specs]
+    pts = torch.from_numpy(np.concatenate([sc["points"] for sc in specs])).to(dev)
+    total = len(pts)
+    batch = wob.SceneBatch(scenes, plist, n_pts)
+    off = batch.offsets
+    d_sum = torch.zeros(total, 3, dtype=torch.float64, device=dev)
+    d_sq = torch.zeros_like(d_sum)
+    d_b = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def sequential(k):
+        for i, (s, p) in enumerate(zip(scenes, plist)):
+            q = dataclasses.replace(p, path_offset=k * paths)
+            s.solve_domain(q, pts[off[i]:off[i + 1]], n_pts[i], d_sum[off[i]:off[i + 1]], d_sq[off[i]:off[i + 1]],
+                           d_b, stream)
+
+    def batched(k):
+        batch.solve(pts, d_sum, d_sq, d_b, k * paths, stream)
+
+    def timed(fn, steps, base):
+        ms = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn(base + k)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    for w in range(args.warmup):
+        batched(w)
+        sequential(w)
+    torch.cuda.synchronize()
+    d_b.zero_()
+    with ClockSampler(local) as clocks:
+        b_ms = timed(batched, args.steps, 100)
+        torch.cuda.synchronize()
+        bounces_batched = int(d_b.item())
+        s_ms = timed(sequential, args.steps, 200)
+        # the sequential solves replayed from a captured graph (no launch overhead)
+        g = torch.cuda.CUDAGraph()
+        gs = torch.cuda.Stream()
+        gs.wait_stream(stream)
+        with torch.cuda.stream(gs):
+            with torch.cuda.graph(g, stream=gs):
+                for i, (s, p) in enumerate(zip(scenes, plist)):
+                    s.solve_domain(p, pts[off[i]:off[i + 1]], n_pts[i], d_sum[off[i]:off[i + 1]],
+                                   d_sq[off[i]:off[i + 1]], d_b, gs)
+        stream.wait_stream(gs)
+        g_ms = timed(lambda k: g.replay(), args.steps, 300)
+    clk = clocks.summary()
+    value = bounces_batched / (sum(b_ms) / 1e3)
+    out = {
+        "metric": "batched plain WoB: speedup of one persistent launch over 256 sequential launches",
+        "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(b_ms) / len(b_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "256 2D star scenes (lobes U{3..9}, amplitude U[0.1,0.35], segments log-uniform "
+                               "[64,16384], points U[1k,64k]); interior/exterior x Neumann (SL forward) / Robin (SL "
+                               "backward, RIS 64); 4 Gaussian sources in interior scenes",
+                   "points": total, "paths_per_point": paths, "path_length": 8,
+                   "batched_ms": sum(b_ms) / len(b_ms), "sequential_ms": sum(s_ms) / len(s_ms),
+                   "graph_sequential_ms": sum(g_ms) / len(g_ms),
+                   "speedup_vs_sequential": (sum(s_ms) / sum(b_ms)),
+                   "speedup_vs_graph_sequential": (sum(g_ms) / sum(b_ms)),
+                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)"},
+        "clocks": clk, "gpu_launches": args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    batch.close()
+    for s in scenes:
+        s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -432,13 +530,17 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d"], default="robin3d",
-                    help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star")
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d"], default="robin3d",
+                    help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
+                         "batch2d: 256 batched 2D scenes vs sequential launches")
+    ap.add_argument("--batch-paths", type=int, default=32, help="paths per point of --workload batch2d")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch2d":
+        run_batch(args)
     else:
         run_ours(args)
 

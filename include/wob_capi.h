@@ -43,6 +43,7 @@ enum { WOB_DIRICHLET_PROBLEM = 0, WOB_NEUMANN_PROBLEM = 1, WOB_ROBIN_PROBLEM = 2
 enum { WOB_DIRICHLET = 0, WOB_NEUMANN = 1, WOB_ROBIN = 2 };
 
 typedef struct wob_scene_s *wob_scene;
+typedef struct wob_batch_s *wob_batch;
 
 /*
  * Solver parameters: the reference's Estimator constructor arguments (estimator.cuh:145-152)
@@ -183,6 +184,22 @@ int wob_solve_domain_host_noalloc(wob_scene scene, const wob_params *params, con
                                   void *stream);
 /* Largest n_points wob_solve_domain_host_noalloc accepts for dim 2 or 3. */
 int wob_noalloc_max_points(int dim, uint32_t *max_points);
+
+/*
+ * Batched domain solves: many scenes, each with its own parameters and evaluation points, in ONE
+ * persistent launch (no counterpart in the reference, where each app launches one scene per
+ * thrust::for_each, runtime_utils.cuh:146-151). scenes[i] (same dimension and device; they must
+ * outlive the batch) is solved with params[i] at n_points[i] points. Points, sums and sums of
+ * squares are concatenated over the scenes in order: scene i owns rows
+ * [n_points[0] + ... + n_points[i-1], ... + n_points[i]). Each scene's values are exactly those of
+ * wob_solve_domain on its rows (same random streams); path_offset_add is added to every scene's
+ * path_offset, so repeated solves continue the streams. Asynchronous on `stream`.
+ */
+int wob_batch_create(const wob_scene *scenes, const wob_params *params, const uint32_t *n_points,
+                     uint32_t n_scenes, wob_batch *out);
+int wob_batch_solve(wob_batch batch, const float *points, double *sum, double *sumsq,
+                    uint64_t *bounces, uint64_t path_offset_add, void *stream);
+int wob_batch_destroy(wob_batch batch);
 
 /*
  * Boundary estimator (replaces Estimator::compute_sample_path_contribution_boundary,

@@ -232,11 +232,50 @@ def test_every_tuned_configuration_is_bit_identical(engine, oracle, cuda, case):
     old = C.c_int32(0)
     engine.check(lib.wob_get_domain_config(v.value, C.byref(old)))
     try:
-        for cfg in range(3):
+        chosen, ms = scene.autotune_domain(p, cuda.from_numpy(sc["points"]).cuda(), len(sc["points"]))
+        assert 0 <= chosen < len(ms) and len(ms) >= 3 and all(m > 0 for m in ms)
+        for cfg in range(len(ms)):
             engine.check(lib.wob_set_domain_config(v.value, cfg))
             _check_domain(engine, oracle, cuda, sc, p)
-        chosen, ms = scene.autotune_domain(p, cuda.from_numpy(sc["points"]).cuda(), len(sc["points"]))
-        assert 0 <= chosen < 3 and len(ms) == 3 and all(m > 0 for m in ms)
     finally:
         lib.wob_set_domain_config(v.value, old.value)
     scene.close()
+
+
+def test_batched_launch_equals_sequential_solves(engine, cuda):
+    """One persistent launch over several scenes (mixed models, domains, estimators, sources and
+    sizes) gives each scene exactly what wob_solve_domain gives it."""
+    from wobtoolbox_gb300 import workloads as W
+    torch = cuda
+    specs = W.batch_scenes(8, seed=3, paths=64, path_length=4, point_range=(50, 300), grid_res=32)
+    scenes, params = [], []
+    for sc in specs:
+        s = engine.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+        if sc["volume"] is not None:
+            s.set_volume_cache(*sc["volume"])
+        scenes.append(s)
+        params.append(engine.EstimatorParams(seed=5, **dict(sc["params"], num_resampling_candidates=8
+                                                             if sc["params"]["num_resampling_candidates"] > 1 else 1)))
+    n_pts = [len(sc["points"]) for sc in specs]
+    pts = torch.from_numpy(np.concatenate([sc["points"] for sc in specs])).cuda()
+    batch = engine.SceneBatch(scenes, params, n_pts)
+    bs = torch.zeros(len(pts), 3, dtype=torch.float64, device="cuda")
+    bq = torch.zeros_like(bs)
+    bb = torch.zeros(1, dtype=torch.int64, device="cuda")
+    batch.solve(pts, bs, bq, bb, path_offset_add=128)
+    ss = torch.zeros_like(bs)
+    sq = torch.zeros_like(bs)
+    sb = torch.zeros_like(bb)
+    off = batch.offsets
+    for i, (s, p) in enumerate(zip(scenes, params)):
+        import dataclasses
+        q = dataclasses.replace(p, path_offset=p.path_offset + 128)
+        s.solve_domain(q, pts[off[i]:off[i + 1]], n_pts[i], ss[off[i]:off[i + 1]], sq[off[i]:off[i + 1]], sb)
+    torch.cuda.synchronize()
+    a, b = bs.cpu().numpy(), ss.cpu().numpy()
+    scale = np.sqrt(64 * sq.cpu().numpy()) + 1e-300
+    assert np.all(np.abs(a - b) <= 1e-12 * scale + 1e-300)
+    assert int(bb.item()) == int(sb.item())
+    batch.close()
+    for s in scenes:
+        s.close()

@@ -24,7 +24,7 @@ __all__ = [
     "Dirichlet", "Neumann", "Robin", "string_to_bie_model_type", "bie_model_type_to_string",
     "string_to_domain_type", "domain_type_to_string", "string_to_estimator_type", "estimator_type_to_string",
     "string_to_problem_type", "problem_type_to_string", "string_to_equation_kernel_type",
-    "EstimatorParams", "SceneHost", "WobError", "load",
+    "EstimatorParams", "SceneHost", "SceneBatch", "WobError", "load",
 ]
 
 # ---- enums (same values as the reference)
@@ -271,6 +271,38 @@ class SceneHost:
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             load().wob_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SceneBatch:
+    """Several scenes (same dimension), each with its own parameters and points, solved in one
+    persistent launch. Points / sums are concatenated over the scenes in order."""
+
+    def __init__(self, scenes, params, n_points):
+        lib = load()
+        n = len(scenes)
+        arr = (C.c_void_p * n)(*[s.handle.value for s in scenes])
+        prm = (_capi.wob_params * n)(*[p.to_c() for p in params])
+        npts = (C.c_uint32 * n)(*[int(x) for x in n_points])
+        h = C.c_void_p()
+        check(lib.wob_batch_create(arr, prm, npts, n, C.byref(h)))
+        self._h = h
+        self.scenes = list(scenes)  # keep them alive
+        self.offsets = np.concatenate([[0], np.cumsum(np.asarray(n_points, dtype=np.int64))])
+
+    def solve(self, points, sum_, sumsq=None, bounces=None, path_offset_add: int = 0, stream=None) -> None:
+        check(load().wob_batch_solve(self._h, _ptr(points), _ptr(sum_), _ptr(sumsq), _ptr(bounces),
+                                     int(path_offset_add), _stream_ptr(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().wob_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -29,6 +29,7 @@ EXPORTED = [
     "wob_solve_domain_host", "wob_solve_boundary", "wob_line_query", "wob_debug_domain_paths",
     "wob_debug_boundary_paths", "wob_solve_domain_host_noalloc", "wob_noalloc_max_points",
     "wob_autotune_domain", "wob_tunable_variant", "wob_set_domain_config", "wob_get_domain_config",
+    "wob_batch_create", "wob_batch_solve", "wob_batch_destroy",
 ]
 
 
@@ -93,6 +94,9 @@ def load() -> C.CDLL:
         "wob_tunable_variant": (C.c_int, [vp, P(wob_params), P(i32)]),
         "wob_set_domain_config": (C.c_int, [i32, i32]),
         "wob_get_domain_config": (C.c_int, [i32, P(i32)]),
+        "wob_batch_create": (C.c_int, [vp, vp, vp, u32, P(vp)]),
+        "wob_batch_solve": (C.c_int, [vp, vp, vp, vp, vp, u64, vp]),
+        "wob_batch_destroy": (C.c_int, [vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

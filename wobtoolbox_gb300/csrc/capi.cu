@@ -100,6 +100,16 @@ struct wob_scene_s {
     }
 };
 
+// A batch of scenes solved in one persistent launch (k_batch.cu). The scenes must outlive it.
+struct wob_batch_s {
+    int device = 0;
+    int dim = 0;
+    uint32_t n_scenes = 0;
+    uint64_t total_units = 0;
+    uint32_t total_points = 0;
+    DevBuf table;
+};
+
 namespace {
 
 struct DeviceGuard {
@@ -148,6 +158,7 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     w.seed = p->seed;
     w.path_offset = p->path_offset;
     w.point_offset = p->point_offset;
+    w.ppt = 1;
     return WOB_OK;
 }
 
@@ -624,6 +635,83 @@ int wob_tunable_variant(wob_scene s, const wob_params *params, int32_t *variant)
     int st = check_params(s, params, w);
     if (st != WOB_OK) return st;
     *variant = wobgb::tunable_domain_variant(s->host.dim, w);
+    return WOB_OK;
+}
+
+int wob_batch_create(const wob_scene *scenes, const wob_params *params, const uint32_t *n_points, uint32_t n_scenes,
+                     wob_batch *out) {
+    if (!out || !scenes || !params || !n_points || n_scenes == 0)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "scenes, params, n_points and out are required, n_scenes >= 1");
+    *out = nullptr;
+    const int dim = scenes[0] ? scenes[0]->host.dim : 0;
+    const int device = scenes[0] ? scenes[0]->device : 0;
+    std::vector<wobgb::BatchEntry<2>> t2;
+    std::vector<wobgb::BatchEntry<3>> t3;
+    uint64_t units = 0, points = 0;
+    for (uint32_t i = 0; i < n_scenes; i++) {
+        const wob_scene_s *s = scenes[i];
+        if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) + " is NULL");
+        if (s->host.dim != dim || s->device != device)
+            return fail(WOB_ERR_INVALID_ARGUMENT, "all scenes of a batch need the same dimension and device");
+        wobgb::WalkParams w;
+        int st = check_params(s, params + i, w);
+        if (st != WOB_OK) return fail(st, "scene " + std::to_string(i) + ": " + g_last_error);
+        w.ppt = wobgb::choose_ppt(n_points[i], w.n_paths);
+        const uint32_t slabs = (w.n_paths + 32u * w.ppt - 1u) / (32u * w.ppt);
+        if (dim == 2) {
+            wobgb::BatchEntry<2> e{};
+            e.view = s->view<2>(); e.params = w; e.unit_begin = units; e.point_begin = (uint32_t)points;
+            e.n_points = n_points[i]; e.slabs = slabs;
+            t2.push_back(e);
+        } else {
+            wobgb::BatchEntry<3> e{};
+            e.view = s->view<3>(); e.params = w; e.unit_begin = units; e.point_begin = (uint32_t)points;
+            e.n_points = n_points[i]; e.slabs = slabs;
+            t3.push_back(e);
+        }
+        units += (uint64_t)n_points[i] * slabs;
+        points += n_points[i];
+        if (points > 0xFFFFFFFFull) return fail(WOB_ERR_INVALID_ARGUMENT, "a batch holds at most 2^32 - 1 points");
+    }
+    wob_batch_s *b = new wob_batch_s();
+    b->device = device;
+    b->dim = dim;
+    b->n_scenes = n_scenes;
+    b->total_units = units;
+    b->total_points = (uint32_t)points;
+    DeviceGuard g(device);
+    cudaError_t e = dim == 2 ? upload(b->table, t2.data(), t2.size() * sizeof(t2[0]))
+                             : upload(b->table, t3.data(), t3.size() * sizeof(t3[0]));
+    if (e != cudaSuccess) {
+        delete b;
+        return fail_cuda(e, "uploading the batch table");
+    }
+    *out = b;
+    return WOB_OK;
+}
+
+int wob_batch_solve(wob_batch b, const float *points, double *sum, double *sumsq, uint64_t *bounces,
+                    uint64_t path_offset_add, void *stream) {
+    if (!b) return fail(WOB_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->total_points == 0) return WOB_OK;
+    if (!points || !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum are required");
+    DeviceGuard g(b->device);
+    cudaError_t e = b->dim == 2
+        ? wobgb::launch_batch_2d((const wobgb::BatchEntry<2> *)b->table.ptr, b->n_scenes, b->total_units, points, sum,
+                                 sumsq, (unsigned long long *)bounces, path_offset_add, (cudaStream_t)stream)
+        : wobgb::launch_batch_3d((const wobgb::BatchEntry<3> *)b->table.ptr, b->n_scenes, b->total_units, points, sum,
+                                 sumsq, (unsigned long long *)bounces, path_offset_add, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail_cuda(e, "launching the batched walk");
+    return WOB_OK;
+}
+
+int wob_batch_destroy(wob_batch b) {
+    if (!b) return WOB_OK;
+    {
+        DeviceGuard g(b->device);
+        b->table.release();
+    }
+    delete b;
     return WOB_OK;
 }
 

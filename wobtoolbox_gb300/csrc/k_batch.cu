@@ -1,0 +1,98 @@
+// Batched walk: many scenes, each with its own parameters and evaluation points, in one persistent
+// launch. A device table holds, per scene, its scene view, walk parameters and the first global
+// work unit; warps take global units in a grid-stride loop and find their scene by bisection over
+// the units' prefix. A unit is 32 * ppt paths of one point of one scene, so a warp never mixes
+// scenes and the per-scene work is exactly what a single-scene launch does (same paths, same
+// values).
+#include "kernels.cuh"
+
+namespace wobgb {
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) batch_domain_kernel(const BatchEntry<D> *__restrict__ table,
+                                                              uint32_t n_scenes, uint64_t total_units,
+                                                              const float *__restrict__ pts, double *__restrict__ sum,
+                                                              double *__restrict__ sumsq,
+                                                              unsigned long long *__restrict__ bounces,
+                                                              uint64_t path_offset_add) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long my_bounces = 0;
+    for (uint64_t u = warp; u < total_units; u += n_warps) {
+        uint32_t lo = 0, hi = n_scenes - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (table[mid].unit_begin <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchEntry<D> &e = table[lo];
+        const WalkParams p = e.params;
+        const uint64_t local = u - e.unit_begin;
+        const uint32_t pt = (uint32_t)(local / e.slabs);
+        const uint32_t span = 32u * p.ppt;
+        const uint32_t first = (uint32_t)(local % e.slabs) * span;
+        const uint32_t row = e.point_begin + pt;
+        V<D> x;
+#pragma unroll
+        for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)row * D + i);
+        double acc[D + 1], acc2[D + 1];
+#pragma unroll
+        for (int c = 0; c <= D; c++) { acc[c] = 0.0; acc2[c] = 0.0; }
+        for (uint32_t k = 0; k < p.ppt; k++) {
+            const uint32_t path = first + k * 32u + lane;
+            if (path < p.n_paths) {
+                float out[D + 1];
+                Walker<D, -1, kStratRuntime, true> w(e.view, p, kStreamDomain, p.point_offset + pt,
+                                                     p.path_offset + path_offset_add + path);
+                w.domain(x, out);
+                my_bounces += w.bounces;
+#pragma unroll
+                for (int c = 0; c <= D; c++) {
+                    const double v = (double)out[c];
+                    acc[c] += v;
+                    acc2[c] += v * v;
+                }
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c <= D; c++) {
+            const double sv = warp_sum(acc[c]);
+            const double qv = warp_sum(acc2[c]);
+            if (lane == 0) {
+                atomicAdd(sum + (size_t)row * (D + 1) + c, sv);
+                if (sumsq) atomicAdd(sumsq + (size_t)row * (D + 1) + c, qv);
+            }
+        }
+    }
+    if (bounces) {
+        __syncwarp();
+        const unsigned long long b = warp_sum_u64(my_bounces);
+        if (lane == 0 && b) atomicAdd(bounces, b);
+    }
+}
+
+template <int D>
+cudaError_t launch_batch_impl(const BatchEntry<D> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
+                              double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
+                              cudaStream_t stream) {
+    if (total_units == 0) return cudaSuccess;
+    auto k = batch_domain_kernel<D>;
+    k<<<persistent_grid(k, total_units), kBlock, 0, stream>>>(table, n_scenes, total_units, pts, sum, sumsq, bounces,
+                                                                path_offset_add);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_2d(const BatchEntry<2> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
+                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
+                            cudaStream_t stream) {
+    return launch_batch_impl<2>(table, n_scenes, total_units, pts, sum, sumsq, bounces, path_offset_add, stream);
+}
+cudaError_t launch_batch_3d(const BatchEntry<3> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
+                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
+                            cudaStream_t stream) {
+    return launch_batch_impl<3>(table, n_scenes, total_units, pts, sum, sumsq, bounces, path_offset_add, stream);
+}
+
+}  // namespace wobgb

@@ -28,6 +28,10 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 
 // kMinB: minimum resident blocks per SM requested from the register allocator (1 = no limit);
 // the autotuner chooses among the compiled values.
+//
+// A unit is 32 * ppt consecutive paths of one point: lane l runs paths l, l + 32, ... and keeps
+// its running (sum, sum of squares) in FP64 registers, so the FP64 warp reduction and the
+// atomics happen once per unit instead of once per 32 paths.
 template <int D, int kBie, int kStrat, bool kVol, bool kPerPath, int kMinB = 1>
 __global__ void __launch_bounds__(kBlock, kMinB) domain_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                         uint32_t n_points, double *__restrict__ sum,
@@ -37,35 +41,45 @@ __global__ void __launch_bounds__(kBlock, kMinB) domain_kernel(SceneView<D> s, W
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t slabs = (p.n_paths + 31u) / 32u;
+    const uint32_t span = 32u * p.ppt;
+    const uint32_t slabs = (p.n_paths + span - 1u) / span;
     const uint64_t units = (uint64_t)n_points * slabs;
     unsigned long long my_bounces = 0;
     for (uint64_t u = warp; u < units; u += n_warps) {
         const uint32_t pt = (uint32_t)(u / slabs);
-        const uint32_t path = (uint32_t)(u % slabs) * 32u + lane;
-        const bool active = path < p.n_paths;
-        float out[D + 1];
+        const uint32_t first = (uint32_t)(u % slabs) * span;
+        V<D> x;
 #pragma unroll
-        for (int c = 0; c <= D; c++) out[c] = 0.0f;
-        if (active) {
-            V<D> x;
+        for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)pt * D + i);
+        double acc[D + 1], acc2[D + 1];
 #pragma unroll
-            for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)pt * D + i);
-            Walker<D, kBie, kStrat, kVol> w(s, p, kStreamDomain, p.point_offset + pt, p.path_offset + path);
-            w.domain(x, out);
-            my_bounces += w.bounces;
-            if (kPerPath) {
+        for (int c = 0; c <= D; c++) { acc[c] = 0.0; acc2[c] = 0.0; }
+        for (uint32_t k = 0; k < p.ppt; k++) {
+            const uint32_t path = first + k * 32u + lane;
+            if (path < p.n_paths) {
+                float out[D + 1];
+                Walker<D, kBie, kStrat, kVol> w(s, p, kStreamDomain, p.point_offset + pt, p.path_offset + path);
+                w.domain(x, out);
+                my_bounces += w.bounces;
+                if (kPerPath) {
 #pragma unroll
-                for (int c = 0; c <= D; c++) per_path[((size_t)pt * p.n_paths + path) * (D + 1) + c] = out[c];
+                    for (int c = 0; c <= D; c++) per_path[((size_t)pt * p.n_paths + path) * (D + 1) + c] = out[c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c <= D; c++) {
+                        const double v = (double)out[c];
+                        acc[c] += v;
+                        acc2[c] += v * v;
+                    }
+                }
             }
         }
         if (!kPerPath) {
             __syncwarp();
 #pragma unroll
             for (int c = 0; c <= D; c++) {
-                const double v = active ? (double)out[c] : 0.0;
-                const double sv = warp_sum(v);
-                const double qv = warp_sum(v * v);
+                const double sv = warp_sum(acc[c]);
+                const double qv = warp_sum(acc2[c]);
                 if (lane == 0) {
                     atomicAdd(sum + (size_t)pt * (D + 1) + c, sv);
                     if (sumsq) atomicAdd(sumsq + (size_t)pt * (D + 1) + c, qv);
@@ -176,10 +190,12 @@ inline int persistent_grid(K kernel, uint64_t work_warps) {
 }
 
 template <int D, int kBie, int kStrat, bool kVol, int kMinB>
-cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p_in, const float *pts, uint32_t n_points,
                                   double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                   cudaStream_t stream) {
-    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
+    WalkParams p = p_in;
+    p.ppt = choose_ppt(n_points, p.n_paths);
+    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
     if (per_path) {
         auto k = domain_kernel<D, kBie, kStrat, kVol, true, kMinB>;
         k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);

@@ -9,12 +9,12 @@
 namespace wobgb {
 
 // ---- autotuned variants: 0 = 3D direct uniform, 1 = 2D double-layer line intersection,
-// 2 = 3D direct Neumann; configurations = minimum resident blocks {1 (no limit), 6, 8}.
+// 2 = 3D direct Neumann; configurations = minimum resident blocks {1 (no limit), 5, 6, 8}.
 namespace {
 std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}};
-const int kMinBOf[kTuneConfigs] = {1, 6, 8};
-const char *kConfigNames[kTuneConfigs] = {"128 threads, no register cap", "128 threads, >=6 blocks/SM",
-                                          "128 threads, >=8 blocks/SM"};
+const int kMinBOf[kTuneConfigs] = {1, 5, 6, 8};
+const char *kConfigNames[kTuneConfigs] = {"128 threads, no register cap", "128 threads, >=5 blocks/SM",
+                                          "128 threads, >=6 blocks/SM", "128 threads, >=8 blocks/SM"};
 }  // namespace
 
 int tunable_domain_variant(int dim, const WalkParams &p) {
@@ -38,6 +38,7 @@ template <int D, int kBie, int kStrat>
 static cudaError_t launch_cfg(int config, const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n,
                               double *sum, double *sumsq, unsigned long long *b, float *pp, cudaStream_t st) {
     switch (kMinBOf[config]) {
+    case 5: return launch_domain_variant<D, kBie, kStrat, false, 5>(s, p, pts, n, sum, sumsq, b, pp, st);
     case 6: return launch_domain_variant<D, kBie, kStrat, false, 6>(s, p, pts, n, sum, sumsq, b, pp, st);
     case 8: return launch_domain_variant<D, kBie, kStrat, false, 8>(s, p, pts, n, sum, sumsq, b, pp, st);
     default: return launch_domain_variant<D, kBie, kStrat, false, 1>(s, p, pts, n, sum, sumsq, b, pp, st);

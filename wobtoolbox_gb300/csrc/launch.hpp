@@ -34,7 +34,7 @@ cudaError_t launch_line_query_impl(const SceneView<D> &s, const float *origins, 
 // tunable_domain_variant() names the tunable variant a solve would use (-1: none);
 // set_domain_config() / domain_config() select the compiled configuration used from then on.
 constexpr int kNumTunable = 3;
-constexpr int kTuneConfigs = 3;
+constexpr int kTuneConfigs = 4;
 int tunable_domain_variant(int dim, const WalkParams &p);
 int domain_config(int variant);
 void set_domain_config(int variant, int config);
@@ -42,6 +42,23 @@ const char *domain_config_name(int variant, int config);
 cudaError_t launch_domain_config(int dim, int variant, int config, const void *scene_view, const WalkParams &p,
                                  const float *pts, uint32_t n_points, double *sum, double *sumsq,
                                  unsigned long long *bounces, float *per_path, cudaStream_t stream);
+
+// One scene of a batched launch (k_batch.cu).
+template <int D> struct BatchEntry;
+cudaError_t launch_batch_2d(const BatchEntry<2> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
+                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
+                            cudaStream_t stream);
+cudaError_t launch_batch_3d(const BatchEntry<3> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
+                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
+                            cudaStream_t stream);
+// Paths per lane of a warp unit: up to 8, keeping at least 16384 units so the grid-stride loop
+// still balances over the persistent grid.
+inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {
+    uint32_t ppt = 8;
+    while (ppt > 1 && ((uint64_t)n_points * ((n_paths + 32u * ppt - 1) / (32u * ppt)) < 16384u || 32u * ppt > n_paths))
+        ppt >>= 1;
+    return ppt;
+}
 
 // Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,

@@ -16,6 +16,7 @@ struct WalkParams {
     float eps, fk;
     uint64_t seed, path_offset;
     uint32_t point_offset;
+    uint32_t ppt;  // paths per lane in one warp unit (set by the launcher, >= 1)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -464,6 +465,15 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
         }
         return r;
     }
+};
+
+// One scene of a batched launch: its view, parameters, first global work unit, first point row
+// in the concatenated point / sum arrays, point count and units per point.
+template <int D> struct BatchEntry {
+    SceneView<D> view;
+    WalkParams params;
+    uint64_t unit_begin;
+    uint32_t point_begin, n_points, slabs, pad;
 };
 
 constexpr uint32_t kStreamDomain = 0u;

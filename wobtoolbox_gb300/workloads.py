@@ -211,3 +211,85 @@ def slice_points_z0(grid_res: int = 512, domain_size: float = 2.6) -> np.ndarray
 def inside_by_parity(counts_pos: np.ndarray) -> np.ndarray:
     """Inside a closed surface iff a half-line from the point crosses it an odd number of times."""
     return (counts_pos % 2) == 1
+
+
+# ------------------------------------------------------------------ batched 2D scenes
+def _star_points_inside(rng, lobes, amp, n, margin=0.9):
+    th = rng.uniform(0, 2 * np.pi, n)
+    rr = margin * (1 + amp * np.cos(lobes * th)) * np.sqrt(rng.uniform(0, 1, n))
+    return np.stack([rr * np.cos(th), rr * np.sin(th)], 1).astype(F32)
+
+
+def _star_points_outside(rng, lobes, amp, scale, n):
+    th = rng.uniform(0, 2 * np.pi, n)
+    r0 = scale * (1 + amp) * 1.1
+    rr = r0 + rng.uniform(0, 1.0, n)
+    return np.stack([rr * np.cos(th), rr * np.sin(th)], 1).astype(F32)
+
+
+def gaussian_source(centers, sigmas, amps, grid_res, domain_size):
+    """f = sum_k a_k exp(-|x - c_k|^2 / (2 s_k^2)) on the volume-cache grid (x fastest)."""
+    p = idx_to_domain_point(grid_res, domain_size, 2).astype(np.float64)
+    f = np.zeros(len(p))
+    for c, s, a in zip(centers, sigmas, amps):
+        f += a * np.exp(-((p - c) ** 2).sum(1) / (2 * s * s))
+    return f.astype(F32)
+
+
+def batch_scenes(n_scenes=256, seed=0, paths=1024, path_length=8, point_range=(1000, 64000), grid_res=128):
+    """Seeded batch of 2D star scenes: lobes U{3..9}, amplitude U[0.1, 0.35], segments log-uniform in
+    [64, 16384]; problem types cycle through interior Neumann, exterior Neumann, interior Robin,
+    exterior Robin (64 each for 256 scenes). Interior scenes carry a source f = 4 Gaussians
+    (sigma U[0.05, 0.2]) on a grid_res^2 volume cache over [-1.3, 1.3]^2; their Neumann data gets the
+    constant flux that makes the problem compatible (the flux of g equals the integral of f).
+    Neumann: single layer, forward estimator; Robin (alpha = 1): single layer, backward estimator,
+    64 resampling candidates, eps 1e-5 (the shipped configs data/config_general_2d_*_{Neumann,Robin}).
+    Boundary data from e^x cos y (interior) or x/|x|^2 (exterior). Returns a list of dicts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        lobes = int(rng.integers(3, 10))
+        amp = float(rng.uniform(0.1, 0.35))
+        n_seg = int(np.exp(rng.uniform(np.log(64), np.log(16384))))
+        kind = i % 4
+        exterior = kind in (1, 3)
+        robin = kind in (2, 3)
+        n_pts = int(rng.integers(point_range[0], point_range[1] + 1))
+        verts, normals = star_polygon(n_seg, lobes, amp)
+        scale = 1.0
+        if exterior:
+            scale = 0.5
+            verts = (verts * F32(scale)).astype(F32)
+            normals = segment_normals(verts)
+        flat = verts.reshape(-1, 2).astype(np.float64)
+        if exterior:
+            r2 = (flat ** 2).sum(1)
+            ug = np.stack([flat[:, 0] / r2, 1 / r2 - 2 * flat[:, 0] ** 2 / r2 ** 2, -2 * flat[:, 0] * flat[:, 1] / r2 ** 2], 1)
+        else:
+            ug = exp_cos(flat)
+        ug = ug.reshape(n_seg, 2, 3)
+        dudn = (ug[..., 1:] * normals[:, None, :].astype(np.float64)).sum(-1)
+        volume = None
+        if robin:
+            g = ug[..., 0] + dudn
+        else:
+            g = dudn
+        if not exterior:
+            cen = _star_points_inside(rng, lobes, amp, 4, 0.5).astype(np.float64)
+            sig = rng.uniform(0.05, 0.2, 4)
+            a = rng.uniform(-5, 5, 4)
+            f = gaussian_source(cen, sig, a, grid_res, 2.6)
+            volume = (grid_res, 2.6, f)
+            if not robin:
+                seg_len = np.linalg.norm(verts[:, 1] - verts[:, 0], axis=1)
+                integral = float(np.sum(a * 2 * np.pi * sig ** 2))
+                g = g + integral / seg_len.sum()
+        pts = _star_points_outside(rng, lobes, amp, scale, n_pts) if exterior else _star_points_inside(rng, lobes, amp, n_pts)
+        params = dict(bie_model=0, domain=1 if exterior else 0, estimator=0 if robin else 1,
+                      problem=2 if robin else 1, path_length=path_length, num_sample_paths=paths,
+                      num_resampling_candidates=64 if robin else 1, num_volume_samples=0 if exterior else 1,
+                      eps=float(F32(1e-5)) if robin else float(np.finfo(np.float32).eps))
+        out.append(dict(verts=verts, normals=normals, bvals=g.astype(F32), types=np.full(n_seg, 2 if robin else 1, np.int32),
+                        alphas=np.full((n_seg, 2), 1.0, F32) if robin else None, volume=volume, points=pts,
+                        params=params, lobes=lobes, amp=amp))
+    return out
