@@ -433,7 +433,8 @@ def run_batch(args):
     wob.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     paths = args.batch_paths
-    specs = W.batch_scenes(256, seed=SEED, paths=paths, path_length=8)
+    specs = W.batch_scenes(256, seed=SEED, paths=paths, path_length=8,
+                           point_range=(args.batch_points_min, args.batch_points_max))
     scenes, plist = [], []
     for sc in specs:
         s = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
@@ -504,7 +505,8 @@ def run_batch(args):
         "config": {"workload": "256 2D star scenes (lobes U{3..9}, amplitude U[0.1,0.35], segments log-uniform "
                                "[64,16384], points U[1k,64k]); interior/exterior x Neumann (SL forward) / Robin (SL "
                                "backward, RIS 64); 4 Gaussian sources in interior scenes",
-                   "points": total, "paths_per_point": paths, "path_length": 8,
+                   "points": total, "points_per_scene": [args.batch_points_min, args.batch_points_max],
+                   "paths_per_point": paths, "path_length": 8,
                    "batched_ms": sum(b_ms) / len(b_ms), "sequential_ms": sum(s_ms) / len(s_ms),
                    "graph_sequential_ms": sum(g_ms) / len(g_ms),
                    "speedup_vs_sequential": (sum(s_ms) / sum(b_ms)),
@@ -519,6 +521,130 @@ def run_batch(args):
         s.close()
 
 
+def run_cv(args):
+    """Learned control variate vs plain WoB, time to RMSE: 3D exterior Neumann problem on a displaced
+    icosphere with 327,680 triangles, u = sum_{k<3} q_k / (4 pi |x - s_k|) with s_k inside (radius
+    <= 0.5) and q_k ~ U[-1, 1]; forward single-layer estimator (the reference's choice for exterior
+    Neumann, data/config_general_3d_exterior_Neumann.json), 4 bounces. The network (32 Fourier
+    features of (x, n), 4 x 64 SiLU, scalar) is trained for 2000 Adam steps on 65,536 boundary
+    points x 256-path walk estimates of the density; evaluation at the 256^2 points of the z = 0
+    slice over [-2, 2]^2 outside the surface. Both estimators run progressive iterations; the RMSE
+    against the exact solution after each one is recorded against cumulative GPU time."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import cv
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rng = np.random.default_rng(SEED)
+    V, F, coeffs = W.displaced_icosphere(args.cv_subdiv, 0.15, 4, SEED)
+    verts, normals = W.mesh_elements(V, F)
+    dirs = rng.standard_normal((3, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    src = dirs * rng.uniform(0, 0.5, (3, 1))
+    q = rng.uniform(-1, 1, 3)
+    uv = W.point_sources(verts.reshape(-1, 3), src, q).reshape(len(F), 3, 4)
+    g = (uv[..., 1:] * normals[:, None, :].astype(np.float64)).sum(-1).astype(np.float32)
+    types = np.ones(len(F), np.int32)
+    scene = wob.SceneHost(verts, normals, g, types)
+    # evaluation points: z = 0 slice, outside the surface (half-line parity on the GPU)
+    cand = W.slice_points_z0(256, 4.0)
+    d_c = torch.from_numpy(cand).to(dev)
+    d_dir = torch.from_numpy(probe_dirs(len(cand))).to(dev)
+    counts = torch.zeros(len(cand), dtype=torch.int32, device=dev)
+    hits = torch.zeros(len(cand), 64, dtype=torch.int32, device=dev)
+    hp = torch.zeros(len(cand), 64, 3, dtype=torch.float32, device=dev)
+    scene.line_query(d_c, d_dir, len(cand), counts, hits, hp)
+    valid = torch.arange(64, device=dev)[None, :] < torch.clamp(counts, max=64)[:, None]
+    t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
+    outside = (((t > 0) & valid).sum(1) % 2 == 0).cpu().numpy()
+    del hits, hp
+    pts = np.ascontiguousarray(cand[outside])
+    exact = W.point_sources(pts, src, q)[:, 0]
+    n_pts = len(pts)
+    d_pts = torch.from_numpy(pts).to(dev)
+    base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.ExteriorDomain,
+                               estimator=wob.ForwardEstimator, problem=wob.NeumannProblem, path_length=4, seed=SEED)
+    paths = args.cv_paths
+    stream = torch.cuda.current_stream()
+
+    def progressive(solve, budget_s):
+        s = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+        b = torch.zeros(1, dtype=torch.int64, device=dev)
+        curve, total_ms, k = [], 0.0, 0
+        while total_ms / 1e3 < budget_s and k < 4096:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solve(dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths), s, b)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            k += 1
+            u = s[:, 0].cpu().numpy() / (k * paths)
+            curve.append((total_ms / 1e3, float(np.sqrt(np.mean((u - exact) ** 2))), k * paths))
+        return curve, int(b.item())
+
+    def time_to(curve, target):
+        for t_s, r, _ in curve:
+            if r <= target:
+                return t_s
+        return None
+
+    # warm up both kernels
+    tmp = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+    scene.solve_domain(dataclasses.replace(base, num_sample_paths=32), d_pts, n_pts, tmp)
+    plain_curve, plain_b = progressive(lambda p, s, b: scene.solve_domain(p, d_pts, n_pts, s, None, b, stream),
+                                       args.cv_budget)
+    t0 = time.perf_counter()
+    mlp, info = cv.train_density_cv(scene, base, n_train=65536, train_paths=256, steps=2000, batch=8192, lr=2e-3,
+                                    freq_sigma=args.cv_sigma, seed=SEED)
+    table = cv.element_cv_table(mlp, scene)
+    cv.set_control_variate(scene, table)
+    t_setup = time.perf_counter() - t0
+    cv.solve_domain_cv(scene, dataclasses.replace(base, num_sample_paths=32), d_pts, n_pts, tmp,
+                       n_potential=args.cv_npot, n_kernel=args.cv_nker)
+    cv_curve, cv_b = progressive(lambda p, s, b: cv.solve_domain_cv(scene, p, d_pts, n_pts, s, None, b,
+                                                                      n_potential=args.cv_npot,
+                                                                      n_kernel=args.cv_nker, stream=stream),
+                                 args.cv_budget)
+    final_plain, final_cv = plain_curve[-1][1], cv_curve[-1][1]
+    target = max(1e-3, max(min(r for _, r, _ in plain_curve), min(r for _, r, _ in cv_curve)) * 1.0001)
+    tp, tc = time_to(plain_curve, target), time_to(cv_curve, target)
+
+    def rmse_at(curve, t_s):
+        best = None
+        for tt, r, _ in curve:
+            if tt <= t_s:
+                best = r
+        return best
+
+    t_eq = min(plain_curve[-1][0], cv_curve[-1][0])
+    out = {
+        "metric": "time to RMSE vs analytic, plain vs learned-CV WoB (3D exterior Neumann, 327,680 triangles)",
+        "value": (tp / tc) if (tp and tc) else None, "unit": "x (plain time / CV time to the common RMSE target)",
+        "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "exterior Neumann, forward single layer, 4 bounces; CV: 32 Fourier features, "
+                               "4x64 SiLU, 2000 Adam steps on 65,536 x 256-path density estimates",
+                   "triangles": int(len(F)), "points": n_pts, "paths_per_iteration": paths,
+                   "cv_potential_samples": args.cv_npot, "cv_kernel_samples": args.cv_nker,
+                   "rmse_target": target, "plain_time_to_target_s": tp, "cv_time_to_target_s": tc,
+                   "cv_setup_s (labels + training + table)": t_setup, "train_info": {k: v for k, v in info.items()
+                                                                                   if k != "history"},
+                   "rmse_at_equal_time": {"t_s": t_eq, "plain": rmse_at(plain_curve, t_eq),
+                                          "cv": rmse_at(cv_curve, t_eq)},
+                   "final": {"plain": plain_curve[-1], "cv": cv_curve[-1]},
+                   "plain_bounces": plain_b, "cv_bounces": cv_b,
+                   "plain_curve": plain_curve[::max(1, len(plain_curve) // 12)],
+                   "cv_curve": cv_curve[::max(1, len(cv_curve) // 12)]},
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    mlp.close()
+    scene.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,10 +656,18 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d"], default="robin3d",
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d"], default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
     ap.add_argument("--batch-paths", type=int, default=32, help="paths per point of --workload batch2d")
+    ap.add_argument("--batch-points-min", type=int, default=1000)
+    ap.add_argument("--batch-points-max", type=int, default=64000)
+    ap.add_argument("--cv-subdiv", type=int, default=7, help="icosphere subdivision of --workload cv3d")
+    ap.add_argument("--cv-paths", type=int, default=256, help="paths per point per iteration of --workload cv3d")
+    ap.add_argument("--cv-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload cv3d")
+    ap.add_argument("--cv-npot", type=int, default=16)
+    ap.add_argument("--cv-nker", type=int, default=16)
+    ap.add_argument("--cv-sigma", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -541,6 +675,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch2d":
         run_batch(args)
+    elif args.workload == "cv3d":
+        run_cv(args)
     else:
         run_ours(args)
 

@@ -44,6 +44,7 @@ enum { WOB_DIRICHLET = 0, WOB_NEUMANN = 1, WOB_ROBIN = 2 };
 
 typedef struct wob_scene_s *wob_scene;
 typedef struct wob_batch_s *wob_batch;
+typedef struct wob_mlp_s *wob_mlp;
 
 /*
  * Solver parameters: the reference's Estimator constructor arguments (estimator.cuh:145-152)
@@ -213,6 +214,55 @@ int wob_solve_boundary(wob_scene scene, const wob_params *params, const float *p
                        const float *n, const float *interior_angle, const float *boundary_value,
                        const int32_t *boundary_type, const float *robin_alpha, uint32_t n_points,
                        double *sum, double *sumsq, uint64_t *bounces, void *stream);
+
+/*
+ * The walk's estimate of the unknown boundary function at boundary points: the value
+ * Estimator::compute_sample_unknown_boundary returns (estimator.cuh:232-357) -- the density of
+ * the indirect models, the missing boundary data of the direct model. Backward estimator only;
+ * arguments as wob_solve_boundary (sum / sumsq accumulated over the paths).
+ */
+int wob_solve_unknown_boundary(wob_scene scene, const wob_params *params, const float *p,
+                               const float *n, const float *interior_angle,
+                               const float *boundary_value, const int32_t *boundary_type,
+                               const float *robin_alpha, uint32_t n_points, double *sum,
+                               double *sumsq, uint64_t *bounces, void *stream);
+
+/*
+ * Learned control variate (no counterpart in the reference). A control-variate density sigma~
+ * is given per stored element (host array, storage order; e.g. the MLP below evaluated at the
+ * element centroids). wob_solve_domain_cv then runs the forward single-layer Neumann estimator
+ * (estimator.cuh:405-454) on the residual r = sigma - sigma~: u(x) = <G_x, sigma~> + <G_x, r>,
+ * where <G_x, sigma~> uses n_potential_samples uniform boundary samples and r is transported by
+ * the reference's forward walk from a residual source s + K sigma~ - sigma~ (K sigma~ from
+ * n_kernel_samples uniform samples). Unbiased for any sigma~; params must select
+ * IndirectSingleLayer / ForwardEstimator / NeumannProblem without a source term. per_path (device,
+ * [n_points][paths][dim+1], may be NULL) receives the per-path values instead of the sums.
+ */
+int wob_scene_set_control_variate(wob_scene scene, const float *values, uint32_t n_elems);
+int wob_solve_domain_cv(wob_scene scene, const wob_params *params, uint32_t n_potential_samples,
+                        uint32_t n_kernel_samples, const float *points, uint32_t n_points, double *sum,
+                        double *sumsq, uint64_t *bounces, float *per_path, void *stream);
+
+/*
+ * Fourier-feature MLP trained with the engine's own CUDA kernels: (x, n) in R^6 ->
+ * [sin, cos](2 pi B (x, n)) with B n_freq x 6 ~ N(0, freq_sigma^2) -> hidden_layers x (64, SiLU)
+ * -> out_dim. 2 n_freq must be 64. Parameters in FP32 (Adam master copy); every GEMM runs on
+ * BF16 tensor cores with FP32 accumulation. Device pointers; inputs [n][6], outputs [n][out_dim].
+ * wob_mlp_gradient: gradient of mean((y - t)^2) over all n * out_dim entries (grad [n_params],
+ * loss [1], device); wob_mlp_adam_step: the same gradient and one Adam update
+ * (beta 0.9 / 0.999, eps 1e-8). Parameter layout: per layer W [out][in] row-major, then b [out].
+ */
+int wob_mlp_create(uint32_t n_freq, uint32_t hidden_layers, uint32_t out_dim, float freq_sigma,
+                   uint64_t seed, wob_mlp *out);
+int wob_mlp_destroy(wob_mlp mlp);
+int wob_mlp_num_params(wob_mlp mlp, uint32_t *n);
+int wob_mlp_get_params(wob_mlp mlp, float *params, float *freqs);
+int wob_mlp_set_params(wob_mlp mlp, const float *params);
+int wob_mlp_forward(wob_mlp mlp, const float *inputs, uint32_t n, float *outputs, void *stream);
+int wob_mlp_gradient(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, float *grad,
+                     float *loss, void *stream);
+int wob_mlp_adam_step(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, float lr,
+                      float *loss, void *stream);
 
 /*
  * All hits of the infinite lines origin + t dir (the query of scene.cuh:483-486 / 787-790).

@@ -138,6 +138,66 @@ uint64_t solve_boundary(const Scene<D> &s, const oracle_params *op, const float 
     return total_bounces;
 }
 
+template <int D>
+uint64_t solve_domain_cv(const Scene<D> &s, const oracle_params *op, const float *sigma_t, unsigned n_pot,
+                         unsigned m_ker, const float *points, uint32_t n_points, double *sum, double *sumsq,
+                         float *per_path) {
+    const Params prm = to_params(op);
+    const uint32_t P = op->num_sample_paths;
+    uint64_t total_bounces = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total_bounces)
+    for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        Vec<D> x;
+        for (int k = 0; k < D; k++) x.v[k] = points[(size_t)i * D + k];
+        double s_[D + 1] = {}, q_[D + 1] = {};
+        for (uint32_t j = 0; j < P; j++) {
+            Rng rng(op->seed, kStreamDomain, op->point_offset + i, op->path_offset + j);
+            Estimator<D> est(&s, prm, &rng);
+            float out[D + 1];
+            est.domain_cv(x, sigma_t, n_pot, m_ker, out);
+            total_bounces += est.bounces;
+            for (int c = 0; c <= D; c++) {
+                s_[c] += (double)out[c];
+                q_[c] += (double)out[c] * (double)out[c];
+            }
+            if (per_path)
+                for (int c = 0; c <= D; c++) per_path[((size_t)i * P + j) * (D + 1) + c] = out[c];
+        }
+        if (sum) for (int c = 0; c <= D; c++) sum[(size_t)i * (D + 1) + c] += s_[c];
+        if (sumsq) for (int c = 0; c <= D; c++) sumsq[(size_t)i * (D + 1) + c] += q_[c];
+    }
+    return total_bounces;
+}
+
+template <int D>
+uint64_t solve_unknown(const Scene<D> &s, const oracle_params *op, const float *p, const float *n,
+                       const float *angle, const float *bv, const int32_t *type, const float *alpha,
+                       uint32_t n_points, double *sum, float *per_path) {
+    const Params prm = to_params(op);
+    const uint32_t P = op->num_sample_paths;
+    uint64_t total_bounces = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total_bounces)
+    for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        BoundaryPoint<D> x;
+        for (int k = 0; k < D; k++) { x.p.v[k] = p[(size_t)i * D + k]; x.n.v[k] = n[(size_t)i * D + k]; }
+        x.interior_angle = angle[i]; x.boundary_value = bv[i]; x.boundary_type = type[i];
+        x.robin_alpha = alpha ? alpha[i] : 0.0f;
+        double s_ = 0.0;
+        for (uint32_t j = 0; j < P; j++) {
+            Rng rng(op->seed, kStreamBoundary, op->point_offset + i, op->path_offset + j);
+            Estimator<D> est(&s, prm, &rng);
+            const float v = est.unknown_boundary(x);
+            total_bounces += est.bounces;
+            s_ += (double)v;
+            if (per_path) per_path[(size_t)i * P + j] = v;
+        }
+        if (sum) sum[i] += s_;
+    }
+    return total_bounces;
+}
+
 template <int D> struct Holder {
     Scene<D> scene;
     VolumeCache<D> vol;
@@ -182,6 +242,40 @@ uint64_t oracle_solve_boundary(int dim, uint32_t n_elems, const float *verts, co
     fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
     if (vol_res) { h->vol.build(vol_res, vol_size, vol_values); h->scene.vol = &h->vol; }
     return solve_boundary<3>(h->scene, params, p, n, angle, bv, type, alpha, n_points, sum, sumsq, per_path);
+}
+
+// Forward single-layer Neumann with a per-element control-variate density (storage order).
+uint64_t oracle_solve_domain_cv(int dim, uint32_t n_elems, const float *verts, const float *normals,
+                                const float *bvals, const float *alphas, const int32_t *types,
+                                const oracle_params *params, const float *sigma_t, uint32_t n_pot,
+                                uint32_t m_ker, const float *points, uint32_t n_points, double *sum,
+                                double *sumsq, float *per_path, int n_threads) {
+    set_threads(n_threads);
+    if (dim == 2) {
+        auto h = std::make_unique<Holder<2>>();
+        fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        return solve_domain_cv<2>(h->scene, params, sigma_t, n_pot, m_ker, points, n_points, sum, sumsq, per_path);
+    }
+    auto h = std::make_unique<Holder<3>>();
+    fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+    return solve_domain_cv<3>(h->scene, params, sigma_t, n_pot, m_ker, points, n_points, sum, sumsq, per_path);
+}
+
+// compute_sample_unknown_boundary at boundary points (the boundary density / unknown).
+uint64_t oracle_solve_unknown(int dim, uint32_t n_elems, const float *verts, const float *normals,
+                              const float *bvals, const float *alphas, const int32_t *types,
+                              const oracle_params *params, const float *p, const float *n, const float *angle,
+                              const float *bv, const int32_t *type, const float *alpha, uint32_t n_points,
+                              double *sum, float *per_path, int n_threads) {
+    set_threads(n_threads);
+    if (dim == 2) {
+        auto h = std::make_unique<Holder<2>>();
+        fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        return solve_unknown<2>(h->scene, params, p, n, angle, bv, type, alpha, n_points, sum, per_path);
+    }
+    auto h = std::make_unique<Holder<3>>();
+    fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+    return solve_unknown<3>(h->scene, params, p, n, angle, bv, type, alpha, n_points, sum, per_path);
 }
 
 // Brute-force line query: counts[i] = total hits, hits[i][0..63] = element indices in order,

@@ -49,6 +49,12 @@ def lib() -> C.CDLL:
         L.oracle_solve_boundary.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, u32, f32, vp,
                                             C.POINTER(oracle_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp,
                                             C.c_int]
+        L.oracle_solve_domain_cv.restype = u64
+        L.oracle_solve_domain_cv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
+                                             u32, vp, u32, vp, vp, vp, C.c_int]
+        L.oracle_solve_unknown.restype = u64
+        L.oracle_solve_unknown.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, vp, vp,
+                                           vp, vp, vp, u32, vp, vp, C.c_int]
         L.oracle_line_query.restype = None
         L.oracle_line_query.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp, vp]
         L.oracle_scene_cdfs.restype = None
@@ -140,6 +146,39 @@ def solve_boundary(el: Elements, params, p, n, angle, bv, btype, alpha=None, per
                                     _ptr(angle), _ptr(bv), _ptr(btype), _ptr(alpha), m, _ptr(s), _ptr(q), _ptr(pp),
                                     n_threads)
     return s, q, int(b), pp
+
+
+def solve_domain_cv(el: Elements, params, sigma_t, n_pot: int, m_ker: int, points, per_path: bool = False,
+                    n_threads: int = 0):
+    pts = _f32(points).reshape(-1, el.dim)
+    n = len(pts)
+    D = el.dim
+    sg = _f32(sigma_t).reshape(el.n)
+    s = np.zeros((n, D + 1))
+    q = np.zeros((n, D + 1))
+    pp = np.zeros((n, params.num_sample_paths, D + 1), dtype=np.float32) if per_path else None
+    ps = params_struct(params)
+    b = lib().oracle_solve_domain_cv(D, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
+                                     _ptr(el.types), C.byref(ps), _ptr(sg), n_pot, m_ker, _ptr(pts), n, _ptr(s),
+                                     _ptr(q), _ptr(pp), n_threads)
+    return s, q, int(b), pp
+
+
+def solve_unknown(el: Elements, params, p, n, angle, bv, btype, alpha=None, per_path: bool = False, n_threads: int = 0):
+    D = el.dim
+    p = _f32(p).reshape(-1, D)
+    m = len(p)
+    n = _f32(n).reshape(m, D)
+    angle, bv = _f32(angle).reshape(m), _f32(bv).reshape(m)
+    btype = np.ascontiguousarray(btype, dtype=np.int32).reshape(m)
+    alpha = None if alpha is None else _f32(alpha).reshape(m)
+    s = np.zeros(m)
+    pp = np.zeros((m, params.num_sample_paths), dtype=np.float32) if per_path else None
+    ps = params_struct(params)
+    b = lib().oracle_solve_unknown(D, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
+                                   _ptr(el.types), C.byref(ps), _ptr(p), _ptr(n), _ptr(angle), _ptr(bv),
+                                   _ptr(btype), _ptr(alpha), m, _ptr(s), _ptr(pp), n_threads)
+    return s, int(b), pp
 
 
 def line_query(el: Elements, origins, dirs):

@@ -973,6 +973,78 @@ template <int D> struct Estimator {
         }
     }
 
+    // Forward single-layer Neumann estimator with a control variate on the density (no counterpart in
+    // the reference). sigma_t[i] is the control-variate density on stored element i (piecewise
+    // constant). u(x) = <G_x, sigma_t> + <G_x, r>, r solving r = s_r + K r with the residual source
+    // s_r = s + K sigma_t - sigma_t. The first term: n_pot uniform samples; the second: the
+    // reference's forward transport (estimator.cuh:433-451) started from a uniform point y0 with
+    // weight A (s(y0) + K^ sigma_t(y0) - sigma_t(y0)), K^ from m_ker uniform samples.
+    BoundaryPoint<D> uniform_idx(float &ip, unsigned &idx) {
+        const float u1 = rng->uniform();
+        idx = binary_search(scene->area_cdf.data(), (unsigned)scene->elems.size(), u1);
+        const Element<D> &e = scene->elems[idx];
+        BoundaryPoint<D> r;
+        if constexpr (D == 2) {
+            const float u2 = rng->uniform();
+            r.p = interp2(e.v[0], e.v[1], u2); r.n = e.n; r.interior_angle = 0.5f;
+            r.boundary_value = interp2(e.bv[0], e.bv[1], u2); r.boundary_type = e.type;
+            r.robin_alpha = interp2(e.alpha[0], e.alpha[1], u2);
+        } else {
+            const float u2 = rng->uniform();
+            const float u3 = rng->uniform();
+            r.p = interp3(e.v[0], e.v[1], e.v[2], u2, u3); r.n = e.n; r.interior_angle = 0.5f;
+            r.boundary_value = interp3(e.bv[0], e.bv[1], e.bv[2], u2, u3); r.boundary_type = e.type;
+            r.robin_alpha = interp3(e.alpha[0], e.alpha[1], e.alpha[2], u2, u3);
+        }
+        ip = scene->total_area;
+        return r;
+    }
+    void domain_cv(const Vec<D> &x, const float *sigma_t, unsigned n_pot, unsigned m_ker, float out[D + 1]) {
+        float p1 = 0.0f;
+        Vec<D> g1 = vzero<D>();
+        for (unsigned k = 0; k < n_pot; k++) {
+            float ip; unsigned id;
+            const BoundaryPoint<D> y = uniform_idx(ip, id);
+            const float c = sigma_t[id] * ip;
+            p1 = p1 + bie.K.G(y.p, x) * c;
+            const Vec<D> g = bie.K.dG_dx(y.p, x);
+            for (int i = 0; i < D; i++) g1.v[i] = g1.v[i] + g.v[i] * c;
+        }
+        if (n_pot > 0) {
+            p1 = p1 / (float)n_pot;
+            for (int i = 0; i < D; i++) g1.v[i] = g1.v[i] / (float)n_pot;
+        }
+        float ip0; unsigned id0;
+        BoundaryPoint<D> y = uniform_idx(ip0, id0);
+        const float s0 = bie.fbk(y, y, ip0);
+        float ks = 0.0f;
+        for (unsigned j = 0; j < m_ker; j++) {
+            float ipz; unsigned idz;
+            BoundaryPoint<D> z = uniform_idx(ipz, idz);
+            BoundaryPoint<D> yc = y;
+            ks = ks + bie.fbu(yc, z, ipz, true) * sigma_t[idz];
+        }
+        if (m_ker > 0) ks = ks / (float)m_ker;
+        float w = ip0 * (s0 + ks - sigma_t[id0]);
+        float res = 0.0f;
+        Vec<D> gres = vzero<D>();
+        BoundaryPoint<D> y_prev;
+        float ip = 0.0f;
+        const unsigned L = prm.path_length;
+        for (unsigned m = 0; m < L; m++) {
+            bounces++;
+            if (m == L - 1) w = w * 0.5f;
+            res = res + w * bie.sdu(x, y, 1.0f);
+            const Vec<D> gu = bie.gdu(x, y, 1.0f);
+            for (int i = 0; i < D; i++) gres.v[i] = gres.v[i] + w * gu.v[i];
+            y_prev = y;
+            y = scene->sample_line_intersection(*rng, y_prev.p, ip);
+            w = bie.fbu(y, y_prev, ip, false) * w;
+        }
+        out[0] = p1 + res;
+        for (int i = 0; i < D; i++) out[1 + i] = g1.v[i] + gres.v[i];
+    }
+
     // compute_sample_path_contribution_boundary: backward (estimator.cuh:193-222),
     // forward (:456-496).
     float boundary(const BoundaryPoint<D> &x) {

@@ -29,7 +29,10 @@ EXPORTED = [
     "wob_solve_domain_host", "wob_solve_boundary", "wob_line_query", "wob_debug_domain_paths",
     "wob_debug_boundary_paths", "wob_solve_domain_host_noalloc", "wob_noalloc_max_points",
     "wob_autotune_domain", "wob_tunable_variant", "wob_set_domain_config", "wob_get_domain_config",
-    "wob_batch_create", "wob_batch_solve", "wob_batch_destroy",
+    "wob_batch_create", "wob_batch_solve", "wob_batch_destroy", "wob_solve_unknown_boundary",
+    "wob_scene_set_control_variate", "wob_solve_domain_cv", "wob_mlp_create", "wob_mlp_destroy",
+    "wob_mlp_num_params", "wob_mlp_get_params", "wob_mlp_set_params", "wob_mlp_forward", "wob_mlp_gradient",
+    "wob_mlp_adam_step",
 ]
 
 
@@ -97,6 +100,17 @@ def load() -> C.CDLL:
         "wob_batch_create": (C.c_int, [vp, vp, vp, u32, P(vp)]),
         "wob_batch_solve": (C.c_int, [vp, vp, vp, vp, vp, u64, vp]),
         "wob_batch_destroy": (C.c_int, [vp]),
+        "wob_solve_unknown_boundary": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp]),
+        "wob_scene_set_control_variate": (C.c_int, [vp, vp, u32]),
+        "wob_solve_domain_cv": (C.c_int, [vp, P(wob_params), u32, u32, vp, u32, vp, vp, vp, vp, vp]),
+        "wob_mlp_create": (C.c_int, [u32, u32, u32, f32, u64, P(vp)]),
+        "wob_mlp_destroy": (C.c_int, [vp]),
+        "wob_mlp_num_params": (C.c_int, [vp, P(u32)]),
+        "wob_mlp_get_params": (C.c_int, [vp, vp, vp]),
+        "wob_mlp_set_params": (C.c_int, [vp, vp]),
+        "wob_mlp_forward": (C.c_int, [vp, vp, u32, vp, vp]),
+        "wob_mlp_gradient": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
+        "wob_mlp_adam_step": (C.c_int, [vp, vp, vp, u32, f32, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

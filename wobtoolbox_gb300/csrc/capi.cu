@@ -51,11 +51,16 @@ cudaError_t upload(DevBuf &b, const void *src, size_t bytes) {
 
 }  // namespace
 
+namespace wobgb {
+void set_last_error(const char *msg) { g_last_error = msg; }
+}  // namespace wobgb
+
 struct wob_scene_s {
     int device = 0;
     wobgb::HostScene host;
     DevBuf elems, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
     DevBuf vol_values, vol_cdf, vol_guide;
+    DevBuf cv_table;  // control-variate density per stored element
     bool has_volume = false;
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
     float vol_size = 0.0f;
@@ -78,6 +83,7 @@ struct wob_scene_s {
         v.vol_cdf = (const float *)vol_cdf.ptr;
         v.vol_guide = (const uint4 *)vol_guide.ptr;
         v.err = (uint32_t *)err.ptr;
+        v.cv_table = (const float *)cv_table.ptr;
         v.n_elems = host.n;
         v.n_nodes = host.n_nodes;
         v.area_G = (uint32_t)(host.area_guide.size() / 4);
@@ -93,7 +99,7 @@ struct wob_scene_s {
     }
     void release_all() {
         for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
-                          &vol_cdf, &vol_guide, &ws})
+                          &vol_cdf, &vol_guide, &cv_table, &ws})
             b->release();
         if (ws_stream) cudaStreamDestroy(ws_stream);
         ws_stream = nullptr;
@@ -159,6 +165,9 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     w.path_offset = p->path_offset;
     w.point_offset = p->point_offset;
     w.ppt = 1;
+    w.mode = 0;
+    w.n_pot = 0;
+    w.m_ker = 0;
     return WOB_OK;
 }
 
@@ -713,6 +722,60 @@ int wob_batch_destroy(wob_batch b) {
     }
     delete b;
     return WOB_OK;
+}
+
+int wob_scene_set_control_variate(wob_scene s, const float *values, uint32_t n) {
+    if (!s || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and values are required");
+    if (n != s->host.n) return fail(WOB_ERR_INVALID_ARGUMENT, "need one value per element");
+    for (uint32_t i = 0; i < n; i++)
+        if (!(values[i] == values[i]) || values[i] > 3.0e38f || values[i] < -3.0e38f)
+            return fail(WOB_ERR_INVALID_ARGUMENT, "control-variate values must be finite");
+    DeviceGuard g(s->device);
+    cudaError_t e = upload(s->cv_table, values, (size_t)n * 4);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "uploading the control variate");
+}
+
+int wob_solve_domain_cv(wob_scene s, const wob_params *params, uint32_t n_potential_samples, uint32_t n_kernel_samples,
+                        const float *points, uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                        float *per_path, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (w.bie != WOB_INDIRECT_SINGLE_LAYER || w.estimator != WOB_FORWARD_ESTIMATOR || w.problem != WOB_NEUMANN_PROBLEM)
+        return fail(WOB_ERR_UNSUPPORTED, "the control-variate estimator is the forward single-layer Neumann estimator");
+    if (w.n_volume != 0) return fail(WOB_ERR_UNSUPPORTED, "the control-variate estimator takes no source term");
+    if (!s->cv_table.ptr) return fail(WOB_ERR_INVALID_ARGUMENT, "no control variate set (wob_scene_set_control_variate)");
+    if (n_points == 0) return WOB_OK;
+    if (!points || (!sum && !per_path)) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum (or per_path) are required");
+    w.n_pot = n_potential_samples;
+    w.m_ker = n_kernel_samples;
+    DeviceGuard g(s->device);
+    cudaError_t e = s->host.dim == 2
+        ? wobgb::launch_domain_cv_2d(s->view<2>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
+        : wobgb::launch_domain_cv_3d(s->view<3>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate walk");
+}
+
+int wob_solve_unknown_boundary(wob_scene s, const wob_params *params, const float *p, const float *n,
+                               const float *interior_angle, const float *boundary_value, const int32_t *boundary_type,
+                               const float *robin_alpha, uint32_t n_points, double *sum, double *sumsq,
+                               uint64_t *bounces, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (w.estimator != WOB_BACKWARD_ESTIMATOR) return fail(WOB_ERR_UNSUPPORTED, "the unknown boundary density comes from the backward estimator");
+    if (n_points == 0) return WOB_OK;
+    if (!p || !n || !interior_angle || !boundary_value || !boundary_type || !sum)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "p, n, interior_angle, boundary_value, boundary_type and sum are required");
+    w.mode = 1;
+    wobgb::BoundaryInput bin{p, n, interior_angle, boundary_value, boundary_type, robin_alpha};
+    DeviceGuard g(s->device);
+    cudaError_t e = s->host.dim == 2
+        ? wobgb::launch_boundary_2d(s->view<2>(), w, bin, n_points, sum, sumsq, (unsigned long long *)bounces, nullptr, (cudaStream_t)stream)
+        : wobgb::launch_boundary_3d(s->view<3>(), w, bin, n_points, sum, sumsq, (unsigned long long *)bounces, nullptr, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the unknown-boundary walk");
 }
 
 }  // extern "C"

@@ -181,6 +181,7 @@ template <int D> struct SceneView {
     const float *__restrict__ vol_values;
     const float *__restrict__ vol_cdf;
     const uint4 *__restrict__ vol_guide;
+    const float *__restrict__ cv_table;  // control-variate density per stored element (or null)
     uint32_t *err;                       // device error word (kErr* bits)
     uint32_t n_elems, n_nodes, area_G, bv_G;
     uint32_t vol_n, vol_G, vol_res, traversal_limit;
@@ -438,6 +439,17 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const Scene
 #pragma unroll
     for (int i = 0; i < D; i++) u[i] = rng.uniform();
     const uint32_t idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, u[0]);
+    inv_pdf = s.total_area;
+    return uniform_point<D>(load_elem<D>(s, idx), u);
+}
+
+// A uniform sample that also returns the stored index of its element.
+template <int D> __device__ __forceinline__ BPoint<D> sample_uniform_idx(const SceneView<D> &s, PathRng &rng, float &inv_pdf,
+                                                                        uint32_t &idx) {
+    float u[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) u[i] = rng.uniform();
+    idx = cdf_search(s.area_cdf, s.area_guide, s.area_G, u[0]);
     inv_pdf = s.total_area;
     return uniform_point<D>(load_elem<D>(s, idx), u);
 }

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kBlock) boundary_kernel(SceneView<D> s, WalkPa
             x.type = __ldg(bin.type + pt);
             x.alpha = bin.alpha ? __ldg(bin.alpha + pt) : 0.0f;
             Walker<D, kBie, kStrat, kVol> w(s, p, kStreamBoundary, p.point_offset + pt, p.path_offset + path);
-            out = w.boundary(x);
+            out = p.mode == 1 ? w.unknown_boundary(x) : w.boundary(x);
             my_bounces += w.bounces;
             if (kPerPath) per_path[(size_t)pt * p.n_paths + path] = out;
         }
@@ -143,6 +143,71 @@ __global__ void __launch_bounds__(kBlock) boundary_kernel(SceneView<D> s, WalkPa
         const unsigned long long b = warp_sum_u64(my_bounces);
         if (lane == 0 && b) atomicAdd(bounces, b);
     }
+}
+
+// Control-variate domain estimator (forward single layer, Neumann): as domain_kernel with
+// ppt = 1, the per-path estimate from Walker::domain_cv.
+template <int D>
+__global__ void __launch_bounds__(kBlock) domain_cv_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
+                                                           uint32_t n_points, double *__restrict__ sum,
+                                                           double *__restrict__ sumsq,
+                                                           unsigned long long *__restrict__ bounces,
+                                                           float *__restrict__ per_path) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t slabs = (p.n_paths + 31u) / 32u;
+    const uint64_t units = (uint64_t)n_points * slabs;
+    unsigned long long my_bounces = 0;
+    for (uint64_t u = warp; u < units; u += n_warps) {
+        const uint32_t pt = (uint32_t)(u / slabs);
+        const uint32_t path = (uint32_t)(u % slabs) * 32u + lane;
+        const bool active = path < p.n_paths;
+        float out[D + 1];
+#pragma unroll
+        for (int c = 0; c <= D; c++) out[c] = 0.0f;
+        if (active) {
+            V<D> x;
+#pragma unroll
+            for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)pt * D + i);
+            Walker<D, kSingleLayer, kStratFwdSlNeumann, false> w(s, p, kStreamDomain, p.point_offset + pt,
+                                                                 p.path_offset + path);
+            w.domain_cv(x, s.cv_table, out);
+            my_bounces += w.bounces;
+            if (per_path) {
+#pragma unroll
+                for (int c = 0; c <= D; c++) per_path[((size_t)pt * p.n_paths + path) * (D + 1) + c] = out[c];
+            }
+        }
+        if (!per_path) {
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c <= D; c++) {
+                const double v = active ? (double)out[c] : 0.0;
+                const double sv = warp_sum(v);
+                const double qv = warp_sum(v * v);
+                if (lane == 0) {
+                    atomicAdd(sum + (size_t)pt * (D + 1) + c, sv);
+                    if (sumsq) atomicAdd(sumsq + (size_t)pt * (D + 1) + c, qv);
+                }
+            }
+        }
+    }
+    if (bounces) {
+        __syncwarp();
+        const unsigned long long b = warp_sum_u64(my_bounces);
+        if (lane == 0 && b) atomicAdd(bounces, b);
+    }
+}
+
+template <int D>
+cudaError_t launch_domain_cv_impl(const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                  double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                  cudaStream_t stream) {
+    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
+    auto k = domain_cv_kernel<D>;
+    k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);
+    return cudaGetLastError();
 }
 
 template <int D>

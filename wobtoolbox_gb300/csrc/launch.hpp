@@ -43,6 +43,16 @@ cudaError_t launch_domain_config(int dim, int variant, int config, const void *s
                                  const float *pts, uint32_t n_points, double *sum, double *sumsq,
                                  unsigned long long *bounces, float *per_path, cudaStream_t stream);
 
+// Control-variate domain estimator (k_cv.cu).
+cudaError_t launch_domain_cv_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                cudaStream_t stream);
+cudaError_t launch_domain_cv_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                cudaStream_t stream);
+// Shared error message of the C ABI (capi.cu).
+void set_last_error(const char *msg);
+
 // One scene of a batched launch (k_batch.cu).
 template <int D> struct BatchEntry;
 cudaError_t launch_batch_2d(const BatchEntry<2> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,

@@ -16,7 +16,9 @@ struct WalkParams {
     float eps, fk;
     uint64_t seed, path_offset;
     uint32_t point_offset;
-    uint32_t ppt;  // paths per lane in one warp unit (set by the launcher, >= 1)
+    uint32_t ppt;   // paths per lane in one warp unit (set by the launcher, >= 1)
+    uint32_t mode;  // boundary kernel: 0 = boundary estimate, 1 = unknown boundary density
+    uint32_t n_pot, m_ker;  // control-variate estimator: samples of <G_x, sigma~> and of K sigma~
 };
 
 // ------------------------------------------------------------------------------------------
@@ -421,6 +423,64 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
             else y = sample_uniform<D>(s, rng, ip);
             w = fbu(y, y_prev, ip, false) * w;
         }
+    }
+
+    // Forward single-layer Neumann estimator with a per-element control-variate density sig
+    // (storage order; no counterpart in the reference): u(x) = <G_x, sig> + <G_x, r>, r = s_r + K r,
+    // s_r = s + K sig - sig. <G_x, sig> from n_pot uniform samples; <G_x, r> by the reference's
+    // forward transport (estimator.cuh:433-451) from a uniform source point y0 with weight
+    // A (s(y0) + K^ sig(y0) - sig(y0)), K^ sig from m_ker uniform samples.
+    __device__ __forceinline__ void domain_cv(const V<D> &x, const float *__restrict__ sig, float out[D + 1]) {
+        float p1 = 0.0f;
+        V<D> g1 = vzero<D>();
+        for (uint32_t k = 0; k < p.n_pot; k++) {
+            float ip;
+            uint32_t id;
+            const BPoint<D> y = sample_uniform_idx<D>(s, rng, ip, id);
+            const float c = __ldg(sig + id) * ip;
+            p1 = p1 + K.G(y.p, x) * c;
+            const V<D> g = K.dG_dx(y.p, x);
+#pragma unroll
+            for (int i = 0; i < D; i++) g1.v[i] = g1.v[i] + g.v[i] * c;
+        }
+        if (p.n_pot > 0) {
+            p1 = p1 / (float)p.n_pot;
+#pragma unroll
+            for (int i = 0; i < D; i++) g1.v[i] = g1.v[i] / (float)p.n_pot;
+        }
+        float ip0;
+        uint32_t id0;
+        BPoint<D> y = sample_uniform_idx<D>(s, rng, ip0, id0);
+        const float s0 = fbk(y, y, ip0);
+        float ks = 0.0f;
+        for (uint32_t j = 0; j < p.m_ker; j++) {
+            float ipz;
+            uint32_t idz;
+            BPoint<D> z = sample_uniform_idx<D>(s, rng, ipz, idz);
+            BPoint<D> yc = y;
+            ks = ks + fbu(yc, z, ipz, true) * __ldg(sig + idz);
+        }
+        if (p.m_ker > 0) ks = ks / (float)p.m_ker;
+        float w = ip0 * (s0 + ks - __ldg(sig + id0));
+        float res = 0.0f;
+        V<D> gres = vzero<D>();
+        BPoint<D> y_prev;
+        float ip = 0.0f;
+        const uint32_t L = p.path_length;
+        for (uint32_t m = 0; m < L; m++) {
+            bounces++;
+            if (m == L - 1) w = w * 0.5f;
+            res = res + w * sdu(x, y, 1.0f);
+            const V<D> gu = gdu(x, y, 1.0f);
+#pragma unroll
+            for (int i = 0; i < D; i++) gres.v[i] = gres.v[i] + w * gu.v[i];
+            y_prev = y;
+            y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
+            w = fbu(y, y_prev, ip, false) * w;
+        }
+        out[0] = p1 + res;
+#pragma unroll
+        for (int i = 0; i < D; i++) out[1 + i] = g1.v[i] + gres.v[i];
     }
 
     // compute_sample_path_contribution_boundary (estimator.cuh:193-222 backward, 456-496 forward)
