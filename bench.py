@@ -645,6 +645,179 @@ def run_cv(args):
     scene.close()
 
 
+def mixed_rhs_scene(subdiv, n_rhs, seed=SEED, dev=None):
+    """Interior mixed problem of the multi-RHS workload: displaced icosphere (as the Robin workload),
+    Dirichlet on faces whose centroid has z > 0, Neumann elsewhere; RHS r is the exact solution of
+    three exterior point sources (radius U[2, 4], strengths U[-1, 1]). Returns the element arrays, the
+    RHS table [n, 3, n_rhs] (per element vertex: u on Dirichlet faces, du/dn on Neumann faces) and
+    the sources [n_rhs, 3, 3] / strengths [n_rhs, 3]."""
+    from wobtoolbox_gb300 import workloads as W
+    V, F, _ = W.displaced_icosphere(subdiv, 0.15, 4, seed)
+    verts, normals = W.mesh_elements(V, F)
+    cz = V[F][:, :, 2].astype(np.float64).mean(1)
+    types = np.where(cz > 0, 0, 1).astype(np.int32)
+    rng = np.random.default_rng(seed + 1)
+    dirs = rng.standard_normal((n_rhs, 3, 3))
+    dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
+    src = dirs * rng.uniform(2.0, 4.0, (n_rhs, 3, 1))
+    q = rng.uniform(-1.0, 1.0, (n_rhs, 3))
+    if dev is None:
+        table = np.empty((len(F), 3, n_rhs), np.float32)
+        nrm = normals.astype(np.float64)
+        dirichlet = (types == 0)[:, None]
+        for r in range(n_rhs):
+            ug = W.point_sources(V, src[r], q[r])                   # [n_vertices, 4]: u, grad u
+            uf = ug[F]                                              # [n, 3, 4]
+            dudn = (uf[..., 1:] * nrm[:, None, :]).sum(-1)
+            table[:, :, r] = np.where(dirichlet, uf[..., 0], dudn)
+    else:  # the same formulas in float64 on the device
+        import torch
+        Vt = torch.from_numpy(V.astype(np.float64)).to(dev)
+        Ft = torch.from_numpy(F.astype(np.int64)).to(dev)
+        nt = torch.from_numpy(normals.astype(np.float64)).to(dev)
+        dt = torch.from_numpy(types == 0).to(dev)[:, None]
+        tt = torch.empty((len(F), 3, n_rhs), dtype=torch.float32, device=dev)
+        for r in range(n_rhs):
+            u = torch.zeros(len(V), dtype=torch.float64, device=dev)
+            gr = torch.zeros(len(V), 3, dtype=torch.float64, device=dev)
+            for k in range(3):
+                d = Vt - torch.from_numpy(src[r, k]).to(dev)[None, :]
+                rr = torch.linalg.norm(d, dim=1)
+                u += q[r, k] / (4.0 * np.pi * rr)
+                gr += (-q[r, k] / (4.0 * np.pi)) * d / (rr ** 3)[:, None]
+            dudn = (gr[Ft] * nt[:, None, :]).sum(-1)
+            tt[:, :, r] = torch.where(dt, u[Ft], dudn).float()
+        table = tt.cpu().numpy()
+    return dict(V=V, F=F, verts=verts, normals=normals, types=types, table=table, src=src, q=q)
+
+
+def inside_points(scene, n, lo, hi, seed, dev):
+    """n points uniform in the box [lo, hi]^3 and inside the surface (half-line crossing parity)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    out, have = [], 0
+    while have < n:
+        m = int((n - have) * 2.2) + 1024
+        cand = rng.uniform(lo, hi, (m, 3)).astype(np.float32)
+        d_c = torch.from_numpy(cand).to(dev)
+        d_dir = torch.from_numpy(probe_dirs(m)).to(dev)
+        counts = torch.zeros(m, dtype=torch.int32, device=dev)
+        hits = torch.zeros(m, 64, dtype=torch.int32, device=dev)
+        hp = torch.zeros(m, 64, 3, dtype=torch.float32, device=dev)
+        scene.line_query(d_c, d_dir, m, counts, hits, hp)
+        valid = torch.arange(64, device=dev)[None, :] < torch.clamp(counts, max=64)[:, None]
+        t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
+        inside = (((t > 0) & valid).sum(1) % 2 == 1).cpu().numpy()
+        out.append(cand[inside])
+        have += int(inside.sum())
+    return np.ascontiguousarray(np.concatenate(out)[:n])
+
+
+def run_multi_rhs(args):
+    """Multi-RHS workload: 3D interior mixed problem (Dirichlet on faces with centroid z > 0, Neumann
+    elsewhere) on a displaced icosphere with 1,310,720 triangles; 64 RHS, each the exact solution of
+    three exterior point sources (radius 2-4, strengths U[-1, 1]), share one set of walks. Estimator:
+    the reference's interior Mixed configuration (data/config_general_3d_interior_Mixed.json: single
+    layer, backward, 4 bounces, 64 RIS candidates, eps 1e-5, first-kind scaling 2). Evaluation: 10^6
+    random interior points. Progressive iterations of --mrhs-paths paths per point; after each, the
+    mean over the 64 RHS of the RMSE against the exact solutions is recorded against cumulative GPU
+    time. The same iteration is also timed as one scalar walk (one RHS) to give the cost of 64
+    separate solves."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    R = args.mrhs_rhs
+    t0 = time.perf_counter()
+    sc = mixed_rhs_scene(args.mrhs_subdiv, R, dev=dev)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scene = wob.SceneHost(sc["verts"], sc["normals"], sc["table"][:, :, 0], sc["types"])
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scene.set_rhs(sc["table"])
+    t_rhs = time.perf_counter() - t0
+    lo, hi = float(sc["V"].min()), float(sc["V"].max())
+    pts = inside_points(scene, args.mrhs_points, lo, hi, SEED + 2, dev)
+    n_pts = len(pts)
+    d_pts = torch.from_numpy(pts).to(dev)
+    # exact solutions [n_pts, R] (float64, on the device)
+    src = torch.from_numpy(sc["src"]).to(dev)
+    qq = torch.from_numpy(sc["q"]).to(dev)
+    xp = d_pts.double()
+    exact = torch.zeros(n_pts, R, dtype=torch.float64, device=dev)
+    for k in range(3):
+        dist = torch.linalg.norm(xp[:, None, :] - src[None, :, k, :], dim=2)
+        exact += qq[None, :, k] / (4.0 * np.pi * dist)
+    base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.InteriorDomain,
+                               estimator=wob.BackwardEstimator, problem=wob.MixedProblem, path_length=4,
+                               num_resampling_candidates=64, eps=1e-5, first_kind_equation_scaling_constant=2.0,
+                               seed=SEED)
+    paths = args.mrhs_paths
+    stream = torch.cuda.current_stream()
+    s = torch.zeros(n_pts, R, dtype=torch.float64, device=dev)
+    b = torch.zeros(1, dtype=torch.int64, device=dev)
+    # warm-up of both kernels (small path offsets beyond any timed one are not reused)
+    warm = dataclasses.replace(base, num_sample_paths=1, path_offset=1 << 40)
+    for _ in range(args.warmup):
+        scene.solve_domain_multi(warm, d_pts, n_pts, s, None, None, None, stream)
+    s1 = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+    for _ in range(args.warmup):
+        scene.solve_domain(warm, d_pts, n_pts, s1, None, None, stream)
+    # one scalar walk iteration (RHS 0 only), timed
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s1.zero_()
+    e0.record(stream)
+    scene.solve_domain(dataclasses.replace(base, num_sample_paths=paths), d_pts, n_pts, s1, None, None, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_scalar = e0.elapsed_time(e1) / 1e3
+    s.zero_()
+    curve, total, k = [], 0.0, 0
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.__enter__()
+    while (total < args.mrhs_budget and k < args.steps * 1000) or k < args.steps:
+        p = dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths)
+        e0.record(stream)
+        scene.solve_domain_multi(p, d_pts, n_pts, s, None, b, None, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1) / 1e3
+        k += 1
+        u = s / (k * paths)
+        rmse = torch.sqrt(((u - exact) ** 2).mean(0))
+        curve.append((total, float(rmse.mean().item()), k * paths))
+    sampler.__exit__(None, None, None)
+    clocks = sampler.summary()
+    t_iter = total / k
+    bounces = int(b.item())
+    # time to mean RMSE 1e-3, extrapolated from the last point with RMSE ~ 1/sqrt(paths)
+    t_last, r_last, n_last = curve[-1]
+    t_target = t_last * (r_last / 1e-3) ** 2
+    out = {
+        "metric": "multi-RHS WoB: 64 RHS sharing walks, 3D interior mixed problem, 1,310,720 triangles",
+        "value": bounces / total, "unit": "bounces/s (each bounce serves every RHS)",
+        "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "interior mixed (Dirichlet z>0, Neumann elsewhere), single layer, backward, 4 bounces, "
+                               "64 RIS candidates; 64 RHS of 3 exterior point sources each; 10^6 interior points",
+                   "triangles": int(len(sc["F"])), "points": n_pts, "rhs": R, "paths_per_iteration": paths,
+                   "iterations": k, "gpu_time_s": total, "bounces": bounces,
+                   "rhs_bounces_per_s": bounces * R / total,
+                   "iteration_ms": {"shared_walk_64_rhs": t_iter * 1e3, "scalar_walk_1_rhs": t_scalar * 1e3},
+                   "speedup_vs_separate_scalar_solves": R * t_scalar / t_iter,
+                   "mean_rmse_over_rhs": r_last, "paths_per_point": n_last,
+                   "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": t_target,
+                   "setup_s": {"rhs_data": t_data, "scene_build": t_build, "rhs_upload": t_rhs},
+                   "curve": curve[::max(1, len(curve) // 12)]},
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    scene.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -656,7 +829,7 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d"], default="robin3d",
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d"], default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
     ap.add_argument("--batch-paths", type=int, default=32, help="paths per point of --workload batch2d")
@@ -668,6 +841,12 @@ def main():
     ap.add_argument("--cv-npot", type=int, default=16)
     ap.add_argument("--cv-nker", type=int, default=16)
     ap.add_argument("--cv-sigma", type=float, default=1.0)
+    ap.add_argument("--mrhs-subdiv", type=int, default=8, help="icosphere subdivision of --workload mrhs3d")
+    ap.add_argument("--mrhs-rhs", type=int, default=64)
+    ap.add_argument("--mrhs-points", type=int, default=1000000)
+    ap.add_argument("--mrhs-paths", type=int, default=32, help="paths per point per iteration of --workload mrhs3d "
+                                                                "(a warp runs 32 paths of one point)")
+    ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds of --workload mrhs3d")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -677,6 +856,8 @@ def main():
         run_batch(args)
     elif args.workload == "cv3d":
         run_cv(args)
+    elif args.workload == "mrhs3d":
+        run_multi_rhs(args)
     else:
         run_ours(args)
 

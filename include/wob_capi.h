@@ -228,6 +228,35 @@ int wob_solve_unknown_boundary(wob_scene scene, const wob_params *params, const 
                                double *sumsq, uint64_t *bounces, void *stream);
 
 /*
+ * Multi-RHS walks (no counterpart in the reference, which solves one set of boundary data per
+ * run; the data enter through BoundaryPoint::boundary_value, points.hpp:32-39). Up to
+ * WOB_MAX_RHS right-hand sides share one set of paths: the estimator's sampling must not depend
+ * on the data -- backward IndirectSingleLayer (uniform or RIS sampling, estimator.cuh:276-334) or
+ * backward Direct with uniform sampling (estimator.cuh:335-347, i.e. not NeumannProblem) -- and
+ * there is no source term. The value of each path for RHS r is bit-identical to the scalar walk
+ * (wob_solve_domain / wob_solve_unknown_boundary) on the data of RHS r.
+ *
+ * wob_scene_set_rhs: host array values [n_elems][dim][n_rhs] in the caller's element order
+ * (per element vertex, as boundary_values of wob_scene_create); n_rhs = 0 removes the table.
+ * wob_solve_domain_multi: u(x) only (no gradient) at points [n_points][dim] (device);
+ * sum / sumsq [n_points][n_rhs] double, accumulated; per_path [n_points][paths][n_rhs] float
+ * (may be NULL; sums may be NULL when per_path is given).
+ * wob_solve_unknown_boundary_multi: the unknown boundary function at boundary points (arguments as
+ * wob_solve_unknown_boundary) whose data per RHS are boundary_values [n_points][n_rhs] (device).
+ */
+#define WOB_MAX_RHS 64
+int wob_scene_set_rhs(wob_scene scene, const float *values, uint32_t n_rhs);
+int wob_solve_domain_multi(wob_scene scene, const wob_params *params, const float *points,
+                           uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                           float *per_path, void *stream);
+int wob_solve_unknown_boundary_multi(wob_scene scene, const wob_params *params, const float *p,
+                                     const float *n, const float *interior_angle,
+                                     const float *boundary_values, const int32_t *boundary_type,
+                                     const float *robin_alpha, uint32_t n_points, double *sum,
+                                     double *sumsq, uint64_t *bounces, float *per_path,
+                                     void *stream);
+
+/*
  * Learned control variate (no counterpart in the reference). A control-variate density sigma~
  * is given per stored element (host array, storage order; e.g. the MLP below evaluated at the
  * element centroids). wob_solve_domain_cv then runs the forward single-layer Neumann estimator

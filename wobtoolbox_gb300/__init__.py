@@ -181,6 +181,7 @@ class SceneHost:
         check(lib.wob_scene_get_element_order(h, order.ctypes.data))
         self.element_order = order
         self._host = (v, nrm, bv, ty, al)
+        self.n_rhs = 0
 
     @property
     def handle(self):
@@ -253,6 +254,37 @@ class SceneHost:
     def line_query(self, origins, dirs, n_rays: int, counts, hits, hit_points=None, stream=None) -> None:
         check(load().wob_line_query(self._h, _ptr(origins), _ptr(dirs), int(n_rays), _ptr(counts), _ptr(hits),
                                     _ptr(hit_points), _stream_ptr(stream)))
+
+    # ---- multi-RHS walks: several sets of boundary data share one set of paths
+    def set_rhs(self, values) -> None:
+        """values [n_elems, dim, n_rhs] in the caller's element order (n_rhs <= 64); None removes them."""
+        if values is None:
+            check(load().wob_scene_set_rhs(self._h, None, 0))
+            self.n_rhs = 0
+            return
+        v = _f32(values)
+        if v.ndim != 3 or v.shape[0] != self.n_elems or v.shape[1] != self.dim:
+            raise ValueError("values must have shape [n_elems, dim, n_rhs]")
+        check(load().wob_scene_set_rhs(self._h, v.ctypes.data, int(v.shape[2])))
+        self.n_rhs = int(v.shape[2])
+
+    def solve_domain_multi(self, params: EstimatorParams, points, n_points: int, sum_=None, sumsq=None, bounces=None,
+                           per_path=None, stream=None) -> None:
+        """u at points for every RHS: sum_ / sumsq [n_points, n_rhs] FP64 (accumulated), per_path
+        [n_points, paths, n_rhs] (optional)."""
+        p = params.to_c()
+        check(load().wob_solve_domain_multi(self._h, C.byref(p), _ptr(points), int(n_points), _ptr(sum_),
+                                            _ptr(sumsq), _ptr(bounces), _ptr(per_path), _stream_ptr(stream)))
+
+    def solve_unknown_boundary_multi(self, params: EstimatorParams, p, n, interior_angle, boundary_values,
+                                     boundary_type, robin_alpha, n_points: int, sum_=None, sumsq=None, bounces=None,
+                                     per_path=None, stream=None) -> None:
+        """The unknown boundary function at boundary points for every RHS; boundary_values [n_points, n_rhs]."""
+        pp = params.to_c()
+        check(load().wob_solve_unknown_boundary_multi(self._h, C.byref(pp), _ptr(p), _ptr(n), _ptr(interior_angle),
+                                                      _ptr(boundary_values), _ptr(boundary_type), _ptr(robin_alpha),
+                                                      int(n_points), _ptr(sum_), _ptr(sumsq), _ptr(bounces),
+                                                      _ptr(per_path), _stream_ptr(stream)))
 
     # ---- host-buffer solve (synchronous), the end-to-end entry point
     def solve_domain_host(self, params: EstimatorParams, points: np.ndarray, sum_=None, sumsq=None):

@@ -7,6 +7,7 @@
 #include "../../include/wob_capi.h"
 
 #include "launch.hpp"
+#include "multi_rhs.hpp"
 #include "scene_host.hpp"
 #include "walk_generic.cuh"
 
@@ -61,6 +62,8 @@ struct wob_scene_s {
     DevBuf elems, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
     DevBuf vol_values, vol_cdf, vol_guide;
     DevBuf cv_table;  // control-variate density per stored element
+    DevBuf rhs;       // multi-RHS data [n][dim][n_rhs], storage order
+    uint32_t n_rhs = 0;
     bool has_volume = false;
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
     float vol_size = 0.0f;
@@ -99,7 +102,7 @@ struct wob_scene_s {
     }
     void release_all() {
         for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
-                          &vol_cdf, &vol_guide, &cv_table, &ws})
+                          &vol_cdf, &vol_guide, &cv_table, &rhs, &ws})
             b->release();
         if (ws_stream) cudaStreamDestroy(ws_stream);
         ws_stream = nullptr;
@@ -755,6 +758,89 @@ int wob_solve_domain_cv(wob_scene s, const wob_params *params, uint32_t n_potent
         ? wobgb::launch_domain_cv_2d(s->view<2>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
         : wobgb::launch_domain_cv_3d(s->view<3>(), w, points, n_points, sum, sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate walk");
+}
+
+int wob_scene_set_rhs(wob_scene s, const float *values, uint32_t n_rhs) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (n_rhs > wobgb::kMaxRhs) return fail(WOB_ERR_INVALID_ARGUMENT, "n_rhs must be at most WOB_MAX_RHS (64)");
+    DeviceGuard g(s->device);
+    if (n_rhs == 0) {
+        s->rhs.release();
+        s->n_rhs = 0;
+        return WOB_OK;
+    }
+    if (!values) return fail(WOB_ERR_INVALID_ARGUMENT, "values are required");
+    const uint32_t n = s->host.n, D = (uint32_t)s->host.dim;
+    const size_t row = (size_t)D * n_rhs;
+    std::vector<float> stored((size_t)n * row);
+    for (uint32_t i = 0; i < n; i++) {
+        const float *src = values + (size_t)s->host.order[i] * row;
+        for (size_t k = 0; k < row; k++) {
+            const float v = src[k];
+            if (!(v == v) || v > 3.0e38f || v < -3.0e38f) return fail(WOB_ERR_INVALID_ARGUMENT, "RHS values must be finite");
+            stored[(size_t)i * row + k] = v;
+        }
+    }
+    cudaError_t e = upload(s->rhs, stored.data(), stored.size() * 4);
+    if (e != cudaSuccess) {
+        s->n_rhs = 0;
+        return fail_cuda(e, "uploading the RHS table");
+    }
+    s->n_rhs = n_rhs;
+    return WOB_OK;
+}
+
+namespace {
+int check_multi(const wob_scene_s *s, const wob_params *params, wobgb::WalkParams &w) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (!wobgb::multi_rhs_supported(w))
+        return fail(WOB_ERR_UNSUPPORTED, "multi-RHS walks need sampling that ignores the boundary data: backward "
+                                         "IndirectSingleLayer, or backward Direct without NeumannProblem, and no source term");
+    if (s->n_rhs == 0) return fail(WOB_ERR_INVALID_ARGUMENT, "no RHS table set (wob_scene_set_rhs)");
+    return WOB_OK;
+}
+}  // namespace
+
+int wob_solve_domain_multi(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                           double *sumsq, uint64_t *bounces, float *per_path, void *stream) {
+    wobgb::WalkParams w;
+    int st = check_multi(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!points || (!sum && !per_path)) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum (or per_path) are required");
+    DeviceGuard g(s->device);
+    const wobgb::BoundaryInput bin{};
+    const float *tab = (const float *)s->rhs.ptr;
+    cudaError_t e = s->host.dim == 2
+        ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, false, points, bin, tab, nullptr, s->n_rhs, n_points, sum, sumsq,
+                                     (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
+        : wobgb::launch_multi_rhs_3d(s->view<3>(), w, false, points, bin, tab, nullptr, s->n_rhs, n_points, sum, sumsq,
+                                     (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS walk");
+}
+
+int wob_solve_unknown_boundary_multi(wob_scene s, const wob_params *params, const float *p, const float *n,
+                                     const float *interior_angle, const float *boundary_values,
+                                     const int32_t *boundary_type, const float *robin_alpha, uint32_t n_points,
+                                     double *sum, double *sumsq, uint64_t *bounces, float *per_path, void *stream) {
+    wobgb::WalkParams w;
+    int st = check_multi(s, params, w);
+    if (st != WOB_OK) return st;
+    if (n_points == 0) return WOB_OK;
+    if (!p || !n || !interior_angle || !boundary_values || !boundary_type || (!sum && !per_path))
+        return fail(WOB_ERR_INVALID_ARGUMENT,
+                    "p, n, interior_angle, boundary_values, boundary_type and sum (or per_path) are required");
+    DeviceGuard g(s->device);
+    const wobgb::BoundaryInput bin{p, n, interior_angle, nullptr, boundary_type, robin_alpha};
+    const float *tab = (const float *)s->rhs.ptr;
+    cudaError_t e = s->host.dim == 2
+        ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, true, nullptr, bin, tab, boundary_values, s->n_rhs, n_points, sum,
+                                     sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
+        : wobgb::launch_multi_rhs_3d(s->view<3>(), w, true, nullptr, bin, tab, boundary_values, s->n_rhs, n_points, sum,
+                                     sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS unknown-boundary walk");
 }
 
 int wob_solve_unknown_boundary(wob_scene s, const wob_params *params, const float *p, const float *n,

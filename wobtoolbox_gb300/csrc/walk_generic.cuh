@@ -108,9 +108,10 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
     PathRng rng;
     Green<D> K;
     uint32_t bounces;
+    bool stayed;  // the last fbu call kept the current point (first-kind roulette)
 
     __device__ __forceinline__ Walker(const SceneView<D> &s_, const WalkParams &p_, uint32_t stream, uint32_t point, uint64_t path)
-        : s(s_), p(p_), rng(p_.seed, stream, point, path), bounces(0) {
+        : s(s_), p(p_), rng(p_.seed, stream, point, path), bounces(0), stayed(false) {
         K.eps = p.eps;
     }
 
@@ -251,9 +252,10 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
         return r;
     }
     __device__ __forceinline__ float fbu(BPoint<D> &x, BPoint<D> &y, float ip, bool backward) {
+        stayed = false;
         if (model() == kDoubleLayer) return dtc() / (1.0f - ift(x.angle)) * ip * K.dG_dny(y.p, x.p, y.n);
         if (backward && x.type == kDirichlet) {
-            if (rng.uniform() * (1.0f + p.fk) < 1.0f) { y = x; return (1.0f + p.fk) * 1.0f; }
+            if (rng.uniform() * (1.0f + p.fk) < 1.0f) { y = x; stayed = true; return (1.0f + p.fk) * 1.0f; }
             ip = ip * ((1.0f + p.fk) / p.fk);
         } else if (!backward && y.type == kDirichlet) {
             if (rng.uniform() * (1.0f + p.fk) < 1.0f) { x = y; return (1.0f + p.fk) * 1.0f; }
