@@ -773,28 +773,49 @@ def run_multi_rhs(args):
     e1.record(stream)
     torch.cuda.synchronize()
     t_scalar = e0.elapsed_time(e1) / 1e3
-    s.zero_()
-    curve, total, k = [], 0.0, 0
     sampler = ClockSampler(torch.cuda.current_device())
     sampler.__enter__()
-    while (total < args.mrhs_budget and k < args.steps * 1000) or k < args.steps:
-        p = dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths)
-        e0.record(stream)
-        scene.solve_domain_multi(p, d_pts, n_pts, s, None, b, None, stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        total += e0.elapsed_time(e1) / 1e3
-        k += 1
-        u = s / (k * paths)
-        rmse = torch.sqrt(((u - exact) ** 2).mean(0))
-        curve.append((total, float(rmse.mean().item()), k * paths))
+
+    def progressive(solve, budget_s):
+        s.zero_()
+        b.zero_()
+        curve, total, k = [], 0.0, 0
+        while (total < budget_s and k < args.steps * 1000) or k < args.steps:
+            p = dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths)
+            e0.record(stream)
+            solve(p)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1) / 1e3
+            k += 1
+            u = s / (k * paths)
+            rmse = torch.sqrt(((u - exact) ** 2).mean(0))
+            curve.append((total, float(rmse.mean().item()), k * paths))
+        # time to mean RMSE 1e-3, extrapolated from the last point with RMSE ~ 1/sqrt(paths)
+        t_last, r_last, _ = curve[-1]
+        return curve, int(b.item()), t_last * (r_last / 1e-3) ** 2
+
+    plain_curve, bounces, plain_target = progressive(
+        lambda p: scene.solve_domain_multi(p, d_pts, n_pts, s, None, b, None, stream), args.mrhs_budget)
     sampler.__exit__(None, None, None)
     clocks = sampler.summary()
-    t_iter = total / k
-    bounces = int(b.item())
-    # time to mean RMSE 1e-3, extrapolated from the last point with RMSE ~ 1/sqrt(paths)
-    t_last, r_last, n_last = curve[-1]
-    t_target = t_last * (r_last / 1e-3) ** 2
+    total = plain_curve[-1][0]
+    t_iter = total / len(plain_curve)
+    # learned control variate: one MLP with an R-wide head trained on shared-walk density labels
+    from wobtoolbox_gb300 import cv
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mlp, info = cv.train_density_cv_multi(scene, sc["table"], base, n_train=131072, train_paths=128, steps=2000,
+                                          batch=8192, lr=2e-3, seed=SEED)
+    scene.set_rhs_control_variate(cv.element_cv_table(mlp, scene))
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        scene.solve_domain_multi_cv(warm, args.mrhs_npot, d_pts, n_pts, s, None, None, None, stream)
+    cv_curve, _, cv_target = progressive(
+        lambda p: scene.solve_domain_multi_cv(p, args.mrhs_npot, d_pts, n_pts, s, None, b, None, stream),
+        args.mrhs_budget)
+    mlp.close()
     out = {
         "metric": "multi-RHS WoB: 64 RHS sharing walks, 3D interior mixed problem, 1,310,720 triangles",
         "value": bounces / total, "unit": "bounces/s (each bounce serves every RHS)",
@@ -803,14 +824,20 @@ def run_multi_rhs(args):
         "config": {"workload": "interior mixed (Dirichlet z>0, Neumann elsewhere), single layer, backward, 4 bounces, "
                                "64 RIS candidates; 64 RHS of 3 exterior point sources each; 10^6 interior points",
                    "triangles": int(len(sc["F"])), "points": n_pts, "rhs": R, "paths_per_iteration": paths,
-                   "iterations": k, "gpu_time_s": total, "bounces": bounces,
+                   "iterations": len(plain_curve), "gpu_time_s": total, "bounces": bounces,
                    "rhs_bounces_per_s": bounces * R / total,
                    "iteration_ms": {"shared_walk_64_rhs": t_iter * 1e3, "scalar_walk_1_rhs": t_scalar * 1e3},
                    "speedup_vs_separate_scalar_solves": R * t_scalar / t_iter,
-                   "mean_rmse_over_rhs": r_last, "paths_per_point": n_last,
-                   "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": t_target,
-                   "setup_s": {"rhs_data": t_data, "scene_build": t_build, "rhs_upload": t_rhs},
-                   "curve": curve[::max(1, len(curve) // 12)]},
+                   "plain": {"mean_rmse_over_rhs": plain_curve[-1][1], "paths_per_point": plain_curve[-1][2],
+                             "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": plain_target,
+                             "curve": plain_curve[::max(1, len(plain_curve) // 10)]},
+                   "learned_cv": {"potential_samples": args.mrhs_npot, "setup_s (labels + training + table)": t_setup,
+                                  "train_info": info, "mean_rmse_over_rhs": cv_curve[-1][1],
+                                  "paths_per_point": cv_curve[-1][2],
+                                  "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": cv_target,
+                                  "curve": cv_curve[::max(1, len(cv_curve) // 10)]},
+                   "plain_over_cv_time_to_target": plain_target / (cv_target + t_setup),
+                   "setup_s": {"rhs_data": t_data, "scene_build": t_build, "rhs_upload": t_rhs}},
         "clocks": clocks,
     }
     if rank == 0:
@@ -846,7 +873,8 @@ def main():
     ap.add_argument("--mrhs-points", type=int, default=1000000)
     ap.add_argument("--mrhs-paths", type=int, default=32, help="paths per point per iteration of --workload mrhs3d "
                                                                 "(a warp runs 32 paths of one point)")
-    ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds of --workload mrhs3d")
+    ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload mrhs3d")
+    ap.add_argument("--mrhs-npot", type=int, default=4, help="potential samples of the learned CV (mrhs3d)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -257,6 +257,22 @@ int wob_solve_unknown_boundary_multi(wob_scene scene, const wob_params *params, 
                                      void *stream);
 
 /*
+ * Multi-RHS domain estimate with a control variate cv on the unknown boundary function (no
+ * counterpart in the reference): host array values [n_elems][n_rhs] in storage order, piecewise
+ * constant per element (e.g. the MLP with an n_rhs-wide head at the element centroids). The
+ * estimate u(x) = sdk(x, y1) + (mu(y0) - cv(y0)) sdu(x, y0) + sum_{i<n} (sdu(x, z_i) / n) cv(z_i)
+ * -- sdk / sdu the known / unknown domain terms of the model (bie_models.cuh), y0, y1 the start
+ * samples, z_i n_potential_samples uniform samples drawn after the walk -- is unbiased for any cv;
+ * the walk (and mu) is the one wob_solve_domain_multi runs. Setting a new RHS table removes cv.
+ */
+int wob_scene_set_rhs_control_variate(wob_scene scene, const float *values, uint32_t n_elems,
+                                      uint32_t n_rhs);
+int wob_solve_domain_multi_cv(wob_scene scene, const wob_params *params,
+                              uint32_t n_potential_samples, const float *points, uint32_t n_points,
+                              double *sum, double *sumsq, uint64_t *bounces, float *per_path,
+                              void *stream);
+
+/*
  * Learned control variate (no counterpart in the reference). A control-variate density sigma~
  * is given per stored element (host array, storage order; e.g. the MLP below evaluated at the
  * element centroids). wob_solve_domain_cv then runs the forward single-layer Neumann estimator

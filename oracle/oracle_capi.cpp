@@ -171,6 +171,33 @@ uint64_t solve_domain_cv(const Scene<D> &s, const oracle_params *op, const float
 }
 
 template <int D>
+uint64_t solve_domain_bcv(const Scene<D> &s, const oracle_params *op, const float *cv, unsigned n_pot,
+                          const float *points, uint32_t n_points, double *sum, double *sumsq, float *per_path) {
+    const Params prm = to_params(op);
+    const uint32_t P = op->num_sample_paths;
+    uint64_t total_bounces = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total_bounces)
+    for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        Vec<D> x;
+        for (int k = 0; k < D; k++) x.v[k] = points[(size_t)i * D + k];
+        double s_ = 0.0, q_ = 0.0;
+        for (uint32_t j = 0; j < P; j++) {
+            Rng rng(op->seed, kStreamDomain, op->point_offset + i, op->path_offset + j);
+            Estimator<D> est(&s, prm, &rng);
+            const float out = est.domain_bcv(x, cv, n_pot);
+            total_bounces += est.bounces;
+            s_ += (double)out;
+            q_ += (double)out * (double)out;
+            if (per_path) per_path[(size_t)i * P + j] = out;
+        }
+        if (sum) sum[i] += s_;
+        if (sumsq) sumsq[i] += q_;
+    }
+    return total_bounces;
+}
+
+template <int D>
 uint64_t solve_unknown(const Scene<D> &s, const oracle_params *op, const float *p, const float *n,
                        const float *angle, const float *bv, const int32_t *type, const float *alpha,
                        uint32_t n_points, double *sum, float *per_path) {
@@ -259,6 +286,23 @@ uint64_t oracle_solve_domain_cv(int dim, uint32_t n_elems, const float *verts, c
     auto h = std::make_unique<Holder<3>>();
     fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
     return solve_domain_cv<3>(h->scene, params, sigma_t, n_pot, m_ker, points, n_points, sum, sumsq, per_path);
+}
+
+// Backward estimator with a per-element control variate on the unknown boundary function (storage
+// order); u only: sum [n], sumsq [n], per_path [n][paths].
+uint64_t oracle_solve_domain_bcv(int dim, uint32_t n_elems, const float *verts, const float *normals,
+                                 const float *bvals, const float *alphas, const int32_t *types,
+                                 const oracle_params *params, const float *cv, uint32_t n_pot, const float *points,
+                                 uint32_t n_points, double *sum, double *sumsq, float *per_path, int n_threads) {
+    set_threads(n_threads);
+    if (dim == 2) {
+        auto h = std::make_unique<Holder<2>>();
+        fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        return solve_domain_bcv<2>(h->scene, params, cv, n_pot, points, n_points, sum, sumsq, per_path);
+    }
+    auto h = std::make_unique<Holder<3>>();
+    fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+    return solve_domain_bcv<3>(h->scene, params, cv, n_pot, points, n_points, sum, sumsq, per_path);
 }
 
 // compute_sample_unknown_boundary at boundary points (the boundary density / unknown).

@@ -52,6 +52,9 @@ def lib() -> C.CDLL:
         L.oracle_solve_domain_cv.restype = u64
         L.oracle_solve_domain_cv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
                                              u32, vp, u32, vp, vp, vp, C.c_int]
+        L.oracle_solve_domain_bcv.restype = u64
+        L.oracle_solve_domain_bcv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
+                                              vp, u32, vp, vp, vp, C.c_int]
         L.oracle_solve_unknown.restype = u64
         L.oracle_solve_unknown.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, vp, vp,
                                            vp, vp, vp, u32, vp, vp, C.c_int]
@@ -161,6 +164,22 @@ def solve_domain_cv(el: Elements, params, sigma_t, n_pot: int, m_ker: int, point
     b = lib().oracle_solve_domain_cv(D, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
                                      _ptr(el.types), C.byref(ps), _ptr(sg), n_pot, m_ker, _ptr(pts), n, _ptr(s),
                                      _ptr(q), _ptr(pp), n_threads)
+    return s, q, int(b), pp
+
+
+def solve_domain_bcv(el: Elements, params, cv, n_pot: int, points, per_path: bool = False, n_threads: int = 0):
+    """Backward estimator with a per-element control variate (storage order) on the unknown
+    boundary function; u only."""
+    pts = _f32(points).reshape(-1, el.dim)
+    n = len(pts)
+    c = _f32(cv).reshape(el.n)
+    s = np.zeros(n)
+    q = np.zeros(n)
+    pp = np.zeros((n, params.num_sample_paths), dtype=np.float32) if per_path else None
+    ps = params_struct(params)
+    b = lib().oracle_solve_domain_bcv(el.dim, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
+                                      _ptr(el.types), C.byref(ps), _ptr(c), n_pot, _ptr(pts), n, _ptr(s), _ptr(q),
+                                      _ptr(pp), n_threads)
     return s, q, int(b), pp
 
 

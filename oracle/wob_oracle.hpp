@@ -1045,6 +1045,28 @@ template <int D> struct Estimator {
         for (int i = 0; i < D; i++) out[1 + i] = g1.v[i] + gres.v[i];
     }
 
+    // Backward estimator with a control variate cv on the unknown boundary function (no
+    // counterpart in the reference; uniform start samples: single layer, or direct without
+    // NeumannProblem). cv[i] is constant on stored element i. u(x) = sdk(x, y1) +
+    // (mu(y0) - cv(y0)) sdu(x, y0) + sum_{i<n} (sdu(x, z_i) / n) cv(z_i): the walk is the plain
+    // estimator's (estimator.cuh:154-191, 232-357), the n uniform samples z_i are drawn after it.
+    float domain_bcv(const Vec<D> &x, const float *cv, unsigned n_pot) {
+        float ip, ip1;
+        unsigned id, id1;
+        const BoundaryPoint<D> y = uniform_idx(ip, id);
+        const BoundaryPoint<D> y1 = uniform_idx(ip1, id1);
+        float out = bie.sdk(x, y1, ip1);
+        const float mu = unknown_boundary(y);
+        out = out + (mu - cv[id]) * bie.sdu(x, y, ip);
+        for (unsigned k = 0; k < n_pot; k++) {
+            float ipz;
+            unsigned idz;
+            const BoundaryPoint<D> z = uniform_idx(ipz, idz);
+            out = out + (bie.sdu(x, z, ipz) / (float)n_pot) * cv[idz];
+        }
+        return out;
+    }
+
     // compute_sample_path_contribution_boundary: backward (estimator.cuh:193-222),
     // forward (:456-496).
     float boundary(const BoundaryPoint<D> &x) {

@@ -169,3 +169,34 @@ def test_unsupported_and_invalid(engine, cuda):
     with pytest.raises(engine.WobError):
         scene.solve_domain_multi(params, d_pts, len(sc["points"]), s)
     scene.close()
+
+
+@pytest.mark.parametrize("case", [CASES[0], CASES[2], CASES[5], CASES[7]], ids=_ids)
+def test_control_variate_paths_match_oracle(engine, oracle, cuda, case):
+    """Multi-RHS domain estimate with a per-element control variate per RHS: bit-identical per path
+    and RHS to the oracle's backward control-variate estimator on that RHS's data and column."""
+    torch = cuda
+    R = 3
+    sc, scene, rhs, params = _setup(engine, case, R, seed=4)
+    cvt = np.random.default_rng(5).uniform(-0.5, 0.5, (scene.n_elems, R)).astype(np.float32)
+    scene.set_rhs_control_variate(cvt)
+    pts = sc["points"][:6]
+    P = len(pts)
+    d_pts = torch.from_numpy(pts).cuda()
+    per = torch.full((P, params.num_sample_paths, R), float("nan"), dtype=torch.float32, device="cuda")
+    s = torch.zeros(P, R, dtype=torch.float64, device="cuda")
+    b = torch.zeros(1, dtype=torch.int64, device="cuda")
+    scene.solve_domain_multi_cv(params, 3, d_pts, P, s, None, b, per)
+    torch.cuda.synchronize()
+    got = per.cpu().numpy()
+    for r in range(R):
+        os_, _, ob, ref = oracle.solve_domain_bcv(_oracle_elems(oracle, scene, rhs[:, :, r]), params, cvt[:, r], 3,
+                                                  pts, per_path=True)
+        _compare(got[:, :, r], ref)
+        assert np.all(np.abs(s.cpu().numpy()[:, r] - os_) <= 1e-12 * np.abs(ref.astype(np.float64)).sum(1) + 1e-300)
+        assert int(b.item()) == ob
+    # a new RHS table removes the control variate
+    scene.set_rhs(rhs)
+    with pytest.raises(engine.WobError):
+        scene.solve_domain_multi_cv(params, 3, d_pts, P, s)
+    scene.close()

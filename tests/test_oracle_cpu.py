@@ -146,3 +146,26 @@ def test_estimators_unbiased_3d(oracle, combo):
         bias = np.abs(mean[:, c] - ex[:, c])
         ok = (np.abs(z) < 5.0) | (bias < 0.05 * np.abs(ex[:, c]) + 2e-3)
         assert np.all(ok), (c, z, mean[:, c], ex[:, c])
+
+
+@pytest.mark.parametrize("bie", [0, 2])
+def test_backward_control_variate_oracle(oracle, bie):
+    """Backward estimator with a per-element control variate on the unknown boundary function:
+    with cv = 0 it is the plain estimator path for path; with any cv its mean agrees with the plain
+    estimator's (the same walks, so the difference of the two per-path values is the CV's
+    zero-mean correction)."""
+    import wobtoolbox_gb300 as wob
+    sc = S.scene3d(3, False, subdiv=2)
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    p = wob.EstimatorParams(bie_model=bie, domain=0, estimator=0, problem=3, path_length=4, num_sample_paths=4000,
+                            seed=2, first_kind_equation_scaling_constant=2.0,
+                            eps=1e-5 if bie == 0 else float(np.finfo(np.float32).eps))
+    pts = sc["points"][:3]
+    _, _, _, plain = oracle.solve_domain(el, p, pts, per_path=True)
+    _, _, _, zero = oracle.solve_domain_bcv(el, p, np.zeros(el.n, np.float32), 4, pts, per_path=True)
+    assert np.array_equal(zero, plain[:, :, 0])
+    cv = np.random.default_rng(0).uniform(-0.5, 0.5, el.n).astype(np.float32)
+    _, _, _, withcv = oracle.solve_domain_bcv(el, p, cv, 4, pts, per_path=True)
+    d = withcv.astype(np.float64) - plain[:, :, 0]
+    z = d.mean(1) / (d.std(1) / np.sqrt(d.shape[1]))
+    assert np.all(np.abs(z) < 4.5), z

@@ -286,6 +286,20 @@ class SceneHost:
                                                       int(n_points), _ptr(sum_), _ptr(sumsq), _ptr(bounces),
                                                       _ptr(per_path), _stream_ptr(stream)))
 
+    def set_rhs_control_variate(self, values) -> None:
+        """values [n_elems, n_rhs] in storage order (one control-variate column per RHS)."""
+        v = _f32(values)
+        if v.ndim != 2:
+            raise ValueError("values must have shape [n_elems, n_rhs]")
+        check(load().wob_scene_set_rhs_control_variate(self._h, v.ctypes.data, int(v.shape[0]), int(v.shape[1])))
+
+    def solve_domain_multi_cv(self, params: EstimatorParams, n_potential: int, points, n_points: int, sum_=None,
+                              sumsq=None, bounces=None, per_path=None, stream=None) -> None:
+        p = params.to_c()
+        check(load().wob_solve_domain_multi_cv(self._h, C.byref(p), int(n_potential), _ptr(points), int(n_points),
+                                               _ptr(sum_), _ptr(sumsq), _ptr(bounces), _ptr(per_path),
+                                               _stream_ptr(stream)))
+
     # ---- host-buffer solve (synchronous), the end-to-end entry point
     def solve_domain_host(self, params: EstimatorParams, points: np.ndarray, sum_=None, sumsq=None):
         pts = _f32(points).reshape(-1, self.dim)

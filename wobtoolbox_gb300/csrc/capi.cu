@@ -63,6 +63,7 @@ struct wob_scene_s {
     DevBuf vol_values, vol_cdf, vol_guide;
     DevBuf cv_table;  // control-variate density per stored element
     DevBuf rhs;       // multi-RHS data [n][dim][n_rhs], storage order
+    DevBuf rhs_cv;    // multi-RHS control variate [n][n_rhs], storage order
     uint32_t n_rhs = 0;
     bool has_volume = false;
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
@@ -102,7 +103,7 @@ struct wob_scene_s {
     }
     void release_all() {
         for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
-                          &vol_cdf, &vol_guide, &cv_table, &rhs, &ws})
+                          &vol_cdf, &vol_guide, &cv_table, &rhs, &rhs_cv, &ws})
             b->release();
         if (ws_stream) cudaStreamDestroy(ws_stream);
         ws_stream = nullptr;
@@ -764,6 +765,7 @@ int wob_scene_set_rhs(wob_scene s, const float *values, uint32_t n_rhs) {
     if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
     if (n_rhs > wobgb::kMaxRhs) return fail(WOB_ERR_INVALID_ARGUMENT, "n_rhs must be at most WOB_MAX_RHS (64)");
     DeviceGuard g(s->device);
+    s->rhs_cv.release();
     if (n_rhs == 0) {
         s->rhs.release();
         s->n_rhs = 0;
@@ -811,14 +813,61 @@ int wob_solve_domain_multi(wob_scene s, const wob_params *params, const float *p
     if (n_points == 0) return WOB_OK;
     if (!points || (!sum && !per_path)) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum (or per_path) are required");
     DeviceGuard g(s->device);
-    const wobgb::BoundaryInput bin{};
-    const float *tab = (const float *)s->rhs.ptr;
-    cudaError_t e = s->host.dim == 2
-        ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, false, points, bin, tab, nullptr, s->n_rhs, n_points, sum, sumsq,
-                                     (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
-        : wobgb::launch_multi_rhs_3d(s->view<3>(), w, false, points, bin, tab, nullptr, s->n_rhs, n_points, sum, sumsq,
-                                     (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
+    wobgb::MultiRhsArgs a{};
+    a.unknown = false;
+    a.points = points;
+    a.rhs_table = (const float *)s->rhs.ptr;
+    a.n_rhs = s->n_rhs;
+    a.n_points = n_points;
+    a.sum = sum;
+    a.sumsq = sumsq;
+    a.bounces = (unsigned long long *)bounces;
+    a.per_path = per_path;
+    a.stream = (cudaStream_t)stream;
+    cudaError_t e = s->host.dim == 2 ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, a) : wobgb::launch_multi_rhs_3d(s->view<3>(), w, a);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS walk");
+}
+
+int wob_scene_set_rhs_control_variate(wob_scene s, const float *values, uint32_t n_elems, uint32_t n_rhs) {
+    if (!s || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and values are required");
+    if (s->n_rhs == 0) return fail(WOB_ERR_INVALID_ARGUMENT, "no RHS table set (wob_scene_set_rhs)");
+    if (n_elems != s->host.n || n_rhs != s->n_rhs)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "need [n_elems][n_rhs] values matching the scene and its RHS table");
+    const size_t cnt = (size_t)n_elems * n_rhs;
+    for (size_t i = 0; i < cnt; i++)
+        if (!(values[i] == values[i]) || values[i] > 3.0e38f || values[i] < -3.0e38f)
+            return fail(WOB_ERR_INVALID_ARGUMENT, "control-variate values must be finite");
+    DeviceGuard g(s->device);
+    cudaError_t e = upload(s->rhs_cv, values, cnt * 4);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "uploading the multi-RHS control variate");
+}
+
+int wob_solve_domain_multi_cv(wob_scene s, const wob_params *params, uint32_t n_potential_samples, const float *points,
+                              uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces, float *per_path,
+                              void *stream) {
+    wobgb::WalkParams w;
+    int st = check_multi(s, params, w);
+    if (st != WOB_OK) return st;
+    if (!s->rhs_cv.ptr) return fail(WOB_ERR_INVALID_ARGUMENT, "no control variate set (wob_scene_set_rhs_control_variate)");
+    if (n_potential_samples < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "n_potential_samples must be >= 1");
+    if (n_points == 0) return WOB_OK;
+    if (!points || (!sum && !per_path)) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum (or per_path) are required");
+    DeviceGuard g(s->device);
+    wobgb::MultiRhsArgs a{};
+    a.unknown = false;
+    a.points = points;
+    a.rhs_table = (const float *)s->rhs.ptr;
+    a.cv_table = (const float *)s->rhs_cv.ptr;
+    a.n_rhs = s->n_rhs;
+    a.n_potential = n_potential_samples;
+    a.n_points = n_points;
+    a.sum = sum;
+    a.sumsq = sumsq;
+    a.bounces = (unsigned long long *)bounces;
+    a.per_path = per_path;
+    a.stream = (cudaStream_t)stream;
+    cudaError_t e = s->host.dim == 2 ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, a) : wobgb::launch_multi_rhs_3d(s->view<3>(), w, a);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS control-variate walk");
 }
 
 int wob_solve_unknown_boundary_multi(wob_scene s, const wob_params *params, const float *p, const float *n,
@@ -833,13 +882,19 @@ int wob_solve_unknown_boundary_multi(wob_scene s, const wob_params *params, cons
         return fail(WOB_ERR_INVALID_ARGUMENT,
                     "p, n, interior_angle, boundary_values, boundary_type and sum (or per_path) are required");
     DeviceGuard g(s->device);
-    const wobgb::BoundaryInput bin{p, n, interior_angle, nullptr, boundary_type, robin_alpha};
-    const float *tab = (const float *)s->rhs.ptr;
-    cudaError_t e = s->host.dim == 2
-        ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, true, nullptr, bin, tab, boundary_values, s->n_rhs, n_points, sum,
-                                     sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream)
-        : wobgb::launch_multi_rhs_3d(s->view<3>(), w, true, nullptr, bin, tab, boundary_values, s->n_rhs, n_points, sum,
-                                     sumsq, (unsigned long long *)bounces, per_path, (cudaStream_t)stream);
+    wobgb::MultiRhsArgs a{};
+    a.unknown = true;
+    a.bin = wobgb::BoundaryInput{p, n, interior_angle, nullptr, boundary_type, robin_alpha};
+    a.rhs_table = (const float *)s->rhs.ptr;
+    a.rhs_input = boundary_values;
+    a.n_rhs = s->n_rhs;
+    a.n_points = n_points;
+    a.sum = sum;
+    a.sumsq = sumsq;
+    a.bounces = (unsigned long long *)bounces;
+    a.per_path = per_path;
+    a.stream = (cudaStream_t)stream;
+    cudaError_t e = s->host.dim == 2 ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, a) : wobgb::launch_multi_rhs_3d(s->view<3>(), w, a);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS unknown-boundary walk");
 }
 

@@ -17,12 +17,19 @@
 //
 // The per-path accumulators live in shared memory ([32 paths][64 RHS] floats per warp). Sums are
 // FP64 per (point, RHS), added once per warp unit.
+//
+// With a control variate cv (piecewise constant per stored element, one column per RHS; no
+// counterpart in the reference) the domain estimate becomes
+//   u(x) = sdk(x, y1) + (mu(y0) - cv(y0)) sdu(x, y0) + sum_{i < n} (sdu(x, z_i) / n) cv(z_i),
+// unbiased for any cv: the z_i are n uniform boundary samples drawn after the walk, so the walk
+// itself (and mu) is the plain estimator's. The potential samples go through the same tape.
+#pragma once
+
 #include "kernels.cuh"
 #include "multi_rhs.hpp"
 
 namespace wobgb {
-
-namespace {
+namespace mrhs {
 
 constexpr uint32_t kRefInput = 0xFFFFFFFFu;  // the evaluation point's own data (boundary input)
 constexpr uint32_t kRefZero = 0xFFFFFFFEu;   // the zero point an empty RIS selection returns
@@ -178,7 +185,8 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
 template <int D> struct RhsData {
     const float *__restrict__ table;  // [n_elems][D][R], storage order
     const float *__restrict__ input;  // [n_points][R]: data of the boundary evaluation points
-    uint32_t R;
+    const float *__restrict__ cv;     // [n_elems][R]: control variate per stored element (or null)
+    uint32_t R, n_pot;
 
     __device__ __forceinline__ float at(const PRef &r, uint32_t pt, uint32_t c) const {
         if (r.e == kRefInput) return __ldg(input + (size_t)pt * R + c);
@@ -187,16 +195,18 @@ template <int D> struct RhsData {
         if constexpr (D == 2) return interp2(__ldg(q), __ldg(q + R), r.k0);
         else return interp3(__ldg(q), __ldg(q + R), __ldg(q + 2 * R), r.k0, r.k1, r.k2);
     }
+    __device__ __forceinline__ float cv_at(uint32_t e, uint32_t c) const { return __ldg(cv + (size_t)e * R + c); }
 };
 
 constexpr uint32_t kFull = 0xffffffffu;
 
-template <int D, int kBie, int kStrat, bool kUnknown>
+template <int D, int kBie, int kStrat, bool kUnknown, bool kCV>
 __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                            BoundaryInput bin, RhsData<D> rd, uint32_t n_points,
                                                            double *__restrict__ sum, double *__restrict__ sumsq,
                                                            unsigned long long *__restrict__ bounces,
                                                            float *__restrict__ per_path) {
+    static_assert(!(kUnknown && kCV), "the control variate applies to the domain estimate");
     __shared__ float s_acc[kBlock / 32][32][kMaxRhs];
     __shared__ TapeEntry s_tape[kBlock / 32][32];
     const uint32_t lane = threadIdx.x & 31u;
@@ -228,6 +238,8 @@ __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkP
             PRef yref{kRefZero, 0.0f, 0.0f, 0.0f};
             PRef y1ref{kRefZero, 0.0f, 0.0f, 0.0f};
             float sdu_v = 0.0f, k0 = 0.0f;
+            uint32_t e0 = 0;
+            V<D> x = vzero<D>();
             if (active) {
                 if constexpr (kUnknown) {
 #pragma unroll
@@ -243,7 +255,6 @@ __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkP
                 } else {
                     // compute_sample_path_contribution_domain (estimator.cuh:154-191): start points y
                     // (unknown term) and y1 (known term), both uniform.
-                    V<D> x;
 #pragma unroll
                     for (int i = 0; i < D; i++) x.v[i] = __ldg(pts + (size_t)pt * D + i);
                     BPoint<D> y, y1;
@@ -258,6 +269,7 @@ __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkP
                     sdu_v = w.sdu(x, y, ip);
                     yprev = y;
                     yref = r;
+                    e0 = r.e;
                 }
             }
             // compute_sample_unknown_boundary (estimator.cuh:232-357), one bounce per step of the warp
@@ -302,32 +314,67 @@ __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkP
                 __syncwarp();
             }
             my_bounces += w.bounces;
-            // path values: out = sdk + mu * sdu (domain) or mu (unknown boundary)
+            // path values in place: out = sdk + (mu - cv(y0)) * sdu (domain) or mu (unknown boundary)
             const uint32_t act = __ballot_sync(kFull, active);
-            for (uint32_t j = 0; j < 32u; j++) {
-                if (!((act >> j) & 1u)) continue;
-                const float sdu_j = __shfl_sync(kFull, sdu_v, j);
-                PRef r1j;
-                float k0j = 0.0f;
-                if constexpr (kStrat == kStratUniform && !kUnknown) {
-                    k0j = __shfl_sync(kFull, k0, j);
-                    r1j.e = __shfl_sync(kFull, y1ref.e, j);
-                    r1j.k0 = __shfl_sync(kFull, y1ref.k0, j);
-                    r1j.k1 = __shfl_sync(kFull, y1ref.k1, j);
-                    r1j.k2 = __shfl_sync(kFull, y1ref.k2, j);
+            if constexpr (!kUnknown) {
+                for (uint32_t j = 0; j < 32u; j++) {
+                    if (!((act >> j) & 1u)) continue;
+                    const float sdu_j = __shfl_sync(kFull, sdu_v, j);
+                    const uint32_t e0j = __shfl_sync(kFull, e0, j);
+                    PRef r1j;
+                    float k0j = 0.0f;
+                    if constexpr (kStrat == kStratUniform) {
+                        k0j = __shfl_sync(kFull, k0, j);
+                        r1j.e = __shfl_sync(kFull, y1ref.e, j);
+                        r1j.k0 = __shfl_sync(kFull, y1ref.k0, j);
+                        r1j.k1 = __shfl_sync(kFull, y1ref.k1, j);
+                        r1j.k2 = __shfl_sync(kFull, y1ref.k2, j);
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const uint32_t c = lane + 32u * h;
+                        if (c < R) {
+                            float out0 = 0.0f;
+                            if constexpr (kStrat == kStratUniform) out0 = out0 + k0j * (rd.at(r1j, pt, c) + 0.0f);
+                            if constexpr (kCV) acc[j][c] = out0 + (acc[j][c] - rd.cv_at(e0j, c)) * sdu_j;
+                            else acc[j][c] = out0 + acc[j][c] * sdu_j;
+                        }
+                    }
                 }
+                if constexpr (kCV) {
+                    // potential of the control variate: n_pot uniform samples per path, after the walk
+                    for (uint32_t i = 0; i < rd.n_pot; i++) {
+                        if (active) {
+                            float ip;
+                            PRef r;
+                            const BPoint<D> z = sample_uniform_ref<D>(s, w.rng, ip, r);
+                            TapeEntry e;
+                            e.w = w.sdu(x, z, ip) / (float)rd.n_pot;
+                            e.a = r;
+                            tape[lane] = e;
+                        }
+                        __syncwarp();
+                        for (uint32_t v = act; v; v &= v - 1u) {
+                            const uint32_t j = __ffs(v) - 1u;
+                            const float pw = tape[j].w;
+                            const uint32_t ez = tape[j].a.e;
+#pragma unroll
+                            for (int h = 0; h < 2; h++) {
+                                const uint32_t c = lane + 32u * h;
+                                if (c < R) acc[j][c] = acc[j][c] + pw * rd.cv_at(ez, c);
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+            for (uint32_t v = act; v; v &= v - 1u) {
+                const uint32_t j = __ffs(v) - 1u;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const uint32_t c = lane + 32u * h;
                     if (c < R) {
-                        float out;
-                        if constexpr (kUnknown) {
-                            out = acc[j][c];
-                        } else {
-                            float out0 = 0.0f;
-                            if constexpr (kStrat == kStratUniform) out0 = out0 + k0j * (rd.at(r1j, pt, c) + 0.0f);
-                            out = out0 + acc[j][c] * sdu_j;
-                        }
+                        const float out = acc[j][c];
                         if (per_path) per_path[((size_t)pt * p.n_paths + path0 + j) * R + c] = out;
                         const double dv = (double)out;
                         a_sum[h] += dv;
@@ -354,54 +401,33 @@ __global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkP
     }
 }
 
-template <int D, int kBie, int kStrat, bool kUnknown>
+template <int D, int kBie, int kStrat, bool kUnknown, bool kCV>
 cudaError_t launch_one(const SceneView<D> &s, const WalkParams &p_in, const float *pts, const BoundaryInput &bin,
                        const RhsData<D> &rd, uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces,
                        float *per_path, cudaStream_t stream) {
     WalkParams p = p_in;
     p.ppt = choose_ppt(n_points, p.n_paths);
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
-    auto k = multi_rhs_kernel<D, kBie, kStrat, kUnknown>;
+    auto k = multi_rhs_kernel<D, kBie, kStrat, kUnknown, kCV>;
     k<<<persistent_grid(k, units), kBlock, 0, stream>>>(s, p, pts, bin, rd, n_points, sum, sumsq, bounces, per_path);
     return cudaGetLastError();
 }
 
 template <int D>
-cudaError_t launch_multi(const SceneView<D> &s, const WalkParams &p, bool unknown, const float *pts,
-                         const BoundaryInput &bin, const float *rhs_table, const float *rhs_input, uint32_t n_rhs,
-                         uint32_t n_points, double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
-                         cudaStream_t stream) {
-    const RhsData<D> rd{rhs_table, rhs_input, n_rhs};
+cudaError_t launch_multi(const SceneView<D> &s, const WalkParams &p, const MultiRhsArgs &a) {
+    const RhsData<D> rd{a.rhs_table, a.rhs_input, a.cv_table, a.n_rhs, a.n_potential};
     const bool sl = p.bie == kSingleLayer;
-    if (unknown) {
-        return sl ? launch_one<D, kSingleLayer, kStratSingleLayer, true>(s, p, pts, bin, rd, n_points, sum, sumsq, bounces, per_path, stream)
-                  : launch_one<D, kDirect, kStratUniform, true>(s, p, pts, bin, rd, n_points, sum, sumsq, bounces, per_path, stream);
-    }
-    return sl ? launch_one<D, kSingleLayer, kStratSingleLayer, false>(s, p, pts, bin, rd, n_points, sum, sumsq, bounces, per_path, stream)
-              : launch_one<D, kDirect, kStratUniform, false>(s, p, pts, bin, rd, n_points, sum, sumsq, bounces, per_path, stream);
+    cudaStream_t st = a.stream;
+#define WOB_MRHS_LAUNCH(BIE, STRAT, UNK, CV) \
+    launch_one<D, BIE, STRAT, UNK, CV>(s, p, a.points, a.bin, rd, a.n_points, a.sum, a.sumsq, a.bounces, a.per_path, st)
+    if (a.unknown) return sl ? WOB_MRHS_LAUNCH(kSingleLayer, kStratSingleLayer, true, false)
+                             : WOB_MRHS_LAUNCH(kDirect, kStratUniform, true, false);
+    if (a.cv_table) return sl ? WOB_MRHS_LAUNCH(kSingleLayer, kStratSingleLayer, false, true)
+                              : WOB_MRHS_LAUNCH(kDirect, kStratUniform, false, true);
+    return sl ? WOB_MRHS_LAUNCH(kSingleLayer, kStratSingleLayer, false, false)
+              : WOB_MRHS_LAUNCH(kDirect, kStratUniform, false, false);
+#undef WOB_MRHS_LAUNCH
 }
 
-}  // namespace
-
-bool multi_rhs_supported(const WalkParams &p) {
-    if (p.estimator != kBackward || p.n_volume != 0) return false;
-    const int st = strategy_of(p.bie, p.estimator, p.problem);
-    return st == kStratSingleLayer || (p.bie == kDirect && st == kStratUniform);
-}
-
-cudaError_t launch_multi_rhs_2d(const SceneView<2> &s, const WalkParams &p, bool unknown, const float *pts,
-                                const BoundaryInput &bin, const float *rhs_table, const float *rhs_input,
-                                uint32_t n_rhs, uint32_t n_points, double *sum, double *sumsq,
-                                unsigned long long *bounces, float *per_path, cudaStream_t stream) {
-    return launch_multi<2>(s, p, unknown, pts, bin, rhs_table, rhs_input, n_rhs, n_points, sum, sumsq, bounces,
-                           per_path, stream);
-}
-cudaError_t launch_multi_rhs_3d(const SceneView<3> &s, const WalkParams &p, bool unknown, const float *pts,
-                                const BoundaryInput &bin, const float *rhs_table, const float *rhs_input,
-                                uint32_t n_rhs, uint32_t n_points, double *sum, double *sumsq,
-                                unsigned long long *bounces, float *per_path, cudaStream_t stream) {
-    return launch_multi<3>(s, p, unknown, pts, bin, rhs_table, rhs_input, n_rhs, n_points, sum, sumsq, bounces,
-                           per_path, stream);
-}
-
+}  // namespace mrhs
 }  // namespace wobgb

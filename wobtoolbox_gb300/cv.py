@@ -109,7 +109,7 @@ def sample_boundary_points(verts: np.ndarray, normals: np.ndarray, bvals: np.nda
     p = (v[idx] * bary[:, :, None]).sum(1).astype(F32)
     g = (bvals[idx].astype(np.float64) * bary).sum(1).astype(F32)
     return dict(p=p, n=normals[idx].astype(F32), angle=np.full(n, 0.5, F32), bv=g, type=types[idx].astype(np.int32),
-                elem=idx)
+                elem=idx, bary=bary)
 
 
 def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256, steps: int = 2000,
@@ -168,8 +168,59 @@ def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256
     return mlp, info
 
 
+def train_density_cv_multi(scene, rhs_table: np.ndarray, params, n_train: int = 131072, train_paths: int = 128,
+                           steps: int = 2000, batch: int = 8192, lr: float = 2e-3, freq_sigma: float = 1.0,
+                           seed: int = 0, device=None):
+    """The multi-RHS variant of train_density_cv: one network with an n_rhs-wide head. Labels are the
+    unknown boundary function of every RHS at the training points from one set of shared walks
+    (wob_solve_unknown_boundary_multi); rhs_table [n_elems, dim, n_rhs] in the caller's element
+    order (the table given to scene.set_rhs). Returns (mlp, info)."""
+    import dataclasses
+
+    import torch
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    v, nrm, bv, ty, _ = scene._host[:5]
+    R = rhs_table.shape[2]
+    bp = sample_boundary_points(v, nrm, bv, ty, n_train, seed)
+    # data of every RHS at the training points: the same barycentric interpolation per RHS
+    data = np.einsum("nk,nkr->nr", bp["bary"].astype(np.float64),
+                     rhs_table[bp["elem"]].astype(np.float64)).astype(F32)
+    d = {k: torch.from_numpy(np.ascontiguousarray(bp[k])).to(dev) for k in ("p", "n", "angle", "type")}
+    d_data = torch.from_numpy(np.ascontiguousarray(data)).to(dev)
+    s = torch.zeros(n_train, R, dtype=torch.float64, device=dev)
+    b = torch.zeros(1, dtype=torch.int64, device=dev)
+    lp = dataclasses.replace(params, num_sample_paths=train_paths)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    scene.solve_unknown_boundary_multi(lp, d["p"], d["n"], d["angle"], d_data, d["type"], None, n_train, s, None, b)
+    torch.cuda.synchronize()
+    t_labels = time.perf_counter() - t0
+    labels = (s / train_paths).float().contiguous()
+    x = torch.cat([d["p"], d["n"]], dim=1).contiguous()
+    if scene.dim == 2:
+        z = torch.zeros(n_train, 1, device=dev)
+        x = torch.cat([d["p"], z, d["n"], z], dim=1).contiguous()
+    mlp = MLP(32, 4, R, freq_sigma, seed)
+    loss = torch.zeros(1, dtype=torch.float32, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    t1 = time.perf_counter()
+    for it in range(steps):
+        idx = torch.randint(0, n_train, (batch,), device=dev, generator=gen)
+        cur_lr = lr * 0.5 * (1 + np.cos(np.pi * it / steps))
+        mlp.adam_step(x[idx].contiguous(), labels[idx].contiguous(), batch, cur_lr, loss)
+        loss.zero_()
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    info = dict(n_train=n_train, train_paths=train_paths, steps=steps, batch=batch, t_labels_s=t_labels,
+                t_train_s=t_train, label_bounces=int(b.item()),
+                label_mean_abs=float(labels.abs().mean().item()))
+    return mlp, info
+
+
 def element_cv_table(mlp: MLP, scene, device=None) -> np.ndarray:
-    """The network at every stored element's centroid (with its normal), storage order."""
+    """The network at every stored element's centroid (with its normal), storage order:
+    [n_elems] for a scalar head, [n_elems, out_dim] otherwise."""
     import torch
     dev = device or torch.device("cuda", torch.cuda.current_device())
     v, nrm, _, _, _ = scene.stored_arrays()
@@ -180,10 +231,11 @@ def element_cv_table(mlp: MLP, scene, device=None) -> np.ndarray:
     else:
         inp = np.concatenate([c, nrm], 1)
     x = torch.from_numpy(np.ascontiguousarray(inp, dtype=F32)).to(dev)
-    out = torch.zeros(len(c), dtype=torch.float32, device=dev)
+    out = torch.zeros(len(c), mlp.out_dim, dtype=torch.float32, device=dev)
     mlp.forward(x, len(c), out)
     torch.cuda.synchronize()
-    return out.cpu().numpy()
+    o = out.cpu().numpy()
+    return o[:, 0].copy() if mlp.out_dim == 1 else o
 
 
 def set_control_variate(scene, values: np.ndarray) -> None:
