@@ -46,10 +46,12 @@ SEED = 0
 # Algorithmic bytes per bounce of this workload: two uniform boundary samples, each one element
 # record (76 B) plus one sampling-table entry (8 B).
 BYTES_PER_BOUNCE = 2 * (76 + 8)
-# DRAM bytes (read + write) of one walk launch, measured by ncu on the same kernel over 1/16 of
-# the evaluation points and scaled to a full launch by the bounces it processes; None until
-# captured (profiles/walk_uniform3d_robin_icosphere81920.md).
-TRAFFIC_BYTES_PER_BOUNCE = None
+# DRAM bytes (read + write) of one full-size walk launch of this workload, measured by ncu on the
+# timed launch itself (dram__bytes_read.sum + dram__bytes_write.sum, one pass; 16,758,016 +
+# 413,440 B, profiles/launches_robin3d_default_bench.md). The scene (6.6 MB of records, 1.3 MB of
+# guides) stays in L2, so DRAM traffic is the scene once plus the points and sums, not a per-bounce
+# quantity; it applies to the default (full) workload only.
+TRAFFIC_BYTES_PER_LAUNCH = 16_758_016 + 413_440
 WORKLOAD = ("3D interior Robin (du/dn + 2u = h), direct BIE, backward estimator, uniform sampling; "
             "displaced icosphere 81920 triangles; 512x512 z=0 slice over [-1.3,1.3]^2, inside points; "
             "4096 paths x 16 bounces per point per step")
@@ -396,8 +398,7 @@ def run_ours(args):
                          "frac": achieved / peak,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if peaks else
                          "fallback 6.8 TB/s",
-                         "traffic": None if TRAFFIC_BYTES_PER_BOUNCE is None else
-                         TRAFFIC_BYTES_PER_BOUNCE * bounces_per_launch,
+                         "traffic": None if (args.small or args.workload != "robin3d") else TRAFFIC_BYTES_PER_LAUNCH,
                          "algorithmic_bytes_per_bounce": bytes_per_bounce},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_pts * D * 4,
                     "d2h_bytes_per_step": n_pts * (D + 1) * 8 * 2 + 8 + 4, "steps": e2e_steps},
@@ -801,6 +802,15 @@ def run_multi_rhs(args):
     clocks = sampler.summary()
     total = plain_curve[-1][0]
     t_iter = total / len(plain_curve)
+    if args.mrhs_plain_only:
+        if rank == 0:
+            print(json.dumps({"metric": "multi-RHS WoB (plain leg only)", "value": bounces / total,
+                              "unit": "bounces/s (each bounce serves every RHS)", "n_gpus": world,
+                              "config": {"triangles": int(len(sc["F"])), "points": n_pts, "rhs": R,
+                                         "iteration_ms": t_iter * 1e3, "scalar_iteration_ms": t_scalar * 1e3,
+                                         "mean_rmse_over_rhs": plain_curve[-1][1]}, "clocks": clocks}), flush=True)
+        scene.close()
+        return
     # learned control variate: one MLP with an R-wide head trained on shared-walk density labels
     from wobtoolbox_gb300 import cv
     torch.cuda.synchronize()
@@ -851,7 +861,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-points", type=int, default=2048, help="CPU baseline sample (inside points)")
+    ap.add_argument("--cpu-points", type=int, default=8192, help="CPU baseline sample (inside points)")
     ap.add_argument("--cpu-paths", type=int, default=PATHS)
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -875,6 +885,7 @@ def main():
                                                                 "(a warp runs 32 paths of one point)")
     ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload mrhs3d")
     ap.add_argument("--mrhs-npot", type=int, default=4, help="potential samples of the learned CV (mrhs3d)")
+    ap.add_argument("--mrhs-plain-only", action="store_true", help="mrhs3d without the learned-CV leg (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -34,11 +34,40 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found")
 
 
+APPS = os.path.join(HERE, "apps")
+APP_BINARIES = {"general_2d": 2, "general_3d": 3}
+
+
+def app_path(name: str) -> str:
+    return os.path.join(OUT, name)
+
+
 def _deps() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(INCLUDE, "wob_capi.h"))
     files.append(os.path.abspath(__file__))
     return files
+
+
+def build_apps(force: bool = False) -> list[str]:
+    """The JSON apps (apps/general.cpp for dim 2 and 3), linked against the library."""
+    cxx = os.environ.get("CXX", "g++")
+    deps = [os.path.join(APPS, f) for f in os.listdir(APPS)] + [os.path.join(INCLUDE, "wob_gb300.hpp"),
+                                                                 os.path.join(INCLUDE, "wob_capi.h"), LIB]
+    jobs, outs = [], []
+    for name, dim in APP_BINARIES.items():
+        out = app_path(name)
+        outs.append(out)
+        if force or _stale(out, deps):
+            jobs.append([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall", f"-DWOB_APP_DIM={dim}",
+                         "-I", INCLUDE, os.path.join(APPS, "general.cpp"), "-o", out + ".tmp", "-L", OUT,
+                         "-lwob_gb300", "-Wl,-rpath,$ORIGIN"])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for j, proc in zip(jobs, ex.map(lambda j: subprocess.run(j, capture_output=True, text=True), jobs)):
+            if proc.returncode != 0:
+                raise RuntimeError("build failed:\n" + " ".join(j) + "\n" + proc.stdout + proc.stderr)
+            os.replace(j[j.index("-o") + 1], j[j.index("-o") + 1][:-4])
+    return outs
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -65,6 +94,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
     if not force and not ptxas_info and not _stale(LIB, deps):
+        build_apps()
         return LIB
     nvcc = nvcc_path()
     cxx = os.environ.get("CXX", "g++")
@@ -91,6 +121,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     tmp = LIB + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fPIC"])
     os.replace(tmp, LIB)
+    build_apps(force=True)
     return LIB
 
 
