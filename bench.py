@@ -855,6 +855,68 @@ def run_multi_rhs(args):
     scene.close()
 
 
+def run_build(args):
+    """Scene construction: host build (wob_scene_create) vs GPU build (wob_scene_create_device) of
+    the displaced icosphere with 4^subdiv * 20 triangles, and the line-intersection walk rate on
+    both scenes (their BVHs differ: median-split on the host, radix tree collapsed to 4-wide on the
+    GPU), measured with the 3D double-layer Dirichlet estimator on interior points."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    V, F, _ = W.displaced_icosphere(args.build_subdiv, 0.15, 4, SEED)
+    verts, nrm = W.mesh_elements(V, F)
+    n = len(F)
+    bv = W.point_sources(verts.reshape(-1, 3), np.array([[3.0, 0.5, 0.0]]), np.array([1.0]))[:, 0]
+    bv = bv.reshape(n, 3).astype(np.float32)
+    ty = np.zeros(n, np.int32)
+    t_host = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        hs = wob.SceneHost(verts, nrm, bv, ty)
+        t_host.append(time.perf_counter() - t0)
+        if len(t_host) < 2:
+            hs.close()
+    tv, tn, tb = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (verts, nrm, bv))
+    tt = torch.from_numpy(ty).to(dev)
+    t_dev = []
+    for _ in range(max(3, args.warmup)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ds = wob.SceneHost.build_on_device(tv, tn, tb, tt)
+        torch.cuda.synchronize()
+        t_dev.append(time.perf_counter() - t0)
+        if len(t_dev) < max(3, args.warmup):
+            ds.close()
+    pts = inside_points(hs, 4096, -0.6, 0.6, SEED + 3, dev)
+    d_pts = torch.from_numpy(pts).to(dev)
+    p = wob.EstimatorParams(bie_model=wob.IndirectDoubleLayer, path_length=4, num_sample_paths=256, seed=SEED)
+    rates = {}
+    for name, sc in (("host_bvh", hs), ("device_bvh", ds)):
+        s = torch.zeros(len(pts), 4, dtype=torch.float64, device=dev)
+        b = torch.zeros(1, dtype=torch.int64, device=dev)
+        sc.solve_domain(p, d_pts, len(pts), s)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sc.solve_domain(dataclasses.replace(p, path_offset=256), d_pts, len(pts), s, None, b)
+        e1.record()
+        torch.cuda.synchronize()
+        rates[name] = {"bounces_per_s": int(b.item()) / (e0.elapsed_time(e1) / 1e3),
+                       "nodes": sc.info()["n_nodes"], "depth": sc.info()["bvh_depth"]}
+    out = {"metric": "scene build time, host vs GPU", "value": min(t_host) / min(t_dev),
+           "unit": "x (host build time / GPU build time)", "n_gpus": world, "higher_is_better": True,
+           "config": {"workload": f"displaced icosphere, {n} triangles", "host_build_s": min(t_host),
+                      "device_build_s": min(t_dev), "device_build_all_s": t_dev,
+                      "line_intersection_walk (3D double layer, 4096 interior points x 256 paths x 4 bounces)": rates}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    hs.close()
+    ds.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -866,7 +928,8 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d"], default="robin3d",
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d"],
+                    default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
     ap.add_argument("--batch-paths", type=int, default=32, help="paths per point of --workload batch2d")
@@ -886,6 +949,7 @@ def main():
     ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload mrhs3d")
     ap.add_argument("--mrhs-npot", type=int, default=4, help="potential samples of the learned CV (mrhs3d)")
     ap.add_argument("--mrhs-plain-only", action="store_true", help="mrhs3d without the learned-CV leg (profiling)")
+    ap.add_argument("--build-subdiv", type=int, default=8, help="icosphere subdivision of --workload build3d")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -897,6 +961,8 @@ def main():
         run_cv(args)
     elif args.workload == "mrhs3d":
         run_multi_rhs(args)
+    elif args.workload == "build3d":
+        run_build(args)
     else:
         run_ours(args)
 

@@ -102,6 +102,19 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
                      const float *boundary_values, const float *robin_alphas,
                      const int32_t *boundary_types, wob_scene *out);
 int wob_scene_destroy(wob_scene scene);
+
+/*
+ * The same scene built on the GPU from DEVICE arrays (same layout as wob_scene_create; no
+ * counterpart in the reference, whose SceneHost and lbvh build run on the host, scene.cuh:264-299):
+ * Morton codes, a sort, a binary radix tree collapsed into the 4-wide layout, records, Kahan CDFs
+ * and guide tables, all on the device. The sampling tables are bit-identical to those of a host
+ * build over the same storage order; the BVH topology (and so the storage order) differs, which
+ * changes no hit set. Synchronises the stream. WOB_ERR_INVALID_ARGUMENT also when the tree is too
+ * deep for the traversal stack (then use wob_scene_create).
+ */
+int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                            const float *boundary_values, const float *robin_alphas,
+                            const int32_t *boundary_types, void *stream, wob_scene *out);
 int wob_scene_get_info(wob_scene scene, wob_scene_info *info);
 /* order[i] = caller index of the i-th stored element (n_elems entries, host memory). */
 int wob_scene_get_element_order(wob_scene scene, uint32_t *order);

@@ -183,6 +183,29 @@ class SceneHost:
         self._host = (v, nrm, bv, ty, al)
         self.n_rhs = 0
 
+    @classmethod
+    def build_on_device(cls, vertices, normals, boundary_values, boundary_types, robin_alphas=None, stream=None):
+        """The same scene built on the GPU (wob_scene_create_device) from CUDA tensors of the
+        constructor's shapes (float32; int32 types)."""
+        lib = load()
+        obj = cls.__new__(cls)
+        obj.dim = int(vertices.shape[1])
+        n = int(vertices.shape[0])
+        h = C.c_void_p()
+        check(lib.wob_scene_create_device(obj.dim, n, _ptr(vertices), _ptr(normals), _ptr(boundary_values),
+                                          _ptr(robin_alphas), _ptr(boundary_types), _stream_ptr(stream), C.byref(h)))
+        obj._h = h
+        obj.n_elems = n
+        order = np.empty(n, dtype=np.uint32)
+        check(lib.wob_scene_get_element_order(h, order.ctypes.data))
+        obj.element_order = order
+        cpu = lambda t: None if t is None else t.detach().cpu().numpy()
+        obj._host = (cpu(vertices), cpu(normals).reshape(n, obj.dim), cpu(boundary_values).reshape(n, obj.dim),
+                     cpu(boundary_types).reshape(n),
+                     None if robin_alphas is None else cpu(robin_alphas).reshape(n, obj.dim))
+        obj.n_rhs = 0
+        return obj
+
     @property
     def handle(self):
         return self._h

@@ -8,6 +8,7 @@
 
 #include "launch.hpp"
 #include "multi_rhs.hpp"
+#include "scene_build_gpu.hpp"
 #include "scene_host.hpp"
 #include "walk_generic.cuh"
 
@@ -66,6 +67,7 @@ struct wob_scene_s {
     DevBuf rhs_cv;    // multi-RHS control variate [n][n_rhs], storage order
     uint32_t n_rhs = 0;
     bool has_volume = false;
+    uint32_t area_G = 0, bv_G = 0;  // guide-table records
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
     float vol_size = 0.0f;
     bool all_dirichlet = true;
@@ -90,8 +92,8 @@ struct wob_scene_s {
         v.cv_table = (const float *)cv_table.ptr;
         v.n_elems = host.n;
         v.n_nodes = host.n_nodes;
-        v.area_G = (uint32_t)(host.area_guide.size() / 4);
-        v.bv_G = (uint32_t)(host.bv_guide.size() / 4);
+        v.area_G = area_G;
+        v.bv_G = bv_G;
         v.vol_n = vol_n;
         v.vol_G = vol_G;
         v.vol_res = vol_res;
@@ -266,6 +268,8 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
         return fail_cuda(e, "cudaGetDevice");
     }
     const wobgb::HostScene &h = s->host;
+    s->area_G = (uint32_t)(h.area_guide.size() / 4);
+    s->bv_G = (uint32_t)(h.bv_guide.size() / 4);
     const uint32_t zero = 0;
     if ((e = upload(s->elems, h.elems.data(), h.elems.size() * 4)) != cudaSuccess ||
         (e = upload(s->isect, h.isect.data(), h.isect.size() * 4)) != cudaSuccess ||
@@ -278,6 +282,57 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
         s->release_all();
         delete s;
         return fail_cuda(e, "uploading the scene");
+    }
+    *out = s;
+    return WOB_OK;
+}
+
+int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                            const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                            void *stream, wob_scene *out) {
+    if (!out) return fail(WOB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    wob_scene_s *s = new wob_scene_s();
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail_cuda(e, "cudaGetDevice");
+    }
+    wobgb::DeviceSceneBuild b;
+    std::string err = wobgb::build_device_scene(dim, n_elems, vertices, normals, boundary_values, robin_alphas,
+                                                boundary_types, (cudaStream_t)stream, b, e);
+    if (!err.empty()) {
+        delete s;
+        return e != cudaSuccess ? fail_cuda(e, "building the scene on the device") : fail(WOB_ERR_INVALID_ARGUMENT, err);
+    }
+    auto take = [](DevBuf &d, void *p, size_t bytes) {
+        d.ptr = p;
+        d.bytes = bytes;
+    };
+    take(s->elems, b.elems, b.elems_bytes);
+    take(s->isect, b.isect, b.isect_bytes);
+    take(s->nodes, b.nodes, b.nodes_bytes);
+    take(s->area_cdf, b.area_cdf, b.area_cdf_bytes);
+    take(s->area_guide, b.area_guide, b.area_guide_bytes);
+    take(s->bv_cdf, b.bv_cdf, b.bv_cdf_bytes);
+    take(s->bv_guide, b.bv_guide, b.bv_guide_bytes);
+    wobgb::HostScene &h = s->host;
+    h.dim = dim;
+    h.n = n_elems;
+    h.order = std::move(b.order);
+    h.n_nodes = b.n_nodes;
+    h.depth = b.depth;
+    h.total_area = b.total_area;
+    h.total_bv = b.total_bv;
+    h.bv_valid = b.bv_valid;
+    s->all_dirichlet = b.all_dirichlet;
+    s->area_G = b.area_G;
+    s->bv_G = b.bv_G;
+    const uint32_t zero = 0;
+    if ((e = upload(s->err, &zero, 4)) != cudaSuccess) {
+        s->release_all();
+        delete s;
+        return fail_cuda(e, "allocating the error word");
     }
     *out = s;
     return WOB_OK;
