@@ -917,6 +917,84 @@ def run_build(args):
     ds.close()
 
 
+VPL_FLOPS_PER_PAIR_2D = 60  # FP32 operations of one (point, VPL) pair: G, dG/dx, three products and sums
+
+
+def run_vpl(args):
+    """VPL potential flow (apps/potential_flow_with_vpl.cu with data/config_potential_flow_with_vpl.json:
+    100,000 paths per iteration, 4 bounces, 1024 RIS candidates, eps 1e-4, 256^2 grid minus the four
+    obstacles): per iteration the VPL walks and the dense aggregation over every (point, VPL) pair,
+    each timed with CUDA events. The aggregation is FP32-issue bound; its roofline is the FP32
+    operation rate 152 SMs x 128 lanes x SM clock (no FMA: the kernels keep every product and sum
+    separately rounded)."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    verts, nrm, data, ty, circles = W.vpl_flow_scene()
+    scene = wob.SceneHost(verts, nrm, data, ty)
+    g, keep = W.vpl_flow_points(256, circles)
+    pts = np.ascontiguousarray(g[keep])
+    n_pts = len(pts)
+    d_pts = torch.from_numpy(pts).to(dev)
+    M = args.vpl_paths
+    base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.InteriorDomain,
+                               estimator=wob.BackwardEstimator, problem=wob.NeumannProblem, path_length=4,
+                               num_resampling_candidates=1024, eps=1e-4, seed=SEED)
+    vp = torch.zeros(M, 2, dtype=torch.float32, device=dev)
+    vm = torch.zeros(M, dtype=torch.float32, device=dev)
+    s = torch.zeros(n_pts, 3, dtype=torch.float64, device=dev)
+    b = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    t_paths, t_agg = [], []
+    sampler = ClockSampler(torch.cuda.current_device())
+    for it in range(args.warmup + args.steps):
+        if it == args.warmup:
+            torch.cuda.synchronize()
+            s.zero_()
+            b.zero_()
+            sampler.__enter__()
+        p = dataclasses.replace(base, path_offset=it * M)
+        ev[0].record(stream)
+        scene.vpl_paths(p, M, vp, vm, b, stream)
+        ev[1].record(stream)
+        scene.vpl_aggregate(base.eps, vp, vm, M, d_pts, n_pts, s, stream)
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            t_paths.append(ev[0].elapsed_time(ev[1]) / 1e3)
+            t_agg.append(ev[1].elapsed_time(ev[2]) / 1e3)
+    sampler.__exit__(None, None, None)
+    clocks = sampler.summary()
+    pairs = float(n_pts) * M
+    agg = sum(t_agg) / len(t_agg)
+    pth = sum(t_paths) / len(t_paths)
+    mhz = clocks.get("sm_mhz") or 2070.0
+    peak = 152 * 128 * mhz * 1e6 / 1e12
+    achieved = pairs * VPL_FLOPS_PER_PAIR_2D / agg / 1e12
+    u = (s[:, 0] / (args.steps * M)).cpu().numpy()
+    gx = (s[:, 1] / (args.steps * M)).cpu().numpy()
+    out = {"metric": "VPL potential flow: (point, VPL) pairs per second of the aggregation",
+           "value": pairs / agg, "unit": "pairs/s", "n_gpus": world, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": "box with 4 circular obstacles, 814 segments, SL backward Neumann, 4 bounces, "
+                                  "1024 RIS candidates; 256^2 grid outside the obstacles",
+                      "points": n_pts, "vpl_per_iteration": M, "iterations": args.steps,
+                      "iteration_ms": {"vpl_walks": pth * 1e3, "aggregation": agg * 1e3},
+                      "walk_bounces_per_s": int(b.item()) / sum(t_paths),
+                      "mean_grad_x_far_field": float(np.mean(gx[np.abs(pts[:, 1]) > 0.45]))},
+           "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s (FP32, no FMA)",
+                        "frac": achieved / peak, "flops_per_pair": VPL_FLOPS_PER_PAIR_2D,
+                        "peak_source": "152 SMs x 128 FP32 lanes x median SM clock during the run"},
+           "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    scene.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -928,7 +1006,7 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d"],
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d", "vpl2d"],
                     default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
@@ -950,6 +1028,7 @@ def main():
     ap.add_argument("--mrhs-npot", type=int, default=4, help="potential samples of the learned CV (mrhs3d)")
     ap.add_argument("--mrhs-plain-only", action="store_true", help="mrhs3d without the learned-CV leg (profiling)")
     ap.add_argument("--build-subdiv", type=int, default=8, help="icosphere subdivision of --workload build3d")
+    ap.add_argument("--vpl-paths", type=int, default=100000, help="VPL walks per iteration of --workload vpl2d")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -963,6 +1042,8 @@ def main():
         run_multi_rhs(args)
     elif args.workload == "build3d":
         run_build(args)
+    elif args.workload == "vpl2d":
+        run_vpl(args)
     else:
         run_ours(args)
 

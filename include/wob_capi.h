@@ -286,6 +286,21 @@ int wob_solve_domain_multi_cv(wob_scene scene, const wob_params *params,
                               void *stream);
 
 /*
+ * Virtual point lights (apps/potential_flow_with_vpl.cu:43-88). wob_vpl_paths runs n_paths
+ * backward single-layer walks (PathComputeFunc), path i from a uniform boundary sample y_i, and
+ * writes y_i to vpl_points [n_paths][dim] and the unknown-boundary estimate mu_i to vpl_values
+ * [n_paths] (device); params.path_offset selects the paths (Philox streams of their own).
+ * wob_vpl_aggregate (AggregateFunc) adds, at every point x of points [n_points][dim],
+ * sum_i mu_i * (G(y_i, x) A, dG/dx(y_i, x) A) into sum [n_points][dim+1] (double, device), A the
+ * scene's total boundary area, eps the kernel's distance clamp; partial sums are FP32 over blocks
+ * of 256 VPLs in order, added in FP64.
+ */
+int wob_vpl_paths(wob_scene scene, const wob_params *params, uint32_t n_paths, float *vpl_points,
+                  float *vpl_values, uint64_t *bounces, void *stream);
+int wob_vpl_aggregate(wob_scene scene, float eps, const float *vpl_points, const float *vpl_values,
+                      uint32_t n_vpl, const float *points, uint32_t n_points, double *sum, void *stream);
+
+/*
  * Learned control variate (no counterpart in the reference). A control-variate density sigma~
  * is given per stored element (host array, storage order; e.g. the MLP below evaluated at the
  * element centroids). wob_solve_domain_cv then runs the forward single-layer Neumann estimator

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -303,6 +304,74 @@ uint64_t oracle_solve_domain_bcv(int dim, uint32_t n_elems, const float *verts, 
     auto h = std::make_unique<Holder<3>>();
     fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
     return solve_domain_bcv<3>(h->scene, params, cv, n_pot, points, n_points, sum, sumsq, per_path);
+}
+
+// VPL walks (apps/potential_flow_with_vpl.cu:77-88): path i from a uniform boundary sample, its
+// unknown-boundary estimate; stream kStreamVpl, point 0, path path_offset + i.
+uint64_t oracle_vpl_paths(int dim, uint32_t n_elems, const float *verts, const float *normals, const float *bvals,
+                          const float *alphas, const int32_t *types, const oracle_params *params, uint32_t n_paths,
+                          float *vpl_p, float *vpl_mu, int n_threads) {
+    set_threads(n_threads);
+    auto run = [&](auto &scene, auto dimtag) -> uint64_t {
+        constexpr int D = decltype(dimtag)::value;
+        const Params prm = to_params(params);
+        uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+        for (int64_t ii = 0; ii < (int64_t)n_paths; ii++) {
+            Rng rng(params->seed, kStreamVpl, 0u, params->path_offset + (uint64_t)ii);
+            Estimator<D> est(&scene, prm, &rng);
+            float ip;
+            const BoundaryPoint<D> y = scene.sample_uniform(rng, ip);
+            const float mu = est.unknown_boundary(y);
+            for (int k = 0; k < D; k++) vpl_p[(size_t)ii * D + k] = y.p.v[k];
+            vpl_mu[ii] = mu;
+            total += est.bounces;
+        }
+        return total;
+    };
+    if (dim == 2) {
+        auto h = std::make_unique<Holder<2>>();
+        fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        return run(h->scene, std::integral_constant<int, 2>());
+    }
+    auto h = std::make_unique<Holder<3>>();
+    fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+    return run(h->scene, std::integral_constant<int, 3>());
+}
+
+// VPL aggregation (apps/potential_flow_with_vpl.cu:43-75): sum[pt] += sum_i mu_i (G A, dG/dx A),
+// FP32 partial sums over blocks of 256 VPLs in order, added in FP64 (the engine's blocking).
+void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, const float *vpl_mu, uint32_t n_vpl,
+                          const float *points, uint32_t n_points, double *sum, int n_threads) {
+    set_threads(n_threads);
+    auto run = [&](auto dimtag) {
+        constexpr int D = decltype(dimtag)::value;
+        EqKernel<D> K;
+        K.eps = eps;
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+            Vec<D> x;
+            for (int k = 0; k < D; k++) x.v[k] = points[(size_t)ii * D + k];
+            double acc[D + 1] = {};
+            for (uint32_t t0 = 0; t0 < n_vpl; t0 += 256) {
+                const uint32_t m = std::min<uint32_t>(256u, n_vpl - t0);
+                float part[D + 1] = {};
+                for (uint32_t j = 0; j < m; j++) {
+                    Vec<D> y;
+                    for (int k = 0; k < D; k++) y.v[k] = vpl_p[(size_t)(t0 + j) * D + k];
+                    const float mu = vpl_mu[t0 + j];
+                    const float u = K.G(y, x) * area;
+                    const Vec<D> g = K.dG_dx(y, x);
+                    part[0] = part[0] + mu * u;
+                    for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (g.v[k] * area);
+                }
+                for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
+            }
+            for (int c = 0; c <= D; c++) sum[(size_t)ii * (D + 1) + c] += acc[c];
+        }
+    };
+    if (dim == 2) run(std::integral_constant<int, 2>());
+    else run(std::integral_constant<int, 3>());
 }
 
 // compute_sample_unknown_boundary at boundary points (the boundary density / unknown).

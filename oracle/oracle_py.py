@@ -55,6 +55,11 @@ def lib() -> C.CDLL:
         L.oracle_solve_domain_bcv.restype = u64
         L.oracle_solve_domain_bcv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
                                               vp, u32, vp, vp, vp, C.c_int]
+        L.oracle_vpl_paths.restype = u64
+        L.oracle_vpl_paths.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), u32, vp, vp,
+                                       C.c_int]
+        L.oracle_vpl_aggregate.restype = None
+        L.oracle_vpl_aggregate.argtypes = [C.c_int, f32, f32, vp, vp, u32, vp, u32, vp, C.c_int]
         L.oracle_solve_unknown.restype = u64
         L.oracle_solve_unknown.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, vp, vp,
                                            vp, vp, vp, u32, vp, vp, C.c_int]
@@ -181,6 +186,26 @@ def solve_domain_bcv(el: Elements, params, cv, n_pot: int, points, per_path: boo
                                       _ptr(el.types), C.byref(ps), _ptr(c), n_pot, _ptr(pts), n, _ptr(s), _ptr(q),
                                       _ptr(pp), n_threads)
     return s, q, int(b), pp
+
+
+def vpl_paths(el: Elements, params, n_paths: int, n_threads: int = 0):
+    """VPL walks: (points [n, dim], values [n], bounces)."""
+    p = np.zeros((n_paths, el.dim), dtype=np.float32)
+    mu = np.zeros(n_paths, dtype=np.float32)
+    ps = params_struct(params)
+    b = lib().oracle_vpl_paths(el.dim, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
+                               _ptr(el.types), C.byref(ps), n_paths, _ptr(p), _ptr(mu), n_threads)
+    return p, mu, int(b)
+
+
+def vpl_aggregate(dim: int, area: float, eps: float, vpl_p, vpl_mu, points, n_threads: int = 0):
+    vp_ = _f32(vpl_p).reshape(-1, dim)
+    mu = _f32(vpl_mu).reshape(-1)
+    pts = _f32(points).reshape(-1, dim)
+    out = np.zeros((len(pts), dim + 1))
+    lib().oracle_vpl_aggregate(dim, float(area), float(eps), _ptr(vp_), _ptr(mu), len(mu), _ptr(pts), len(pts),
+                               _ptr(out), n_threads)
+    return out
 
 
 def solve_unknown(el: Elements, params, p, n, angle, bv, btype, alpha=None, per_path: bool = False, n_threads: int = 0):

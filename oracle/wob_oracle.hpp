@@ -1115,6 +1115,7 @@ template <int D> struct Estimator {
 // Random stream tags: the domain and boundary estimators use separate Philox keys.
 constexpr uint32_t kStreamDomain = 0u;
 constexpr uint32_t kStreamBoundary = 1u;
+constexpr uint32_t kStreamVpl = 2u;
 
 // The closed-form double-layer interior Dirichlet walk of apps/simple_wob_and_wos.cu:81-108: a
 // second, independent oracle for the double-layer estimator. Uses the same line samples; weight

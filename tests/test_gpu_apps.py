@@ -97,3 +97,36 @@ def test_general_3d_matches_api(engine, cuda, tmp_path):
     assert np.allclose(u[inside], s[:, 0] / 512, rtol=1e-3, atol=1e-4)
     assert np.allclose(g[inside], s[:, 1:] / 512, rtol=1e-3, atol=1e-3)
     scene.close()
+
+
+def test_potential_flow_vpl_matches_api(engine, cuda, tmp_path):
+    """apps/potential_flow_with_vpl.cu: the app's fields equal the engine API's VPL walks and
+    aggregation on the same scene and points."""
+    import json
+    torch = cuda
+    out = str(tmp_path / "out")
+    cfg = str(tmp_path / "cfg.json")
+    with open(cfg, "w") as f:
+        json.dump({"output_dir": out, "path_length": 4, "num_sample_paths": 2000, "num_resampling_candidates": 64,
+                   "grid_res": 40, "eps": 1e-4, "max_time": 1, "max_iterations": 2}, f)
+    r = A.run_app("potential_flow_vpl", cfg)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n, u = A.read_field(os.path.join(out, "potential2.scalar"))
+    _, g = A.read_field(os.path.join(out, "gradient2.vector2"), 2)
+    verts, nrm, data, ty, circles = W.vpl_flow_scene()
+    grid, keep = W.vpl_flow_points(40, circles)
+    assert n == 40 and np.array_equal(~np.isnan(u), keep)
+    scene = engine.SceneHost(verts, nrm, data, ty)
+    pts = torch.from_numpy(np.ascontiguousarray(grid[keep])).cuda()
+    s = torch.zeros(len(pts), 3, dtype=torch.float64, device="cuda")
+    vp = torch.zeros(2000, 2, dtype=torch.float32, device="cuda")
+    vm = torch.zeros(2000, dtype=torch.float32, device="cuda")
+    for it in range(2):
+        p = engine.EstimatorParams(bie_model=0, domain=0, estimator=0, problem=1, path_length=4,
+                                   num_resampling_candidates=64, eps=1e-4, seed=0, path_offset=it * 2000)
+        scene.vpl_paths(p, 2000, vp, vm)
+        scene.vpl_aggregate(1e-4, vp, vm, 2000, pts, len(pts), s)
+    torch.cuda.synchronize()
+    ref = (s / 4000).cpu().numpy().astype(np.float32)
+    assert np.array_equal(u[keep], ref[:, 0]) and np.array_equal(g[keep], ref[:, 1:])
+    scene.close()

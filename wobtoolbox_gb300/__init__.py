@@ -323,6 +323,18 @@ class SceneHost:
                                                _ptr(sum_), _ptr(sumsq), _ptr(bounces), _ptr(per_path),
                                                _stream_ptr(stream)))
 
+    # ---- virtual point lights (apps/potential_flow_with_vpl.cu)
+    def vpl_paths(self, params: EstimatorParams, n_paths: int, vpl_points, vpl_values, bounces=None,
+                  stream=None) -> None:
+        p = params.to_c()
+        check(load().wob_vpl_paths(self._h, C.byref(p), int(n_paths), _ptr(vpl_points), _ptr(vpl_values),
+                                   _ptr(bounces), _stream_ptr(stream)))
+
+    def vpl_aggregate(self, eps: float, vpl_points, vpl_values, n_vpl: int, points, n_points: int, sum_,
+                      stream=None) -> None:
+        check(load().wob_vpl_aggregate(self._h, float(eps), _ptr(vpl_points), _ptr(vpl_values), int(n_vpl),
+                                       _ptr(points), int(n_points), _ptr(sum_), _stream_ptr(stream)))
+
     # ---- host-buffer solve (synchronous), the end-to-end entry point
     def solve_domain_host(self, params: EstimatorParams, points: np.ndarray, sum_=None, sumsq=None):
         pts = _f32(points).reshape(-1, self.dim)

@@ -23,7 +23,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["capi.cu", "kernels_dispatch.cu", "k2_generic_domain.cu", "k2_generic_boundary.cu", "k3_generic_domain.cu",
               "k3_generic_boundary.cu", "k2_fast.cu", "k3_fast.cu", "k_batch.cu", "k_cv.cu",
-              "k2_multi_rhs.cu", "k3_multi_rhs.cu", "mlp.cu", "scene_build_gpu.cu"]
+              "k2_multi_rhs.cu", "k3_multi_rhs.cu", "mlp.cu", "scene_build_gpu.cu",
+              "k_vpl.cu"]
 CPP_SOURCES = ["scene_build.cpp"]
 
 
@@ -35,7 +36,7 @@ def nvcc_path() -> str:
 
 
 APPS = os.path.join(HERE, "apps")
-APP_BINARIES = {"general_2d": 2, "general_3d": 3}
+APP_BINARIES = {"general_2d": 2, "general_3d": 3, "potential_flow_vpl": 2}
 
 
 def app_path(name: str) -> str:
@@ -55,13 +56,17 @@ def build_apps(force: bool = False) -> list[str]:
     deps = [os.path.join(APPS, f) for f in os.listdir(APPS)] + [os.path.join(INCLUDE, "wob_gb300.hpp"),
                                                                  os.path.join(INCLUDE, "wob_capi.h"), LIB]
     jobs, outs = [], []
+    cuda = os.path.dirname(os.path.dirname(nvcc_path()))
     for name, dim in APP_BINARIES.items():
         out = app_path(name)
         outs.append(out)
+        src = "potential_flow_vpl.cpp" if name == "potential_flow_vpl" else "general.cpp"
+        extra = ["-I", os.path.join(cuda, "include"), "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                 "-Wl,-rpath," + os.path.join(cuda, "lib64")] if name == "potential_flow_vpl" else []
         if force or _stale(out, deps):
             jobs.append([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall", f"-DWOB_APP_DIM={dim}",
-                         "-I", INCLUDE, os.path.join(APPS, "general.cpp"), "-o", out + ".tmp", "-L", OUT,
-                         "-lwob_gb300", "-Wl,-rpath,$ORIGIN"])
+                         "-I", INCLUDE, os.path.join(APPS, src), "-o", out + ".tmp", "-L", OUT,
+                         "-lwob_gb300", "-Wl,-rpath,$ORIGIN"] + extra)
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for j, proc in zip(jobs, ex.map(lambda j: subprocess.run(j, capture_output=True, text=True), jobs)):
             if proc.returncode != 0:

@@ -9,6 +9,7 @@
 #include "launch.hpp"
 #include "multi_rhs.hpp"
 #include "scene_build_gpu.hpp"
+#include "vpl.hpp"
 #include "scene_host.hpp"
 #include "walk_generic.cuh"
 
@@ -951,6 +952,36 @@ int wob_solve_unknown_boundary_multi(wob_scene s, const wob_params *params, cons
     a.stream = (cudaStream_t)stream;
     cudaError_t e = s->host.dim == 2 ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, a) : wobgb::launch_multi_rhs_3d(s->view<3>(), w, a);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS unknown-boundary walk");
+}
+
+int wob_vpl_paths(wob_scene s, const wob_params *params, uint32_t n_paths, float *vpl_points, float *vpl_values,
+                  uint64_t *bounces, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    wobgb::WalkParams w;
+    int st = check_params(s, params, w);
+    if (st != WOB_OK) return st;
+    if (w.bie != WOB_INDIRECT_SINGLE_LAYER || w.estimator != WOB_BACKWARD_ESTIMATOR || w.n_volume != 0)
+        return fail(WOB_ERR_UNSUPPORTED, "VPL walks use the backward single-layer estimator without a source term");
+    if (n_paths == 0) return WOB_OK;
+    if (!vpl_points || !vpl_values) return fail(WOB_ERR_INVALID_ARGUMENT, "vpl_points and vpl_values are required");
+    DeviceGuard g(s->device);
+    cudaError_t e = s->host.dim == 2
+        ? wobgb::launch_vpl_paths_2d(s->view<2>(), w, n_paths, vpl_points, vpl_values, (unsigned long long *)bounces, (cudaStream_t)stream)
+        : wobgb::launch_vpl_paths_3d(s->view<3>(), w, n_paths, vpl_points, vpl_values, (unsigned long long *)bounces, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the VPL walks");
+}
+
+int wob_vpl_aggregate(wob_scene s, float eps, const float *vpl_points, const float *vpl_values, uint32_t n_vpl,
+                      const float *points, uint32_t n_points, double *sum, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (!(eps > 0.0f)) return fail(WOB_ERR_INVALID_ARGUMENT, "eps must be positive");
+    if (n_points == 0) return WOB_OK;
+    if (!points || !sum || (n_vpl && (!vpl_points || !vpl_values)))
+        return fail(WOB_ERR_INVALID_ARGUMENT, "points, sum, vpl_points and vpl_values are required");
+    DeviceGuard g(s->device);
+    cudaError_t e = wobgb::launch_vpl_aggregate(s->host.dim, vpl_points, vpl_values, n_vpl, s->host.total_area, eps,
+                                                points, n_points, sum, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the VPL aggregation");
 }
 
 int wob_solve_unknown_boundary(wob_scene s, const wob_params *params, const float *p, const float *n,

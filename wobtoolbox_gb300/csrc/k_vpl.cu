@@ -1,0 +1,119 @@
+// Virtual-point-light (VPL) variant of the walk (apps/potential_flow_with_vpl.cu:43-88):
+//
+// 1. paths (PathComputeFunc, :77-88): path i starts at a uniform boundary sample y_i and its walk
+//    returns the unknown boundary estimate mu_i (compute_sample_unknown_boundary) -- one thread per
+//    path, Philox stream kStreamVpl, point 0, path index path_offset + i;
+// 2. aggregation (AggregateFunc, :43-75): every evaluation point x sums, over all VPLs,
+//    mu_i * G(y_i, x) * A and mu_i * dG/dx(y_i, x) * A (the single layer's solution_domain_unknown /
+//    gradient_domain_unknown, A = total boundary area) -- an N_points x N_vpl dense sum of kernel
+//    evaluations, FP32-issue bound: each thread owns one point, the block stages tiles of 256 VPLs
+//    (position, mu) in shared memory and every thread runs over the tile. Partial sums are FP32 per
+//    tile of 256 VPLs, added into FP64 per point, in VPL order (the oracle does the same blocking,
+//    so the sums are bit-identical).
+#include "kernels.cuh"
+#include "vpl.hpp"
+
+namespace wobgb {
+
+namespace {
+
+constexpr uint32_t kStreamVpl = 2u;
+constexpr int kVplTile = 256;
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) vpl_paths_kernel(SceneView<D> s, WalkParams p, uint32_t n_paths,
+                                                           float *__restrict__ vpl_p, float *__restrict__ vpl_mu,
+                                                           unsigned long long *__restrict__ bounces) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long b = 0;
+    if (i < n_paths) {
+        Walker<D, kSingleLayer, kStratSingleLayer, false> w(s, p, kStreamVpl, 0u, p.path_offset + i);
+        float ip;
+        const BPoint<D> y = sample_uniform<D>(s, w.rng, ip);
+        const float mu = w.unknown_boundary(y);
+        for (int k = 0; k < D; k++) vpl_p[(size_t)i * D + k] = y.p.v[k];
+        vpl_mu[i] = mu;
+        b = w.bounces;
+    }
+    if (bounces) {
+        const unsigned long long t = warp_sum_u64(b);
+        if ((threadIdx.x & 31u) == 0 && t) atomicAdd(bounces, t);
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kVplTile) vpl_aggregate_kernel(const float *__restrict__ vpl_p,
+                                                                 const float *__restrict__ vpl_mu, uint32_t n_vpl,
+                                                                 float area, float eps, const float *__restrict__ pts,
+                                                                 uint32_t n_points, double *__restrict__ sum) {
+    __shared__ float sp[kVplTile][D];
+    __shared__ float smu[kVplTile];
+    const uint32_t pt = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = pt < n_points;
+    V<D> x = vzero<D>();
+    if (active)
+        for (int k = 0; k < D; k++) x.v[k] = __ldg(pts + (size_t)pt * D + k);
+    Green<D> K;
+    K.eps = eps;
+    double acc[D + 1];
+    for (int c = 0; c <= D; c++) acc[c] = 0.0;
+    for (uint32_t t0 = 0; t0 < n_vpl; t0 += kVplTile) {
+        const uint32_t m = min((uint32_t)kVplTile, n_vpl - t0);
+        __syncthreads();
+        if (threadIdx.x < m) {
+            for (int k = 0; k < D; k++) sp[threadIdx.x][k] = __ldg(vpl_p + (size_t)(t0 + threadIdx.x) * D + k);
+            smu[threadIdx.x] = __ldg(vpl_mu + t0 + threadIdx.x);
+        }
+        __syncthreads();
+        if (!active) continue;
+        float part[D + 1];
+        for (int c = 0; c <= D; c++) part[c] = 0.0f;
+        for (uint32_t j = 0; j < m; j++) {
+            V<D> y;
+            for (int k = 0; k < D; k++) y.v[k] = sp[j][k];
+            const float mu = smu[j];
+            const float u = K.G(y, x) * area;
+            const V<D> g = K.dG_dx(y, x);
+            part[0] = part[0] + mu * u;
+            for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (g.v[k] * area);
+        }
+        for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
+    }
+    if (active)
+        for (int c = 0; c <= D; c++) sum[(size_t)pt * (D + 1) + c] += acc[c];
+}
+
+template <int D>
+cudaError_t paths_impl(const SceneView<D> &s, const WalkParams &p, uint32_t n_paths, float *vpl_p, float *vpl_mu,
+                       unsigned long long *bounces, cudaStream_t st) {
+    if (n_paths == 0) return cudaSuccess;
+    vpl_paths_kernel<D><<<(n_paths + kBlock - 1) / kBlock, kBlock, 0, st>>>(s, p, n_paths, vpl_p, vpl_mu, bounces);
+    return cudaGetLastError();
+}
+
+template <int D>
+cudaError_t aggregate_impl(const float *vpl_p, const float *vpl_mu, uint32_t n_vpl, float area, float eps,
+                           const float *pts, uint32_t n_points, double *sum, cudaStream_t st) {
+    if (n_points == 0) return cudaSuccess;
+    vpl_aggregate_kernel<D><<<(n_points + kVplTile - 1) / kVplTile, kVplTile, 0, st>>>(vpl_p, vpl_mu, n_vpl, area, eps,
+                                                                                      pts, n_points, sum);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_vpl_paths_2d(const SceneView<2> &s, const WalkParams &p, uint32_t n_paths, float *vpl_p,
+                                float *vpl_mu, unsigned long long *bounces, cudaStream_t st) {
+    return paths_impl<2>(s, p, n_paths, vpl_p, vpl_mu, bounces, st);
+}
+cudaError_t launch_vpl_paths_3d(const SceneView<3> &s, const WalkParams &p, uint32_t n_paths, float *vpl_p,
+                                float *vpl_mu, unsigned long long *bounces, cudaStream_t st) {
+    return paths_impl<3>(s, p, n_paths, vpl_p, vpl_mu, bounces, st);
+}
+cudaError_t launch_vpl_aggregate(int dim, const float *vpl_p, const float *vpl_mu, uint32_t n_vpl, float area,
+                                 float eps, const float *pts, uint32_t n_points, double *sum, cudaStream_t st) {
+    return dim == 2 ? aggregate_impl<2>(vpl_p, vpl_mu, n_vpl, area, eps, pts, n_points, sum, st)
+                    : aggregate_impl<3>(vpl_p, vpl_mu, n_vpl, area, eps, pts, n_points, sum, st);
+}
+
+}  // namespace wobgb

@@ -293,3 +293,44 @@ def batch_scenes(n_scenes=256, seed=0, paths=1024, path_length=8, point_range=(1
                         alphas=np.full((n_seg, 2), 1.0, F32) if robin else None, volume=volume, points=pts,
                         params=params, lobes=lobes, amp=amp))
     return out
+
+
+# ------------------------------------------------------------------ VPL potential-flow scene
+def vpl_flow_scene():
+    """The scene of apps/potential_flow_with_vpl.cu:140-176: the box [-1/2, 1/2]^2 with Neumann data
+    -1 / 0 / 1 / 0 on its left / top / right / bottom sides (a unit flow in +x) around four circular
+    obstacles (zero flux) of 360, 180, 180 and 90 segments, normals n = (t_y, -t_x) with
+    t = (v1 - v2)/|v1 - v2| (float32 like the reference). Returns verts [n, 2, 2], normals [n, 2],
+    data [n, 2], types [n] (all Neumann) and the circles (center, radius, segments)."""
+    verts = [[[-0.5, -0.5], [-0.5, 0.5]], [[-0.5, 0.5], [0.5, 0.5]], [[0.5, 0.5], [0.5, -0.5]],
+             [[0.5, -0.5], [-0.5, -0.5]]]
+    normals = [[-1.0, 0.0], [0.0, 1.0], [1.0, 0.0], [0.0, -1.0]]
+    data = [[-1.0, -1.0], [0.0, 0.0], [1.0, 1.0], [0.0, 0.0]]
+    circles = [((0.2, 0.1), 0.25, 360), ((-0.25, 0.3), 0.15, 180), ((-0.20, -0.25), 0.2, 180), ((0.25, -0.3), 0.05, 90)]
+    verts = np.array(verts, F32)
+    normals = np.array(normals, F32)
+    data = np.array(data, F32)
+    vs, ns = [verts], [normals]
+    for (cx, cy), r, m in circles:
+        c = np.array([cx, cy], F32)
+        k = np.arange(m + 1, dtype=np.float64)
+        ang = (2 * np.pi) * k / m
+        u = np.stack([np.cos(ang), np.sin(ang)], 1).astype(F32)
+        p = (c[None, :] + F32(r) * u).astype(F32)
+        v = np.stack([p[:-1], p[1:]], 1)
+        vs.append(v)
+        ns.append(segment_normals(v))
+    verts = np.concatenate(vs).astype(F32)
+    normals = np.concatenate(ns).astype(F32)
+    data = np.concatenate([data, np.zeros((len(verts) - 4, 2), F32)])
+    return verts, normals, data, np.ones(len(verts), np.int32), circles
+
+
+def vpl_flow_points(grid_res: int, circles):
+    """Cell centres of the grid over [-1/2, 1/2]^2 outside the circles (apps/potential_flow_with_vpl.cu:178-185)."""
+    g = idx_to_domain_point(grid_res, 1.0, 2)
+    keep = np.ones(len(g), bool)
+    for (cx, cy), r, _ in circles:
+        d = g - np.array([cx, cy], F32)
+        keep &= ~((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) < F32(r) * F32(r))
+    return g, keep
