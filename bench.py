@@ -995,6 +995,76 @@ def run_vpl(args):
     scene.close()
 
 
+def run_wos(args):
+    """WoB vs walk on spheres (apps/simple_wob_and_wos.cu) on the 2D star workload (1024 segments,
+    g = e^x cos y, 7,960 interior points): the double-layer WoB of the headline 2D workload (8
+    bounces) and WoS with eps 1e-4, each run as progressive iterations for --wos-budget GPU seconds;
+    RMSE against the exact solution is recorded against cumulative GPU time."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sc = W.config0_scene()
+    scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    pts = sc["points"]
+    n_pts = len(pts)
+    exact = W.exp_cos(pts)[:, 0]
+    d_pts = torch.from_numpy(pts).to(dev)
+    stream = torch.cuda.current_stream()
+    wob_p = wob.EstimatorParams(bie_model=wob.IndirectDoubleLayer, path_length=8, num_sample_paths=256, seed=SEED)
+    wos_p = wob.EstimatorParams(num_sample_paths=256, eps=1e-4, seed=SEED)
+
+    def progressive(solve, params, width):
+        s = torch.zeros(n_pts, width, dtype=torch.float64, device=dev)
+        q = torch.zeros(1, dtype=torch.int64, device=dev)
+        for _ in range(args.warmup):
+            solve(dataclasses.replace(params, path_offset=1 << 40), s, q)
+        torch.cuda.synchronize()
+        s.zero_()
+        q.zero_()
+        curve, total, k = [], 0.0, 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        while total < args.wos_budget and k < 100000:
+            e0.record(stream)
+            solve(dataclasses.replace(params, path_offset=k * params.num_sample_paths), s, q)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1) / 1e3
+            k += 1
+            u = (s[:, 0] / (k * params.num_sample_paths)).cpu().numpy()
+            curve.append((total, float(np.sqrt(np.mean((u - exact) ** 2))), k * params.num_sample_paths))
+        return curve, int(q.item())
+
+    wob_curve, wob_b = progressive(lambda p, s, q: scene.solve_domain(p, d_pts, n_pts, s, None, q, stream), wob_p, 3)
+    wos_curve, wos_q = progressive(lambda p, s, q: scene.solve_wos(p, d_pts, n_pts, s, None, q, None, stream), wos_p, 1)
+    target = max(wob_curve[-1][1], wos_curve[-1][1]) * 1.0001
+
+    def time_to(curve):
+        for t_s, r, _ in curve:
+            if r <= target:
+                return t_s
+        return None
+
+    tw, ts = time_to(wob_curve), time_to(wos_curve)
+    out = {"metric": "WoB vs walk on spheres, time to a common RMSE (2D star, 1024 segments)",
+           "value": (ts / tw) if (tw and ts) else None, "unit": "x (WoS time / WoB time to the common RMSE)",
+           "n_gpus": world, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "2D interior Dirichlet star r = 1 + 0.3 cos 5t, g = e^x cos y, 7960 points",
+                      "rmse_target": target, "wob_time_s": tw, "wos_time_s": ts,
+                      "wob": {"paths_per_s": wob_curve[-1][2] * n_pts / wob_curve[-1][0],
+                              "bounces_per_s": wob_b / wob_curve[-1][0], "final": wob_curve[-1]},
+                      "wos": {"paths_per_s": wos_curve[-1][2] * n_pts / wos_curve[-1][0],
+                              "closest_point_queries_per_s": wos_q / wos_curve[-1][0],
+                              "queries_per_path": wos_q / (wos_curve[-1][2] * n_pts), "final": wos_curve[-1]},
+                      "wob_curve": wob_curve[::max(1, len(wob_curve) // 8)],
+                      "wos_curve": wos_curve[::max(1, len(wos_curve) // 8)]}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    scene.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1006,7 +1076,8 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d", "vpl2d"],
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d", "vpl2d",
+                                           "wos2d"],
                     default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
@@ -1029,6 +1100,7 @@ def main():
     ap.add_argument("--mrhs-plain-only", action="store_true", help="mrhs3d without the learned-CV leg (profiling)")
     ap.add_argument("--build-subdiv", type=int, default=8, help="icosphere subdivision of --workload build3d")
     ap.add_argument("--vpl-paths", type=int, default=100000, help="VPL walks per iteration of --workload vpl2d")
+    ap.add_argument("--wos-budget", type=float, default=5.0, help="GPU seconds per method of --workload wos2d")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -1044,6 +1116,8 @@ def main():
         run_build(args)
     elif args.workload == "vpl2d":
         run_vpl(args)
+    elif args.workload == "wos2d":
+        run_wos(args)
     else:
         run_ours(args)
 

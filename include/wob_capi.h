@@ -120,8 +120,9 @@ int wob_scene_get_info(wob_scene scene, wob_scene_info *info);
 int wob_scene_get_element_order(wob_scene scene, uint32_t *order);
 /*
  * Reads and clears the scene's device error word (synchronous): bit 0 = a BVH traversal stack
- * overflowed, bit 1 = a traversal hit its step bound. Kernels that set a bit stop that query and
- * carry on; the reference has no equivalent (its lbvh query has no bound).
+ * overflowed, bit 1 = a traversal hit its step bound, bit 2 = a walk-on-spheres path was stopped
+ * after 4096 jumps. Kernels that set a bit stop that query (or walk) and carry on; the reference
+ * has no equivalent (its lbvh query and its WoS loop have no bound).
  */
 int wob_scene_poll_error(wob_scene scene, uint32_t *bits);
 
@@ -284,6 +285,22 @@ int wob_solve_domain_multi_cv(wob_scene scene, const wob_params *params,
                               uint32_t n_potential_samples, const float *points, uint32_t n_points,
                               double *sum, double *sumsq, uint64_t *bounces, float *per_path,
                               void *stream);
+
+/*
+ * Walk on spheres, the reference's baseline method (apps/simple_wob_and_wos.cu:49-78, 111-137), for
+ * 2D scenes with Dirichlet data: each path jumps to a uniform point on the largest empty circle
+ * until the distance to the boundary is below params.eps and returns the boundary value at the
+ * closest boundary point (BVH closest-point query; ties go to the smallest storage index). Uses
+ * num_sample_paths, eps, seed, path_offset and point_offset of params. points [n][2] (device); sum /
+ * sumsq [n] double (accumulated), queries = closest-point queries made, per_path [n][paths] float
+ * (may be NULL). A path is stopped after 4096 jumps (error-word bit 2).
+ * wob_closest_point: the query alone, for points [n][2]: stored element index, squared distance and
+ * the boundary value at the closest point (device arrays).
+ */
+int wob_solve_wos(wob_scene scene, const wob_params *params, const float *points, uint32_t n_points,
+                  double *sum, double *sumsq, uint64_t *queries, float *per_path, void *stream);
+int wob_closest_point(wob_scene scene, const float *points, uint32_t n_points, uint32_t *elems,
+                      float *dist2, float *values, void *stream);
 
 /*
  * Virtual point lights (apps/potential_flow_with_vpl.cu:43-88). wob_vpl_paths runs n_paths

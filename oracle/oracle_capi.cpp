@@ -306,6 +306,51 @@ uint64_t oracle_solve_domain_bcv(int dim, uint32_t n_elems, const float *verts, 
     return solve_domain_bcv<3>(h->scene, params, cv, n_pot, points, n_points, sum, sumsq, per_path);
 }
 
+// Walk on spheres (2D): per-point sums and per-path values; stream kStreamWos.
+uint64_t oracle_wos(uint32_t n_elems, const float *verts, const float *normals, const float *bvals,
+                    const int32_t *types, const oracle_params *params, const float *points, uint32_t n_points,
+                    double *sum, float *per_path, int n_threads) {
+    set_threads(n_threads);
+    auto h = std::make_unique<Holder<2>>();
+    fill_elements<2>(h->scene, n_elems, verts, normals, bvals, nullptr, types);
+    const Scene<2> &scene = h->scene;
+    const uint32_t P = params->num_sample_paths;
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+        Vec<2> x;
+        x.v[0] = points[2 * ii];
+        x.v[1] = points[2 * ii + 1];
+        double acc = 0.0;
+        for (uint32_t j = 0; j < P; j++) {
+            Rng rng(params->seed, kStreamWos, params->point_offset + (uint32_t)ii, params->path_offset + j);
+            unsigned q = 0;
+            const float v = wos_path(scene, params->eps, rng, x, q);
+            total += q;
+            acc += (double)v;
+            if (per_path) per_path[(size_t)ii * P + j] = v;
+        }
+        if (sum) sum[ii] += acc;
+    }
+    return total;
+}
+
+void oracle_closest_point(uint32_t n_elems, const float *verts, const float *normals, const float *bvals,
+                          const int32_t *types, const float *points, uint32_t n, uint32_t *elem, float *dist2,
+                          float *value) {
+    Scene<2> s;
+    fill_elements<2>(s, n_elems, verts, normals, bvals, nullptr, types);
+    for (uint32_t i = 0; i < n; i++) {
+        Vec<2> x;
+        x.v[0] = points[2 * i];
+        x.v[1] = points[2 * i + 1];
+        const ClosestPoint c = closest_point(s, x);
+        elem[i] = c.elem;
+        dist2[i] = c.d2;
+        value[i] = c.elem == 0xFFFFFFFFu ? 0.0f : closest_value(s, c);
+    }
+}
+
 // VPL walks (apps/potential_flow_with_vpl.cu:77-88): path i from a uniform boundary sample, its
 // unknown-boundary estimate; stream kStreamVpl, point 0, path path_offset + i.
 uint64_t oracle_vpl_paths(int dim, uint32_t n_elems, const float *verts, const float *normals, const float *bvals,

@@ -55,6 +55,10 @@ def lib() -> C.CDLL:
         L.oracle_solve_domain_bcv.restype = u64
         L.oracle_solve_domain_bcv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
                                               vp, u32, vp, vp, vp, C.c_int]
+        L.oracle_wos.restype = u64
+        L.oracle_wos.argtypes = [u32, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32, vp, vp, C.c_int]
+        L.oracle_closest_point.restype = None
+        L.oracle_closest_point.argtypes = [u32, vp, vp, vp, vp, vp, u32, vp, vp, vp]
         L.oracle_vpl_paths.restype = u64
         L.oracle_vpl_paths.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), u32, vp, vp,
                                        C.c_int]
@@ -186,6 +190,28 @@ def solve_domain_bcv(el: Elements, params, cv, n_pot: int, points, per_path: boo
                                       _ptr(el.types), C.byref(ps), _ptr(c), n_pot, _ptr(pts), n, _ptr(s), _ptr(q),
                                       _ptr(pp), n_threads)
     return s, q, int(b), pp
+
+
+def wos(el: Elements, params, points, per_path: bool = False, n_threads: int = 0):
+    """Walk on spheres (2D Dirichlet): (sum [n], per_path [n, paths] or None, closest-point queries)."""
+    pts = _f32(points).reshape(-1, 2)
+    s = np.zeros(len(pts))
+    pp = np.zeros((len(pts), params.num_sample_paths), dtype=np.float32) if per_path else None
+    ps = params_struct(params)
+    q = lib().oracle_wos(el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.types), C.byref(ps),
+                         _ptr(pts), len(pts), _ptr(s), _ptr(pp), n_threads)
+    return s, pp, int(q)
+
+
+def closest_point(el: Elements, points):
+    pts = _f32(points).reshape(-1, 2)
+    n = len(pts)
+    e = np.zeros(n, dtype=np.uint32)
+    d = np.zeros(n, dtype=np.float32)
+    v = np.zeros(n, dtype=np.float32)
+    lib().oracle_closest_point(el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.types), _ptr(pts), n,
+                               _ptr(e), _ptr(d), _ptr(v))
+    return e, d, v
 
 
 def vpl_paths(el: Elements, params, n_paths: int, n_threads: int = 0):

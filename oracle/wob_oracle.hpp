@@ -1116,6 +1116,7 @@ template <int D> struct Estimator {
 constexpr uint32_t kStreamDomain = 0u;
 constexpr uint32_t kStreamBoundary = 1u;
 constexpr uint32_t kStreamVpl = 2u;
+constexpr uint32_t kStreamWos = 3u;
 
 // The closed-form double-layer interior Dirichlet walk of apps/simple_wob_and_wos.cu:81-108: a
 // second, independent oracle for the double-layer estimator. Uses the same line samples; weight
@@ -1134,6 +1135,51 @@ inline float simple_wob_path(const Scene<2> &s, Rng &rng, const Vec<2> &x, unsig
         contrib = contrib + weight * y.boundary_value;
     }
     return contrib;
+}
+
+// Closest boundary point of a 2D scene (apps/simple_wob_and_wos.cu:49-78 with lbvh's nearest
+// query restated as a scan): squared distance to each segment with the clamped parameter
+// t = (p - a).l / |l|^2, the smallest distance winning, ties to the smallest storage index.
+struct ClosestPoint {
+    float d2 = INFINITY;
+    unsigned elem = 0xFFFFFFFFu;
+    float t = 0.0f;
+};
+inline ClosestPoint closest_point(const Scene<2> &s, const Vec<2> &p) {
+    ClosestPoint best;
+    for (unsigned i = 0; i < (unsigned)s.elems.size(); i++) {
+        const Element<2> &e = s.elems[i];
+        const float ax = e.v[0].v[0], ay = e.v[0].v[1];
+        const float lx = e.v[1].v[0] - ax, ly = e.v[1].v[1] - ay;
+        float t = ((p.v[0] - ax) * lx + (p.v[1] - ay) * ly) / (lx * lx + ly * ly);
+        t = std::min(std::max(t, 0.0f), 1.0f);
+        const float cx = (ax + lx * t) - p.v[0], cy = (ay + ly * t) - p.v[1];
+        const float d2 = cx * cx + cy * cy;
+        if (d2 < best.d2 || (d2 == best.d2 && i < best.elem)) best = ClosestPoint{d2, i, t};
+    }
+    return best;
+}
+inline float closest_value(const Scene<2> &s, const ClosestPoint &c) {
+    const Element<2> &e = s.elems[c.elem];
+    return (e.bv[1] - e.bv[0]) * c.t + e.bv[0];
+}
+
+// One walk-on-spheres path (apps/simple_wob_and_wos.cu:111-137): jump to a uniform point on the
+// largest empty circle, angle 2 pi u through sincospi_own(2u), until the distance is below eps;
+// stopped after max_steps jumps.
+inline float wos_path(const Scene<2> &s, float eps, Rng &rng, Vec<2> x, unsigned &queries,
+                      unsigned max_steps = 4096) {
+    for (unsigned step = 0;; step++) {
+        const ClosestPoint c = closest_point(s, x);
+        queries++;
+        const float R = std::sqrt(c.d2);
+        if (R < eps || c.elem == 0xFFFFFFFFu) return c.elem == 0xFFFFFFFFu ? 0.0f : closest_value(s, c);
+        if (step + 1 >= max_steps) return closest_value(s, c);
+        float sn, cs;
+        sincospi_own(2.0f * rng.uniform(), &sn, &cs);
+        x.v[0] = x.v[0] + R * cs;
+        x.v[1] = x.v[1] + R * sn;
+    }
 }
 
 }  // namespace wob_oracle

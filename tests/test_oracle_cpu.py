@@ -169,3 +169,35 @@ def test_backward_control_variate_oracle(oracle, bie):
     d = withcv.astype(np.float64) - plain[:, :, 0]
     z = d.mean(1) / (d.std(1) / np.sqrt(d.shape[1]))
     assert np.all(np.abs(z) < 4.5), z
+
+
+def test_walk_on_spheres_oracle_unbiased(oracle):
+    """apps/simple_wob_and_wos.cu:111-137 restated: WoS on the star with g = e^x cos y (harmonic)
+    is unbiased up to the eps-shell error; per-point z-tests."""
+    import wobtoolbox_gb300 as wob
+    sc = W.config0_scene()
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+    pts = sc["points"][::397]
+    n = 3000
+    p = wob.EstimatorParams(num_sample_paths=n, eps=1e-4, seed=2)
+    s, pp, q = oracle.wos(el, p, pts, per_path=True)
+    mean = s / n
+    sd = pp.std(1)
+    z = (mean - W.exp_cos(pts)[:, 0]) / (sd / np.sqrt(n))
+    assert np.all(np.abs(z) < 4.5), z
+    assert 5 < q / (len(pts) * n) < 60
+
+
+def test_closest_point_oracle_brute_force(oracle):
+    sc = W.config0_scene()
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1.3, 1.3, (200, 2)).astype(np.float32)
+    e, d2, v = oracle.closest_point(el, x)
+    a, b = el.verts[:, 0].astype(np.float64), el.verts[:, 1].astype(np.float64)
+    for i in range(len(x)):
+        l = b - a
+        t = np.clip(((x[i] - a) * l).sum(1) / (l * l).sum(1), 0, 1)
+        dd = (((a + l * t[:, None]) - x[i]) ** 2).sum(1)
+        # float32 distances: the closest point is exact to a few ulp of the coordinates
+        assert abs(np.sqrt(dd.min()) - np.sqrt(d2[i])) <= 1e-6

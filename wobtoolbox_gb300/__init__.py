@@ -323,6 +323,17 @@ class SceneHost:
                                                _ptr(sum_), _ptr(sumsq), _ptr(bounces), _ptr(per_path),
                                                _stream_ptr(stream)))
 
+    # ---- walk on spheres (apps/simple_wob_and_wos.cu), 2D Dirichlet scenes
+    def solve_wos(self, params: EstimatorParams, points, n_points: int, sum_=None, sumsq=None, queries=None,
+                  per_path=None, stream=None) -> None:
+        p = params.to_c()
+        check(load().wob_solve_wos(self._h, C.byref(p), _ptr(points), int(n_points), _ptr(sum_), _ptr(sumsq),
+                                   _ptr(queries), _ptr(per_path), _stream_ptr(stream)))
+
+    def closest_point(self, points, n_points: int, elems, dist2, values, stream=None) -> None:
+        check(load().wob_closest_point(self._h, _ptr(points), int(n_points), _ptr(elems), _ptr(dist2), _ptr(values),
+                                       _stream_ptr(stream)))
+
     # ---- virtual point lights (apps/potential_flow_with_vpl.cu)
     def vpl_paths(self, params: EstimatorParams, n_paths: int, vpl_points, vpl_values, bounces=None,
                   stream=None) -> None:

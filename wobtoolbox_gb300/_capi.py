@@ -34,7 +34,7 @@ EXPORTED = [
     "wob_mlp_num_params", "wob_mlp_get_params", "wob_mlp_set_params", "wob_mlp_forward", "wob_mlp_gradient",
     "wob_mlp_adam_step", "wob_scene_set_rhs", "wob_solve_domain_multi", "wob_solve_unknown_boundary_multi",
     "wob_scene_set_rhs_control_variate", "wob_solve_domain_multi_cv", "wob_scene_create_device",
-    "wob_vpl_paths", "wob_vpl_aggregate",
+    "wob_vpl_paths", "wob_vpl_aggregate", "wob_solve_wos", "wob_closest_point",
 ]
 
 
@@ -121,6 +121,8 @@ def load() -> C.CDLL:
         "wob_scene_create_device": (C.c_int, [C.c_int, u32, vp, vp, vp, vp, vp, vp, P(vp)]),
         "wob_vpl_paths": (C.c_int, [vp, P(wob_params), u32, vp, vp, vp, vp]),
         "wob_vpl_aggregate": (C.c_int, [vp, f32, vp, vp, u32, vp, u32, vp, vp]),
+        "wob_solve_wos": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp, vp, vp, vp]),
+        "wob_closest_point": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
         "wob_solve_domain_multi_cv": (C.c_int, [vp, P(wob_params), u32, vp, u32, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():

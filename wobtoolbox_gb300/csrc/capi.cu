@@ -10,6 +10,7 @@
 #include "multi_rhs.hpp"
 #include "scene_build_gpu.hpp"
 #include "vpl.hpp"
+#include "wos.hpp"
 #include "scene_host.hpp"
 #include "walk_generic.cuh"
 
@@ -952,6 +953,40 @@ int wob_solve_unknown_boundary_multi(wob_scene s, const wob_params *params, cons
     a.stream = (cudaStream_t)stream;
     cudaError_t e = s->host.dim == 2 ? wobgb::launch_multi_rhs_2d(s->view<2>(), w, a) : wobgb::launch_multi_rhs_3d(s->view<3>(), w, a);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the multi-RHS unknown-boundary walk");
+}
+
+int wob_solve_wos(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                  double *sumsq, uint64_t *queries, float *per_path, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (s->host.dim != 2) return fail(WOB_ERR_UNSUPPORTED, "walk on spheres is implemented for 2D scenes");
+    if (!s->all_dirichlet) return fail(WOB_ERR_UNSUPPORTED, "walk on spheres needs Dirichlet data on every element");
+    if (!params) return fail(WOB_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (params->num_sample_paths < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "num_sample_paths must be >= 1");
+    if (!(params->eps > 0.0f)) return fail(WOB_ERR_INVALID_ARGUMENT, "eps must be positive");
+    if (n_points == 0) return WOB_OK;
+    if (!points || (!sum && !per_path)) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum (or per_path) are required");
+    wobgb::WalkParams w{};
+    w.n_paths = params->num_sample_paths;
+    w.eps = params->eps;
+    w.seed = params->seed;
+    w.path_offset = params->path_offset;
+    w.point_offset = params->point_offset;
+    DeviceGuard g(s->device);
+    cudaError_t e = wobgb::launch_wos_2d(s->view<2>(), w, points, n_points, sum, sumsq, (unsigned long long *)queries,
+                                         per_path, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the walk on spheres");
+}
+
+int wob_closest_point(wob_scene s, const float *points, uint32_t n_points, uint32_t *elems, float *dist2,
+                      float *values, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (s->host.dim != 2) return fail(WOB_ERR_UNSUPPORTED, "the closest-point query is implemented for 2D scenes");
+    if (n_points == 0) return WOB_OK;
+    if (!points || !elems || !dist2 || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "all arrays are required");
+    DeviceGuard g(s->device);
+    cudaError_t e = wobgb::launch_closest_point_2d(s->view<2>(), points, n_points, elems, dist2, values,
+                                                   (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the closest-point query");
 }
 
 int wob_vpl_paths(wob_scene s, const wob_params *params, uint32_t n_paths, float *vpl_points, float *vpl_values,

@@ -20,6 +20,8 @@ constexpr uint32_t kChildEmptyD = 0xFFFFFFFFu;
 // Device error word bits (see ErrorWord in capi.cu).
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrTraversalLimit = 2u;
+constexpr uint32_t kErrWosStepLimit = 4u;  // a walk-on-spheres path reached kWosMaxSteps jumps
+constexpr uint32_t kWosMaxSteps = 4096;
 
 enum : int { kDirichlet = 0, kNeumann = 1, kRobin = 2 };
 enum : int { kSingleLayer = 0, kDoubleLayer = 1, kDirect = 2 };
