@@ -4,6 +4,7 @@
 // Elements are passed in the engine's storage order, as SoA arrays with the layout of
 // wob_scene_create; the parameter block has the layout of wob_params.
 #include "wob_oracle.hpp"
+#include "lbvh_count.hpp"
 
 #include <chrono>
 #include <cstdint>
@@ -304,6 +305,53 @@ uint64_t oracle_solve_domain_bcv(int dim, uint32_t n_elems, const float *verts, 
     auto h = std::make_unique<Holder<3>>();
     fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
     return solve_domain_bcv<3>(h->scene, params, cv, n_pot, points, n_points, sum, sumsq, per_path);
+}
+
+// Roofline constants: runs the domain estimator at the points (params as oracle_solve_domain) and
+// measures, for every line query the walks make, the work of the reference's binary LBVH
+// (lbvh_count.hpp). out = {queries, nodes visited, primitives tested}.
+void oracle_lbvh_stats(int dim, uint32_t n_elems, const float *verts, const float *normals, const float *bvals,
+                       const float *alphas, const int32_t *types, const oracle_params *params, const float *points,
+                       uint32_t n_points, double *out, int n_threads) {
+    set_threads(n_threads);
+    auto run = [&](auto &scene, auto dimtag) {
+        constexpr int D = decltype(dimtag)::value;
+        const BinaryLbvh<D> tree(scene);
+        const Params prm = to_params(params);
+        double q = 0, nn = 0, np = 0;
+#pragma omp parallel reduction(+ : q, nn, np)
+        {
+            LbvhCounter<D> counter(&tree);
+            g_line_observer = &counter;
+#pragma omp for schedule(dynamic, 1)
+            for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
+                Vec<D> x;
+                for (int k = 0; k < D; k++) x.v[k] = points[(size_t)ii * D + k];
+                for (uint32_t j = 0; j < params->num_sample_paths; j++) {
+                    Rng rng(params->seed, kStreamDomain, params->point_offset + (uint32_t)ii, params->path_offset + j);
+                    Estimator<D> est(&scene, prm, &rng);
+                    float o[D + 1];
+                    est.domain(x, o);
+                }
+            }
+            g_line_observer = nullptr;
+            q += (double)counter.queries;
+            nn += (double)counter.nodes;
+            np += (double)counter.prims;
+        }
+        out[0] = q;
+        out[1] = nn;
+        out[2] = np;
+    };
+    if (dim == 2) {
+        auto h = std::make_unique<Holder<2>>();
+        fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        run(h->scene, std::integral_constant<int, 2>());
+    } else {
+        auto h = std::make_unique<Holder<3>>();
+        fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
+        run(h->scene, std::integral_constant<int, 3>());
+    }
 }
 
 // Walk on spheres (2D): per-point sums and per-path values; stream kStreamWos.

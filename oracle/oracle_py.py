@@ -55,6 +55,9 @@ def lib() -> C.CDLL:
         L.oracle_solve_domain_bcv.restype = u64
         L.oracle_solve_domain_bcv.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32,
                                               vp, u32, vp, vp, vp, C.c_int]
+        L.oracle_lbvh_stats.restype = None
+        L.oracle_lbvh_stats.argtypes = [C.c_int, u32, vp, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32, vp,
+                                        C.c_int]
         L.oracle_wos.restype = u64
         L.oracle_wos.argtypes = [u32, vp, vp, vp, vp, C.POINTER(oracle_params), vp, u32, vp, vp, C.c_int]
         L.oracle_closest_point.restype = None
@@ -190,6 +193,18 @@ def solve_domain_bcv(el: Elements, params, cv, n_pot: int, points, per_path: boo
                                       _ptr(el.types), C.byref(ps), _ptr(c), n_pot, _ptr(pts), n, _ptr(s), _ptr(q),
                                       _ptr(pp), n_threads)
     return s, q, int(b), pp
+
+
+def lbvh_stats(el: Elements, params, points, n_threads: int = 0):
+    """Mean nodes visited and primitives tested per line query of the reference's binary LBVH on the
+    line queries the domain estimator makes at these points: (queries, N_node, N_prim)."""
+    pts = _f32(points).reshape(-1, el.dim)
+    out = np.zeros(3)
+    ps = params_struct(params)
+    lib().oracle_lbvh_stats(el.dim, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
+                            _ptr(el.types), C.byref(ps), _ptr(pts), len(pts), _ptr(out), n_threads)
+    q = max(out[0], 1.0)
+    return int(out[0]), out[1] / q, out[2] / q
 
 
 def wos(el: Elements, params, points, per_path: bool = False, n_threads: int = 0):

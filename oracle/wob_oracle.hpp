@@ -287,6 +287,14 @@ template <int D> inline BoundaryPoint<D> bp_from_point(const Vec<D> &p) {
 }
 
 // Element: D vertices, normal, per-vertex boundary value and Robin alpha, one boundary type.
+// Sees every line query the oracle makes (used to measure the work of a reference binary BVH on
+// the queries of a workload, oracle/lbvh_count.hpp); null except while measuring.
+struct LineQueryObserver {
+    virtual void on_line(const float *o, const float *d, int dim) = 0;
+    virtual ~LineQueryObserver() = default;
+};
+inline thread_local LineQueryObserver *g_line_observer = nullptr;
+
 template <int D> struct Element {
     Vec<D> v[D];
     Vec<D> n;
@@ -478,6 +486,7 @@ template <int D> struct Scene {
     // Brute-force "all hits of the infinite line" in element order. Returns the full count;
     // at most kHitBuffer element indices are written.
     unsigned line_query(const Vec<D> &o, const Vec<D> &d, unsigned *hits) const {
+        if (g_line_observer) g_line_observer->on_line(o.v, d.v, D);
         unsigned count = 0;
         Vec<D> p;
         for (unsigned i = 0; i < (unsigned)elems.size(); i++) {
