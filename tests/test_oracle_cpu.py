@@ -201,3 +201,18 @@ def test_closest_point_oracle_brute_force(oracle):
         dd = (((a + l * t[:, None]) - x[i]) ** 2).sum(1)
         # float32 distances: the closest point is exact to a few ulp of the coordinates
         assert abs(np.sqrt(dd.min()) - np.sqrt(d2[i])) <= 1e-6
+
+
+def test_lbvh_work_counter(oracle):
+    """The binary-LBVH work counter behind the roofline constants: every line query tests at least
+    the primitives it hits and visits at least the root; a line far from the scene visits only
+    the root."""
+    import wobtoolbox_gb300 as wob
+    sc = W.config0_scene()
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+    p = wob.EstimatorParams(bie_model=1, path_length=2, num_sample_paths=4, seed=0)
+    pts = sc["points"][::50]
+    q, nn, npr = oracle.lbvh_stats(el, p, pts)
+    assert q == len(pts) * 4 * 3
+    assert nn >= 1.0 and npr >= 2.0  # a line through an interior point crosses the closed boundary
+    assert nn < 2 * len(el.verts) and npr < len(el.verts)
