@@ -309,8 +309,8 @@ int wob_closest_point(wob_scene scene, const float *points, uint32_t n_points, u
  * [n_paths] (device); params.path_offset selects the paths (Philox streams of their own).
  * wob_vpl_aggregate (AggregateFunc) adds, at every point x of points [n_points][dim],
  * sum_i mu_i * (G(y_i, x) A, dG/dx(y_i, x) A) into sum [n_points][dim+1] (double, device), A the
- * scene's total boundary area, eps the kernel's distance clamp; partial sums are FP32 over blocks
- * of 256 VPLs in order, added in FP64.
+ * scene's total boundary area, eps the kernel's distance clamp; partial sums are FP32 over tiles
+ * of 256 VPLs, tile t added in FP64 into split t mod 8, the 8 splits added in order.
  */
 int wob_vpl_paths(wob_scene scene, const wob_params *params, uint32_t n_paths, float *vpl_points,
                   float *vpl_values, uint64_t *bounces, void *stream);

@@ -433,7 +433,8 @@ uint64_t oracle_vpl_paths(int dim, uint32_t n_elems, const float *verts, const f
 }
 
 // VPL aggregation (apps/potential_flow_with_vpl.cu:43-75): sum[pt] += sum_i mu_i (G A, dG/dx A),
-// FP32 partial sums over blocks of 256 VPLs in order, added in FP64 (the engine's blocking).
+// the engine's blocking: FP32 partial sums over tiles of 256 VPLs, tile t added in FP64 into split
+// t mod 8 (in tile order), the 8 splits added in order.
 void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, const float *vpl_mu, uint32_t n_vpl,
                           const float *points, uint32_t n_points, double *sum, int n_threads) {
     set_threads(n_threads);
@@ -445,8 +446,10 @@ void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, co
         for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
             Vec<D> x;
             for (int k = 0; k < D; k++) x.v[k] = points[(size_t)ii * D + k];
-            double acc[D + 1] = {};
-            for (uint32_t t0 = 0; t0 < n_vpl; t0 += 256) {
+            const uint32_t n_tiles = (n_vpl + 255) / 256;
+            double split[8][D + 1] = {};
+            for (uint32_t t = 0; t < n_tiles; t++) {
+                const uint32_t t0 = t * 256;
                 const uint32_t m = std::min<uint32_t>(256u, n_vpl - t0);
                 float part[D + 1] = {};
                 for (uint32_t j = 0; j < m; j++) {
@@ -458,9 +461,13 @@ void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, co
                     part[0] = part[0] + mu * u;
                     for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (g.v[k] * area);
                 }
-                for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
+                for (int c = 0; c <= D; c++) split[t % 8][c] += (double)part[c];
             }
-            for (int c = 0; c <= D; c++) sum[(size_t)ii * (D + 1) + c] += acc[c];
+            for (int c = 0; c <= D; c++) {
+                double total = split[0][c];
+                for (int k = 1; k < 8; k++) total = total + split[k][c];
+                sum[(size_t)ii * (D + 1) + c] += total;
+            }
         }
     };
     if (dim == 2) run(std::integral_constant<int, 2>());

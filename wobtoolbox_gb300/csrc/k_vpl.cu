@@ -6,10 +6,9 @@
 // 2. aggregation (AggregateFunc, :43-75): every evaluation point x sums, over all VPLs,
 //    mu_i * G(y_i, x) * A and mu_i * dG/dx(y_i, x) * A (the single layer's solution_domain_unknown /
 //    gradient_domain_unknown, A = total boundary area) -- an N_points x N_vpl dense sum of kernel
-//    evaluations, FP32-issue bound: each thread owns one point, the block stages tiles of 256 VPLs
-//    (position, mu) in shared memory and every thread runs over the tile. Partial sums are FP32 per
-//    tile of 256 VPLs, added into FP64 per point, in VPL order (the oracle does the same blocking,
-//    so the sums are bit-identical).
+//    evaluations, FP32-issue bound. Partial sums are FP32 per tile of 256 VPLs; tile t goes to
+//    split t mod 8, each split adds its tiles in order into FP64, and the 8 split sums of a point
+//    are added in split order (the oracle does the same blocking, so the sums are bit-identical).
 #include "kernels.cuh"
 #include "vpl.hpp"
 
@@ -41,14 +40,21 @@ __global__ void __launch_bounds__(kBlock) vpl_paths_kernel(SceneView<D> s, WalkP
     }
 }
 
+// One block serves 32 points with 8 warps; warp w sums the tiles t = w, w + 8, ... (all lanes read
+// the same VPL at a time: one broadcast load), so 8 threads share a point's pairs and the grid
+// fills the GPU even for a few ten thousand points. The 8 per-warp FP64 partial sums of a point
+// are then added in warp order.
+constexpr int kVplSplit = 8;
+
 template <int D>
-__global__ void __launch_bounds__(kVplTile) vpl_aggregate_kernel(const float *__restrict__ vpl_p,
-                                                                 const float *__restrict__ vpl_mu, uint32_t n_vpl,
-                                                                 float area, float eps, const float *__restrict__ pts,
-                                                                 uint32_t n_points, double *__restrict__ sum) {
-    __shared__ float sp[kVplTile][D];
-    __shared__ float smu[kVplTile];
-    const uint32_t pt = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * kVplSplit) vpl_aggregate_kernel(const float *__restrict__ vpl_p,
+                                                                       const float *__restrict__ vpl_mu, uint32_t n_vpl,
+                                                                       float area, float eps,
+                                                                       const float *__restrict__ pts, uint32_t n_points,
+                                                                       double *__restrict__ sum) {
+    __shared__ double red[kVplSplit][32][D + 1];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t pt = blockIdx.x * 32u + lane;
     const bool active = pt < n_points;
     V<D> x = vzero<D>();
     if (active)
@@ -57,21 +63,16 @@ __global__ void __launch_bounds__(kVplTile) vpl_aggregate_kernel(const float *__
     K.eps = eps;
     double acc[D + 1];
     for (int c = 0; c <= D; c++) acc[c] = 0.0;
-    for (uint32_t t0 = 0; t0 < n_vpl; t0 += kVplTile) {
+    const uint32_t n_tiles = (n_vpl + kVplTile - 1) / kVplTile;
+    for (uint32_t t = w; t < n_tiles; t += kVplSplit) {
+        const uint32_t t0 = t * kVplTile;
         const uint32_t m = min((uint32_t)kVplTile, n_vpl - t0);
-        __syncthreads();
-        if (threadIdx.x < m) {
-            for (int k = 0; k < D; k++) sp[threadIdx.x][k] = __ldg(vpl_p + (size_t)(t0 + threadIdx.x) * D + k);
-            smu[threadIdx.x] = __ldg(vpl_mu + t0 + threadIdx.x);
-        }
-        __syncthreads();
-        if (!active) continue;
         float part[D + 1];
         for (int c = 0; c <= D; c++) part[c] = 0.0f;
         for (uint32_t j = 0; j < m; j++) {
             V<D> y;
-            for (int k = 0; k < D; k++) y.v[k] = sp[j][k];
-            const float mu = smu[j];
+            for (int k = 0; k < D; k++) y.v[k] = __ldg(vpl_p + (size_t)(t0 + j) * D + k);
+            const float mu = __ldg(vpl_mu + t0 + j);
             const float u = K.G(y, x) * area;
             const V<D> g = K.dG_dx(y, x);
             part[0] = part[0] + mu * u;
@@ -79,8 +80,15 @@ __global__ void __launch_bounds__(kVplTile) vpl_aggregate_kernel(const float *__
         }
         for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
     }
-    if (active)
-        for (int c = 0; c <= D; c++) sum[(size_t)pt * (D + 1) + c] += acc[c];
+    for (int c = 0; c <= D; c++) red[w][lane][c] = acc[c];
+    __syncthreads();
+    if (w == 0 && active) {
+        for (int c = 0; c <= D; c++) {
+            double total = red[0][lane][c];
+            for (int k = 1; k < kVplSplit; k++) total = total + red[k][lane][c];
+            sum[(size_t)pt * (D + 1) + c] += total;
+        }
+    }
 }
 
 template <int D>
@@ -95,8 +103,8 @@ template <int D>
 cudaError_t aggregate_impl(const float *vpl_p, const float *vpl_mu, uint32_t n_vpl, float area, float eps,
                            const float *pts, uint32_t n_points, double *sum, cudaStream_t st) {
     if (n_points == 0) return cudaSuccess;
-    vpl_aggregate_kernel<D><<<(n_points + kVplTile - 1) / kVplTile, kVplTile, 0, st>>>(vpl_p, vpl_mu, n_vpl, area, eps,
-                                                                                      pts, n_points, sum);
+    vpl_aggregate_kernel<D><<<(n_points + 31) / 32, 32 * kVplSplit, 0, st>>>(vpl_p, vpl_mu, n_vpl, area, eps, pts,
+                                                                            n_points, sum);
     return cudaGetLastError();
 }
 
