@@ -435,6 +435,18 @@ def run_ours(args):
             out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": threads, "kind": "port",
                                    "sample": f"{len(sample_pts)} inside slice points x {args.cpu_paths} paths x "
                                              f"{PATH_LENGTH} bounces ({dt:.1f} s)"}
+        elif not args.no_cpu_baseline and args.workload == "dl2d":
+            # the full 2D workload on the host cores: 7,960 points x 1024 paths x 8 bounces, line
+            # queries through the oracle's binary BVH (the reference's algorithm, same results)
+            from oracle import oracle_py as O
+            O.build()
+            el = O.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+            t0 = time.perf_counter()
+            _, _, b, _ = O.solve_domain(el, p, sc["points"], accel=True)
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                                   "sample": f"the full workload: {len(sc['points'])} points x {p.num_sample_paths} "
+                                             f"paths x {p.path_length} bounces ({dt:.1f} s)"}
     scene.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

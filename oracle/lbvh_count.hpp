@@ -26,7 +26,7 @@ template <int D> struct BinaryLbvh {
     std::vector<int> left, right;  // child >= 0: internal node; child < 0: leaf -(object + 1)
     std::vector<Box> ibox, lbox;   // internal node boxes, object boxes
 
-    explicit BinaryLbvh(const Scene<D> &s) {
+    explicit BinaryLbvh(const Scene<D> &s, float pad = 0.0f) {
         n = (int)s.elems.size();
         lbox.resize(n);
         std::vector<float> cen((size_t)n * 3, 0.0f);
@@ -44,8 +44,8 @@ template <int D> struct BinaryLbvh {
                     hi = std::max(hi, e.v[j].v[k]);
                     c += e.v[j].v[k];
                 }
-                lbox[i].lo[k] = lo;
-                lbox[i].hi[k] = hi;
+                lbox[i].lo[k] = lo - pad;
+                lbox[i].hi[k] = hi + pad;
                 cen[3 * i + k] = c / D;
                 clo[k] = std::min(clo[k], cen[3 * i + k]);
                 chi[k] = std::max(chi[k], cen[3 * i + k]);
@@ -145,6 +145,37 @@ template <int D> struct BinaryLbvh {
             tf = std::min(tf, t2);
         }
         return tn <= tf;
+    }
+
+    // the objects whose (padded) boxes the line crosses; UINT32_MAX when more than cap
+    unsigned candidates(const float *o, const float *d, unsigned *cand, unsigned cap) const {
+        unsigned m = 0;
+        if (n < 2) {
+            for (int i = 0; i < n; i++) cand[m++] = (unsigned)i;
+            return m;
+        }
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int node = stack[--sp];
+            for (int c : {left[node], right[node]}) {
+                const Box &b = c < 0 ? lbox[-c - 1] : ibox[c];
+                if (!crosses(b, o, d)) continue;
+                if (c < 0) {
+                    if (m == cap) return 0xFFFFFFFFu;
+                    cand[m++] = (unsigned)(-c - 1);
+                } else if (sp < 128) {
+                    stack[sp++] = c;
+                } else {
+                    return 0xFFFFFFFFu;
+                }
+            }
+        }
+        return m;
+    }
+    static unsigned candidates_cb(const void *self, const float *o, const float *d, unsigned *cand, unsigned cap) {
+        return static_cast<const BinaryLbvh *>(self)->candidates(o, d, cand, cap);
     }
 
     // adds the nodes visited and primitives tested by one infinite-line query

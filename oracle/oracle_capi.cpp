@@ -227,6 +227,22 @@ uint64_t solve_unknown(const Scene<D> &s, const oracle_params *op, const float *
     return total_bounces;
 }
 
+// Box padding of the line-query filter: 1e-5 (extent + max |coordinate|), far above the rounding of
+// the box test, so it never drops an element the exact test accepts.
+template <int D> float accel_pad(const Scene<D> &s) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, mag = 0.0f;
+    for (const Element<D> &e : s.elems)
+        for (int j = 0; j < D; j++)
+            for (int k = 0; k < D; k++) {
+                lo[k] = std::min(lo[k], e.v[j].v[k]);
+                hi[k] = std::max(hi[k], e.v[j].v[k]);
+                mag = std::max(mag, std::fabs(e.v[j].v[k]));
+            }
+    float ext = 0.0f;
+    for (int k = 0; k < D; k++) ext = std::max(ext, hi[k] - lo[k]);
+    return 1e-5f * (ext + mag) + 1e-30f;
+}
+
 template <int D> struct Holder {
     Scene<D> scene;
     VolumeCache<D> vol;
@@ -242,15 +258,30 @@ uint64_t oracle_solve_domain(int dim, uint32_t n_elems, const float *verts, cons
                              const float *vol_values, const oracle_params *params, const float *points,
                              uint32_t n_points, double *sum, double *sumsq, float *per_path, int n_threads) {
     set_threads(n_threads);
+    // flags bit 0: filter line queries through a padded binary BVH (same hits, same order; used by
+    // the CPU baseline so the host runs the reference's algorithm at a realistic speed)
+    const bool accel = (params->flags & 1u) != 0u;
     if (dim == 2) {
         auto h = std::make_unique<Holder<2>>();
         fill_elements<2>(h->scene, n_elems, verts, normals, bvals, alphas, types);
         if (vol_res) { h->vol.build(vol_res, vol_size, vol_values); h->scene.vol = &h->vol; }
+        std::unique_ptr<BinaryLbvh<2>> tree;
+        if (accel) {
+            tree = std::make_unique<BinaryLbvh<2>>(h->scene, accel_pad(h->scene));
+            h->scene.accel = tree.get();
+            h->scene.accel_candidates = &BinaryLbvh<2>::candidates_cb;
+        }
         return solve_domain<2>(h->scene, params, points, n_points, sum, sumsq, per_path);
     }
     auto h = std::make_unique<Holder<3>>();
     fill_elements<3>(h->scene, n_elems, verts, normals, bvals, alphas, types);
     if (vol_res) { h->vol.build(vol_res, vol_size, vol_values); h->scene.vol = &h->vol; }
+    std::unique_ptr<BinaryLbvh<3>> tree;
+    if (accel) {
+        tree = std::make_unique<BinaryLbvh<3>>(h->scene, accel_pad(h->scene));
+        h->scene.accel = tree.get();
+        h->scene.accel_candidates = &BinaryLbvh<3>::candidates_cb;
+    }
     return solve_domain<3>(h->scene, params, points, n_points, sum, sumsq, per_path);
 }
 

@@ -94,14 +94,15 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
-def params_struct(p) -> oracle_params:
-    """From any object with the wob_params field names (e.g. wobtoolbox_gb300.EstimatorParams)."""
+def params_struct(p, accel: bool = False) -> oracle_params:
+    """From any object with the wob_params field names (e.g. wobtoolbox_gb300.EstimatorParams).
+    accel: filter line queries through the oracle's padded binary BVH (same results, faster)."""
     s = oracle_params()
     for name, _ in oracle_params._fields_:
         if name == "flags":
             continue
         setattr(s, name, getattr(p, name))
-    s.flags = 0
+    s.flags = 1 if accel else 0
     return s
 
 
@@ -126,7 +127,7 @@ class Elements:
         return res, float(size), vals
 
 
-def solve_domain(el: Elements, params, points, per_path: bool = False, n_threads: int = 0):
+def solve_domain(el: Elements, params, points, per_path: bool = False, n_threads: int = 0, accel: bool = False):
     pts = _f32(points).reshape(-1, el.dim)
     n = len(pts)
     D = el.dim
@@ -134,7 +135,7 @@ def solve_domain(el: Elements, params, points, per_path: bool = False, n_threads
     q = np.zeros((n, D + 1))
     pp = np.zeros((n, params.num_sample_paths, D + 1), dtype=np.float32) if per_path else None
     res, size, vals = el._vol()
-    ps = params_struct(params)
+    ps = params_struct(params, accel)
     b = lib().oracle_solve_domain(D, el.n, _ptr(el.verts), _ptr(el.normals), _ptr(el.bvals), _ptr(el.alphas),
                                   _ptr(el.types), res, size, _ptr(vals), C.byref(ps), _ptr(pts), n, _ptr(s),
                                   _ptr(q), _ptr(pp), n_threads)

@@ -483,12 +483,33 @@ template <int D> struct Scene {
         }
     }
 
-    // Brute-force "all hits of the infinite line" in element order. Returns the full count;
-    // at most kHitBuffer element indices are written.
+    // Optional candidate filter for line_query (oracle/lbvh_count.hpp's padded binary BVH): writes
+    // the elements whose boxes the line crosses, in any order, and returns their number (or
+    // UINT32_MAX when more than cap). The exact test and the storage order stay those below.
+    const void *accel = nullptr;
+    unsigned (*accel_candidates)(const void *, const float *o, const float *d, unsigned *cand, unsigned cap) = nullptr;
+
+    // "All hits of the infinite line" in element order (brute force, or the exact test on the
+    // candidates of the filter, sorted). Returns the full count; at most kHitBuffer element
+    // indices are written.
     unsigned line_query(const Vec<D> &o, const Vec<D> &d, unsigned *hits) const {
         if (g_line_observer) g_line_observer->on_line(o.v, d.v, D);
         unsigned count = 0;
         Vec<D> p;
+        if (accel) {
+            unsigned cand[4096];
+            const unsigned nc = accel_candidates(accel, o.v, d.v, cand, 4096);
+            if (nc != 0xFFFFFFFFu) {
+                std::sort(cand, cand + nc);
+                for (unsigned k = 0; k < nc; k++) {
+                    if (line_elem_intersect(o, d, elems[cand[k]], p)) {
+                        if (count < kHitBuffer) hits[count] = cand[k];
+                        count++;
+                    }
+                }
+                return count;
+            }
+        }
         for (unsigned i = 0; i < (unsigned)elems.size(); i++) {
             if (line_elem_intersect(o, d, elems[i], p)) {
                 if (count < kHitBuffer) hits[count] = i;

@@ -216,3 +216,22 @@ def test_lbvh_work_counter(oracle):
     assert q == len(pts) * 4 * 3
     assert nn >= 1.0 and npr >= 2.0  # a line through an interior point crosses the closed boundary
     assert nn < 2 * len(el.verts) and npr < len(el.verts)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_bvh_filter_is_exact(oracle, dim):
+    """The oracle's optional BVH filter for line queries (used by the CPU baseline) changes no path."""
+    import wobtoolbox_gb300 as wob
+    if dim == 2:
+        sc = W.config0_scene()
+        el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
+        pts = sc["points"][::200]
+        p = wob.EstimatorParams(bie_model=1, path_length=6, num_sample_paths=32, seed=3)
+    else:
+        sc = S.scene3d(1, False, subdiv=3)
+        el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+        pts = sc["points"]
+        p = wob.EstimatorParams(bie_model=2, problem=1, path_length=4, num_sample_paths=32, seed=3)
+    _, _, b1, pp1 = oracle.solve_domain(el, p, pts, per_path=True)
+    _, _, b2, pp2 = oracle.solve_domain(el, p, pts, per_path=True, accel=True)
+    assert b1 == b2 and np.array_equal(pp1, pp2)
