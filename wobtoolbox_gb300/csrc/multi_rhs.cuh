@@ -201,7 +201,7 @@ template <int D> struct RhsData {
 constexpr uint32_t kFull = 0xffffffffu;
 
 template <int D, int kBie, int kStrat, bool kUnknown, bool kCV>
-__global__ void __launch_bounds__(kBlock) multi_rhs_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
+__global__ void __launch_bounds__(kBlock, 5) multi_rhs_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                            BoundaryInput bin, RhsData<D> rd, uint32_t n_points,
                                                            double *__restrict__ sum, double *__restrict__ sumsq,
                                                            unsigned long long *__restrict__ bounces,
