@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["capi.cu", "kernels_dispatch.cu", "k2_generic_domain.cu", "k2_generic_boundary.cu", "k3_generic_domain.cu",
               "k3_generic_boundary.cu", "k2_fast.cu", "k3_fast.cu", "k_batch.cu", "k_cv.cu",
               "k2_multi_rhs.cu", "k3_multi_rhs.cu", "mlp.cu", "scene_build_gpu.cu",
-              "k_vpl.cu", "k_wos.cu"]
+              "k_vpl.cu", "k_wos.cu", "k_sl.cu"]
 CPP_SOURCES = ["scene_build.cpp"]
 
 

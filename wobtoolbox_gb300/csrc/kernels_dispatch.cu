@@ -66,6 +66,10 @@ cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const f
     const int st = strategy_of(p.bie, p.estimator, p.problem);
     if (p.n_volume == 0 && st == kStratDirectNeumann)
         return launch_domain_variant<2, kDirect, kStratDirectNeumann, false>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+    if (p.n_volume == 0 && st == kStratSingleLayer)
+        return launch_domain_variant<2, kSingleLayer, kStratSingleLayer, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+    if (p.n_volume == 0 && st == kStratFwdSlNeumann)
+        return launch_domain_variant<2, kSingleLayer, kStratFwdSlNeumann, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
     return launch_domain_variant<2, -1, kStratRuntime, true>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
 }
 
@@ -74,6 +78,11 @@ cudaError_t launch_domain_3d(const SceneView<3> &s, const WalkParams &p, const f
                              cudaStream_t stream) {
     const int v = tunable_domain_variant(3, p);
     if (v >= 0) return launch_domain_config(3, v, domain_config(v), &s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+    const int st = strategy_of(p.bie, p.estimator, p.problem);
+    if (p.n_volume == 0 && st == kStratSingleLayer)
+        return launch_domain_variant<3, kSingleLayer, kStratSingleLayer, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+    if (p.n_volume == 0 && st == kStratFwdSlNeumann)
+        return launch_domain_variant<3, kSingleLayer, kStratFwdSlNeumann, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
     return launch_domain_variant<3, -1, kStratRuntime, true>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
 }
 
