@@ -458,8 +458,9 @@ def run_ours(args):
 def run_batch(args):
     """Batched workload: 256 seeded 2D scenes (lobes U{3..9}, amplitude U[0.1, 0.35], segments
     log-uniform in [64, 16384], points U[1k, 64k]; interior / exterior x Neumann / Robin, Gaussian
-    sources in the interior scenes) in one persistent launch, against the same 256 solves launched
-    one after another (eagerly and replayed from a captured CUDA graph)."""
+    sources in the interior scenes) in one persistent launch per walk variant (three here: backward
+    single layer, forward single-layer Neumann, the general walk for the scenes with sources), against
+    the same 256 solves launched one after another (eagerly and replayed from a captured CUDA graph)."""
     import torch
     import wobtoolbox_gb300 as wob
     from wobtoolbox_gb300 import workloads as W
@@ -532,7 +533,8 @@ def run_batch(args):
     clk = clocks.summary()
     value = bounces_batched / (sum(b_ms) / 1e3)
     out = {
-        "metric": "batched plain WoB: speedup of one persistent launch over 256 sequential launches",
+        "metric": "batched plain WoB: speedup of persistent batched launches (one per walk variant) over 256 "
+                  "sequential launches",
         "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sum(b_ms) / len(b_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",

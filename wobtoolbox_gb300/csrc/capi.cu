@@ -14,6 +14,7 @@
 #include "scene_host.hpp"
 #include "walk_generic.cuh"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -115,12 +116,16 @@ struct wob_scene_s {
 };
 
 // A batch of scenes solved in one persistent launch (k_batch.cu). The scenes must outlive it.
+// The table is grouped by walk class (batch_walk_class): one persistent launch per class present,
+// each over its contiguous part of the table with unit numbers restarting at 0.
 struct wob_batch_s {
     int device = 0;
     int dim = 0;
     uint32_t n_scenes = 0;
     uint64_t total_units = 0;
     uint32_t total_points = 0;
+    uint32_t cls_first[3] = {0, 0, 0}, cls_count[3] = {0, 0, 0};
+    uint64_t cls_units[3] = {0, 0, 0};
     DevBuf table;
 };
 
@@ -731,12 +736,12 @@ int wob_batch_create(const wob_scene *scenes, const wob_params *params, const ui
         if (dim == 2) {
             wobgb::BatchEntry<2> e{};
             e.view = s->view<2>(); e.params = w; e.unit_begin = units; e.point_begin = (uint32_t)points;
-            e.n_points = n_points[i]; e.slabs = slabs;
+            e.n_points = n_points[i]; e.slabs = slabs; e.cls = wobgb::batch_walk_class(w);
             t2.push_back(e);
         } else {
             wobgb::BatchEntry<3> e{};
             e.view = s->view<3>(); e.params = w; e.unit_begin = units; e.point_begin = (uint32_t)points;
-            e.n_points = n_points[i]; e.slabs = slabs;
+            e.n_points = n_points[i]; e.slabs = slabs; e.cls = wobgb::batch_walk_class(w);
             t3.push_back(e);
         }
         units += (uint64_t)n_points[i] * slabs;
@@ -749,6 +754,26 @@ int wob_batch_create(const wob_scene *scenes, const wob_params *params, const ui
     b->n_scenes = n_scenes;
     b->total_units = units;
     b->total_points = (uint32_t)points;
+    // group by walk class, keeping the caller's order within a class; unit numbers per class
+    auto group = [b](auto &t) {
+        std::stable_sort(t.begin(), t.end(), [](const auto &x, const auto &y) { return x.cls < y.cls; });
+        uint32_t first = 0;
+        for (uint32_t c = 0; c < 3; c++) {
+            uint64_t u = 0;
+            uint32_t k = first;
+            while (k < t.size() && t[k].cls == c) {
+                t[k].unit_begin = u;
+                u += (uint64_t)t[k].n_points * t[k].slabs;
+                k++;
+            }
+            b->cls_first[c] = first;
+            b->cls_count[c] = k - first;
+            b->cls_units[c] = u;
+            first = k;
+        }
+    };
+    if (dim == 2) group(t2);
+    else group(t3);
     DeviceGuard g(device);
     cudaError_t e = dim == 2 ? upload(b->table, t2.data(), t2.size() * sizeof(t2[0]))
                              : upload(b->table, t3.data(), t3.size() * sizeof(t3[0]));
@@ -766,11 +791,17 @@ int wob_batch_solve(wob_batch b, const float *points, double *sum, double *sumsq
     if (b->total_points == 0) return WOB_OK;
     if (!points || !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum are required");
     DeviceGuard g(b->device);
-    cudaError_t e = b->dim == 2
-        ? wobgb::launch_batch_2d((const wobgb::BatchEntry<2> *)b->table.ptr, b->n_scenes, b->total_units, points, sum,
-                                 sumsq, (unsigned long long *)bounces, path_offset_add, (cudaStream_t)stream)
-        : wobgb::launch_batch_3d((const wobgb::BatchEntry<3> *)b->table.ptr, b->n_scenes, b->total_units, points, sum,
-                                 sumsq, (unsigned long long *)bounces, path_offset_add, (cudaStream_t)stream);
+    cudaError_t e = cudaSuccess;
+    for (uint32_t c = 0; c < 3 && e == cudaSuccess; c++) {
+        if (b->cls_count[c] == 0 || b->cls_units[c] == 0) continue;
+        e = b->dim == 2
+            ? wobgb::launch_batch_2d((const wobgb::BatchEntry<2> *)b->table.ptr + b->cls_first[c], b->cls_count[c], c,
+                                     b->cls_units[c], points, sum, sumsq, (unsigned long long *)bounces,
+                                     path_offset_add, (cudaStream_t)stream)
+            : wobgb::launch_batch_3d((const wobgb::BatchEntry<3> *)b->table.ptr + b->cls_first[c], b->cls_count[c], c,
+                                     b->cls_units[c], points, sum, sumsq, (unsigned long long *)bounces,
+                                     path_offset_add, (cudaStream_t)stream);
+    }
     if (e != cudaSuccess) return fail_cuda(e, "launching the batched walk");
     return WOB_OK;
 }

@@ -53,14 +53,15 @@ cudaError_t launch_domain_cv_3d(const SceneView<3> &s, const WalkParams &p, cons
 // Shared error message of the C ABI (capi.cu).
 void set_last_error(const char *msg);
 
-// One scene of a batched launch (k_batch.cu).
+// One scene of a batched launch (k_batch.cu). One launch runs the n_scenes scenes of table, all of
+// walk class cls (batch_walk_class), whose units are numbered from 0.
 template <int D> struct BatchEntry;
-cudaError_t launch_batch_2d(const BatchEntry<2> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
-                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
-                            cudaStream_t stream);
-cudaError_t launch_batch_3d(const BatchEntry<3> *table, uint32_t n_scenes, uint64_t total_units, const float *pts,
-                            double *sum, double *sumsq, unsigned long long *bounces, uint64_t path_offset_add,
-                            cudaStream_t stream);
+cudaError_t launch_batch_2d(const BatchEntry<2> *table, uint32_t n_scenes, uint32_t cls, uint64_t total_units,
+                            const float *pts, double *sum, double *sumsq, unsigned long long *bounces,
+                            uint64_t path_offset_add, cudaStream_t stream);
+cudaError_t launch_batch_3d(const BatchEntry<3> *table, uint32_t n_scenes, uint32_t cls, uint64_t total_units,
+                            const float *pts, double *sum, double *sumsq, unsigned long long *bounces,
+                            uint64_t path_offset_add, cudaStream_t stream);
 // Paths per lane of a warp unit: up to 8, keeping at least 16384 units so the grid-stride loop
 // still balances over the persistent grid.
 inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {

@@ -535,8 +535,19 @@ template <int D> struct BatchEntry {
     SceneView<D> view;
     WalkParams params;
     uint64_t unit_begin;
-    uint32_t point_begin, n_points, slabs, pad;
+    uint32_t point_begin, n_points, slabs;
+    uint32_t cls;  // batch_walk_class of the parameters
 };
+
+// The specialised walk a batched scene runs: 1 = backward single layer, 2 = forward single-layer
+// Neumann (both without a source term), 0 = the general walk.
+__host__ __device__ __forceinline__ uint32_t batch_walk_class(const WalkParams &p) {
+    if (p.n_volume != 0) return 0u;
+    const int st = strategy_of(p.bie, p.estimator, p.problem);
+    if (st == kStratSingleLayer) return 1u;
+    if (st == kStratFwdSlNeumann) return 2u;
+    return 0u;
+}
 
 constexpr uint32_t kStreamDomain = 0u;
 constexpr uint32_t kStreamBoundary = 1u;
