@@ -85,3 +85,37 @@ def test_icosphere_sizes_and_orientation():
     assert np.all((n * V[F].mean(1)).sum(1) > 0)
     Vd, Fd, c = W.displaced_icosphere(3, 0.15, 4, 0)
     assert len(c) == 25 and np.linalg.norm(Vd, axis=1).min() > 0.2
+
+
+def test_cpp_compat_header_compiles_and_links(engine, tmp_path):
+    """include/wob_gb300.hpp (the wob:: names of the reference for C++ hosts) compiles against the
+    C ABI and links with the library; the enum converters and grid helper run without a GPU."""
+    import os
+    import subprocess
+    from wobtoolbox_gb300 import build as B
+    src = tmp_path / "t.cpp"
+    src.write_text(r'''
+#include "wob_gb300.hpp"
+#include <cstdio>
+int main() {
+    using namespace wob;
+    if (string_to_bie_model_type("IndirectDoubleLayer") != IndirectDoubleLayer) return 1;
+    if (string_to_problem_type("MixedProblem") != MixedProblem) return 2;
+    if (string_to_domain_type("nonsense") != DomainTypeCount) return 3;
+    if (bie_model_type_to_string(Direct) != "Direct") return 4;
+    if (estimator_type_to_string(ForwardEstimator) != "ForwardEstimator") return 5;
+    auto p = utils::idx_to_domain_point<2>(0, 4, 1.0f);
+    if (p[0] != -0.375f || p[1] != -0.375f) return 6;
+    EstimatorParams prm;
+    wob_params c = prm.to_c();
+    if (c.bie_model != IndirectDoubleLayer || c.flags != 0) return 7;
+    std::printf("%d\n", wob_version());
+    return 0;
+}
+''')
+    exe = tmp_path / "t"
+    r = subprocess.run(["g++", "-std=c++17", "-I", B.INCLUDE, str(src), "-o", str(exe), "-L", B.OUT, "-lwob_gb300",
+                        "-Wl,-rpath," + B.OUT], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == str(engine.load().wob_version())
