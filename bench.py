@@ -800,10 +800,15 @@ def run_multi_rhs(args):
     for k in range(3):
         dist = torch.linalg.norm(xp[:, None, :] - src[None, :, k, :], dim=2)
         exact += qq[None, :, k] / (4.0 * np.pi * dist)
-    base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.InteriorDomain,
-                               estimator=wob.BackwardEstimator, problem=wob.MixedProblem, path_length=4,
-                               num_resampling_candidates=64, eps=1e-5, first_kind_equation_scaling_constant=2.0,
-                               seed=SEED)
+    if args.mrhs_bie == "direct":  # direct BIE, two uniform samples per bounce (estimator.cuh:335-347)
+        base = wob.EstimatorParams(bie_model=wob.Direct, domain=wob.InteriorDomain, estimator=wob.BackwardEstimator,
+                                   problem=wob.MixedProblem, path_length=args.mrhs_path_length or 4,
+                                   first_kind_equation_scaling_constant=2.0, seed=SEED)
+    else:
+        base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.InteriorDomain,
+                                   estimator=wob.BackwardEstimator, problem=wob.MixedProblem,
+                                   path_length=args.mrhs_path_length or 4, num_resampling_candidates=64, eps=1e-5,
+                                   first_kind_equation_scaling_constant=2.0, seed=SEED)
     paths = args.mrhs_paths
     stream = torch.cuda.current_stream()
     s = torch.zeros(n_pts, R, dtype=torch.float64, device=dev)
@@ -849,6 +854,14 @@ def run_multi_rhs(args):
         lambda p: scene.solve_domain_multi(p, d_pts, n_pts, s, None, b, None, stream), args.mrhs_budget)
     sampler.__exit__(None, None, None)
     clocks = sampler.summary()
+    # how the error is spread over the points (diagnostic): per-point RMS error over the RHS, its
+    # median and the RMSE of the 99 % / 99.9 % of points with the smallest error
+    err_pt = torch.sqrt(((s / plain_curve[-1][2] - exact) ** 2).mean(1))
+    srt = torch.sort(err_pt).values
+    spread = {"median_point_error": float(srt[len(srt) // 2].item()),
+              "rmse_best_99pct_points": float(torch.sqrt((srt[:int(0.99 * len(srt))] ** 2).mean()).item()),
+              "rmse_best_99.9pct_points": float(torch.sqrt((srt[:int(0.999 * len(srt))] ** 2).mean()).item()),
+              "rmse_all_points": float(torch.sqrt((srt ** 2).mean()).item())}
     total = plain_curve[-1][0]
     t_iter = total / len(plain_curve)
     if args.mrhs_plain_only:
@@ -857,7 +870,11 @@ def run_multi_rhs(args):
                               "unit": "bounces/s (each bounce serves every RHS)", "n_gpus": world,
                               "config": {"triangles": int(len(sc["F"])), "points": n_pts, "rhs": R,
                                          "iteration_ms": t_iter * 1e3, "scalar_iteration_ms": t_scalar * 1e3,
-                                         "mean_rmse_over_rhs": plain_curve[-1][1]}, "clocks": clocks}), flush=True)
+                                         "estimator": args.mrhs_bie, "path_length": base.path_length,
+                                         "error_spread": spread,
+                                         "mean_rmse_over_rhs": plain_curve[-1][1], "paths_per_point": plain_curve[-1][2],
+                                         "curve": plain_curve[::max(1, len(plain_curve) // 10)]},
+                              "clocks": clocks}), flush=True)
         scene.close()
         return
     # learned control variate: one MLP with an R-wide head trained on shared-walk density labels
@@ -880,20 +897,24 @@ def run_multi_rhs(args):
         "value": bounces / total, "unit": "bounces/s (each bounce serves every RHS)",
         "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "interior mixed (Dirichlet z>0, Neumann elsewhere), single layer, backward, 4 bounces, "
-                               "64 RIS candidates; 64 RHS of 3 exterior point sources each; 10^6 interior points",
+        "config": {"workload": "interior mixed (Dirichlet z>0, Neumann elsewhere), "
+                               + ("single layer, backward, 64 RIS candidates" if args.mrhs_bie == "sl" else
+                                  "direct BIE, backward, uniform sampling")
+                               + f", {base.path_length} bounces; 64 RHS of 3 exterior point sources each; "
+                                 "10^6 interior points",
                    "triangles": int(len(sc["F"])), "points": n_pts, "rhs": R, "paths_per_iteration": paths,
                    "iterations": len(plain_curve), "gpu_time_s": total, "bounces": bounces,
                    "rhs_bounces_per_s": bounces * R / total,
                    "iteration_ms": {"shared_walk_64_rhs": t_iter * 1e3, "scalar_walk_1_rhs": t_scalar * 1e3},
                    "speedup_vs_separate_scalar_solves": R * t_scalar / t_iter,
                    "plain": {"mean_rmse_over_rhs": plain_curve[-1][1], "paths_per_point": plain_curve[-1][2],
-                             "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": plain_target,
+                             "error_spread": spread,
+                             "time_to_mean_rmse_1e-3_s (variance-only extrapolation, RMSE ~ 1/sqrt(paths); ignores the bias of the truncated series)": plain_target,
                              "curve": plain_curve[::max(1, len(plain_curve) // 10)]},
                    "learned_cv": {"potential_samples": args.mrhs_npot, "setup_s (labels + training + table)": t_setup,
                                   "train_info": info, "mean_rmse_over_rhs": cv_curve[-1][1],
                                   "paths_per_point": cv_curve[-1][2],
-                                  "time_to_mean_rmse_1e-3_s (extrapolated, RMSE ~ 1/sqrt(paths))": cv_target,
+                                  "time_to_mean_rmse_1e-3_s (variance-only extrapolation, RMSE ~ 1/sqrt(paths); ignores the bias of the truncated series)": cv_target,
                                   "curve": cv_curve[::max(1, len(cv_curve) // 10)]},
                    "plain_over_cv_time_to_target": plain_target / (cv_target + t_setup),
                    "setup_s": {"rhs_data": t_data, "scene_build": t_build, "rhs_upload": t_rhs}},
@@ -1147,6 +1168,9 @@ def main():
     ap.add_argument("--mrhs-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload mrhs3d")
     ap.add_argument("--mrhs-npot", type=int, default=4, help="potential samples of the learned CV (mrhs3d)")
     ap.add_argument("--mrhs-plain-only", action="store_true", help="mrhs3d without the learned-CV leg (profiling)")
+    ap.add_argument("--mrhs-bie", choices=["sl", "direct"], default="sl",
+                    help="mrhs3d estimator: single layer + RIS 64 (the reference's Mixed config) or direct, uniform")
+    ap.add_argument("--mrhs-path-length", type=int, default=0, help="mrhs3d bounces (0: 4)")
     ap.add_argument("--build-subdiv", type=int, default=8, help="icosphere subdivision of --workload build3d")
     ap.add_argument("--vpl-paths", type=int, default=100000, help="VPL walks per iteration of --workload vpl2d")
     ap.add_argument("--wos-budget", type=float, default=5.0, help="GPU seconds per method of --workload wos2d")
