@@ -365,6 +365,9 @@ def run_ours(args):
     if exact_u is None:
         exact_u = exact(pts, sc)
     rmse = float(np.sqrt(np.mean((u - exact_u) ** 2)))
+    err = np.sort(np.abs(u - exact_u))
+    error_spread = {"median_point_error": float(err[len(err) // 2]),
+                    "rmse_best_99pct_points": float(np.sqrt(np.mean(err[:int(0.99 * len(err))] ** 2)))}
 
     # end to end through the C ABI with host buffers (copies in the timed region)
     pts_pinned = torch.from_numpy(pts).pin_memory()
@@ -411,7 +414,7 @@ def run_ours(args):
             "config": {"workload": workload, "elements": int(len(sc["verts"])), "points": n_pts,
                        "paths_per_point_per_step": paths, "path_length": p.path_length,
                        "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
-                       "rmse_u_vs_exact": rmse, "paths_per_point_total": n_paths_total,
+                       "rmse_u_vs_exact": rmse, "error_spread": error_spread, "paths_per_point_total": n_paths_total,
                        "parallelism": f"replicas x{world}, points x independent path streams",
                        "autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

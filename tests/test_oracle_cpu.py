@@ -92,7 +92,7 @@ def _z_test(mean, ex, var, n):
 
 
 def test_double_layer_unbiased_2d(oracle):
-    """configs[0]-style walk: DL interior Dirichlet on a star, g = e^x cos y; z-test per point."""
+    """The 2D star workload's walk: DL interior Dirichlet on a star, g = e^x cos y; z-test per point."""
     sc = W.config0_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     import wobtoolbox_gb300 as wob
