@@ -6,6 +6,10 @@
  * Every entry point returns a wob_status; wob_last_error() gives the message of the last failure
  * on the calling thread.
  *
+ * Entry points that take device buffers and a stream only enqueue kernels on that stream (no
+ * allocation, no synchronisation), so they can be captured into a CUDA graph and replayed; the
+ * scene / batch / MLP constructors, the host-buffer solves and the debug entry points synchronise.
+ *
  * Each entry point names the reference interface it replaces (rsugimoto/WoBToolbox, path:line).
  * The enums keep the reference's numbering so a caller can pass the values its string
  * converters produce (bie_models.cuh:24-51, estimator.cuh:24-54, points.hpp:22).
