@@ -471,8 +471,6 @@ void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, co
     set_threads(n_threads);
     auto run = [&](auto dimtag) {
         constexpr int D = decltype(dimtag)::value;
-        EqKernel<D> K;
-        K.eps = eps;
 #pragma omp parallel for schedule(dynamic, 16)
         for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
             Vec<D> x;
@@ -487,10 +485,22 @@ void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, co
                     Vec<D> y;
                     for (int k = 0; k < D; k++) y.v[k] = vpl_p[(size_t)(t0 + j) * D + k];
                     const float mu = vpl_mu[t0 + j];
-                    const float u = K.G(y, x) * area;
-                    const Vec<D> g = K.dG_dx(y, x);
+                    // u = G(y, x) A and dG/dx(y, x) A = w (y - x) with one division (the engine's form)
+                    const Vec<D> r = y - x;
+                    float q = 0.0f;
+                    for (int k = 0; k < D; k++) q = q + r.v[k] * r.v[k];
+                    const float nr = std::sqrt(q);
+                    const float mm = fmax_ref(nr, eps);
+                    float u, w;
+                    if (D == 2) {
+                        u = (-0x1.45f306p-3f * log_own(mm)) * area;
+                        w = nr > 0.0f ? (0x1.45f306p-3f * area) / (nr * mm) : 0.0f;
+                    } else {
+                        u = (1.0f / (0x1.921fb6p+3f * mm)) * area;
+                        w = nr > 0.0f ? (0x1.45f306p-4f * area) / (nr * fmax_ref(q, eps)) : 0.0f;
+                    }
                     part[0] = part[0] + mu * u;
-                    for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (g.v[k] * area);
+                    for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (w * (y.v[k] - x.v[k]));
                 }
                 for (int c = 0; c <= D; c++) split[t % 8][c] += (double)part[c];
             }

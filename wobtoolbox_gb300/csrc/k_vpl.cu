@@ -40,6 +40,27 @@ __global__ void __launch_bounds__(kBlock) vpl_paths_kernel(SceneView<D> s, WalkP
     }
 }
 
+// One (point, VPL) pair: u = G(y, x) A and the factor w of dG/dx(y, x) A = w (y - x), from
+// r = y - x, n = |r|, m = max(n, eps) (equation_kernel.cuh:74-79, 115-121):
+//   2D: G = -log(m) / (2 pi),  dG/dx = r / (2 pi n m);   3D: G = 1 / (4 pi m),  dG/dx = r / (4 pi n max(n^2, eps)),
+// the gradient with one division instead of normalising r and dividing by m (the engine's walk
+// kernels evaluate Green<D>::dG_dx literally; the oracle restates this form for the aggregation).
+// w = 0 at n = 0, where the normalised direction is the zero vector.
+template <int D>
+__device__ __forceinline__ void vpl_pair(const V<D> &y, const V<D> &x, float area, float eps, float &u, float &w) {
+    const V<D> r = vsub(y, x);
+    const float q = vsqnorm(r);
+    const float n = sqrtf(q);
+    const float m = fmax_ref(n, eps);
+    if constexpr (D == 2) {
+        u = (-0x1.45f306p-3f * log_own(m)) * area;
+        w = n > 0.0f ? (0x1.45f306p-3f * area) / (n * m) : 0.0f;
+    } else {
+        u = (1.0f / (0x1.921fb6p+3f * m)) * area;
+        w = n > 0.0f ? (0x1.45f306p-4f * area) / (n * fmax_ref(q, eps)) : 0.0f;
+    }
+}
+
 // One block serves 32 points with 8 warps; warp w sums the tiles t = w, w + 8, ... (all lanes read
 // the same VPL at a time: one broadcast load), so 8 threads share a point's pairs and the grid
 // fills the GPU even for a few ten thousand points. The 8 per-warp FP64 partial sums of a point
@@ -59,8 +80,6 @@ __global__ void __launch_bounds__(32 * kVplSplit) vpl_aggregate_kernel(const flo
     V<D> x = vzero<D>();
     if (active)
         for (int k = 0; k < D; k++) x.v[k] = __ldg(pts + (size_t)pt * D + k);
-    Green<D> K;
-    K.eps = eps;
     double acc[D + 1];
     for (int c = 0; c <= D; c++) acc[c] = 0.0;
     const uint32_t n_tiles = (n_vpl + kVplTile - 1) / kVplTile;
@@ -73,10 +92,10 @@ __global__ void __launch_bounds__(32 * kVplSplit) vpl_aggregate_kernel(const flo
             V<D> y;
             for (int k = 0; k < D; k++) y.v[k] = __ldg(vpl_p + (size_t)(t0 + j) * D + k);
             const float mu = __ldg(vpl_mu + t0 + j);
-            const float u = K.G(y, x) * area;
-            const V<D> g = K.dG_dx(y, x);
+            float u, w;
+            vpl_pair<D>(y, x, area, eps, u, w);
             part[0] = part[0] + mu * u;
-            for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (g.v[k] * area);
+            for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (w * (y.v[k] - x.v[k]));
         }
         for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
     }
