@@ -8,7 +8,8 @@
 // same distance the one with the smallest storage index wins, so the result does not depend on
 // the traversal order (the oracle scans all elements in storage order with the same rule).
 //
-// Work decomposition as the walk kernels: a warp runs 32 paths of one point; FP64 sums per point.
+// Work decomposition as the walk kernels (a warp runs the paths of one point, FP64 sums per point),
+// with path regeneration inside a warp (see wos_kernel).
 // A walk stops after kWosMaxSteps jumps at the latest (taking the value at its current closest
 // point); such walks are counted in the scene's error word (kErrWosStepLimit).
 #include "kernels.cuh"
@@ -19,6 +20,7 @@ namespace wobgb {
 namespace {
 
 constexpr uint32_t kStreamWos = 3u;
+constexpr uint32_t kFullMask = 0xffffffffu;
 
 struct Closest {
     float d2;
@@ -100,24 +102,12 @@ __device__ __forceinline__ float closest_value(const SceneView<2> &s, const Clos
     return (q1.w - q1.z) * c.t + q1.z;
 }
 
-// One WoS path from x (apps/simple_wob_and_wos.cu:120-133); returns the estimate, counts jumps.
-__device__ __forceinline__ float wos_path(const SceneView<2> &s, float eps, PathRng &rng, V<2> x, uint32_t &queries) {
-    for (uint32_t step = 0;; step++) {
-        const Closest c = closest_point(s, x);
-        queries++;
-        const float R = sqrtf(c.d2);
-        if (R < eps || c.elem == 0xFFFFFFFFu) return c.elem == 0xFFFFFFFFu ? 0.0f : closest_value(s, c);
-        if (step + 1 >= kWosMaxSteps) {
-            atomicOr(s.err, kErrWosStepLimit);
-            return closest_value(s, c);
-        }
-        float sn, cs;
-        sincospi_own(2.0f * rng.uniform(), &sn, &cs);
-        x.v[0] = x.v[0] + R * cs;
-        x.v[1] = x.v[1] + R * sn;
-    }
-}
-
+// A warp runs the 32 * ppt paths of one unit (one point) with path regeneration: when a lane's walk
+// ends, the lane takes the next path of the unit, so walks of different lengths do not leave lanes
+// idle until the longest one finishes. A path (apps/simple_wob_and_wos.cu:120-133) is its own
+// Philox stream: query the closest point, stop below eps (or after kWosMaxSteps jumps) with the
+// boundary value there, else jump by the distance in direction 2 pi u; the values do not depend on
+// which lane runs a path.
 __global__ void __launch_bounds__(kBlock) wos_kernel(SceneView<2> s, WalkParams p, const float *__restrict__ pts,
                                                      uint32_t n_points, double *__restrict__ sum,
                                                      double *__restrict__ sumsq, unsigned long long *__restrict__ queries,
@@ -125,29 +115,71 @@ __global__ void __launch_bounds__(kBlock) wos_kernel(SceneView<2> s, WalkParams 
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t slabs = (p.n_paths + 31u) / 32u;
+    const uint32_t span = 32u * p.ppt;
+    const uint32_t slabs = (p.n_paths + span - 1u) / span;
     const uint64_t units = (uint64_t)n_points * slabs;
     unsigned long long my_q = 0;
     for (uint64_t u = warp; u < units; u += n_warps) {
         const uint32_t pt = (uint32_t)(u / slabs);
-        const uint32_t path = (uint32_t)(u % slabs) * 32u + lane;
-        const bool active = path < p.n_paths;
-        float out = 0.0f;
-        if (active) {
-            V<2> x;
-            x.v[0] = __ldg(pts + 2 * (size_t)pt);
-            x.v[1] = __ldg(pts + 2 * (size_t)pt + 1);
-            PathRng rng(p.seed, kStreamWos, p.point_offset + pt, p.path_offset + path);
-            uint32_t q = 0;
-            out = wos_path(s, p.eps, rng, x, q);
-            my_q += q;
-            if (per_path) per_path[(size_t)pt * p.n_paths + path] = out;
+        const uint32_t first = (uint32_t)(u % slabs) * span;
+        const uint32_t end = min(first + span, p.n_paths);
+        V<2> x0;
+        x0.v[0] = __ldg(pts + 2 * (size_t)pt);
+        x0.v[1] = __ldg(pts + 2 * (size_t)pt + 1);
+        uint32_t path = first + lane;
+        uint32_t next = first + 32u;
+        bool active = path < end;
+        PathRng rng(p.seed, kStreamWos, p.point_offset + pt, p.path_offset + path);
+        V<2> x = x0;
+        uint32_t step = 0;
+        double acc = 0.0, acc2 = 0.0;
+        while (__any_sync(kFullMask, active)) {
+            bool done = false;
+            if (active) {
+                // one step of the path
+                const Closest c = closest_point(s, x);
+                my_q++;
+                const float R = sqrtf(c.d2);
+                float out = 0.0f;
+                if (R < p.eps || c.elem == 0xFFFFFFFFu) {
+                    out = c.elem == 0xFFFFFFFFu ? 0.0f : closest_value(s, c);
+                    done = true;
+                } else if (step + 1 >= kWosMaxSteps) {
+                    atomicOr(s.err, kErrWosStepLimit);
+                    out = closest_value(s, c);
+                    done = true;
+                } else {
+                    float sn, cs;
+                    sincospi_own(2.0f * rng.uniform(), &sn, &cs);
+                    x.v[0] = x.v[0] + R * cs;
+                    x.v[1] = x.v[1] + R * sn;
+                    step++;
+                }
+                if (done) {
+                    const double v = (double)out;
+                    acc += v;
+                    acc2 += v * v;
+                    if (per_path) per_path[(size_t)pt * p.n_paths + path] = out;
+                }
+            }
+            const uint32_t fin = __ballot_sync(kFullMask, done);
+            if (fin) {
+                if (done) {
+                    path = next + __popc(fin & ((1u << lane) - 1u));
+                    active = path < end;
+                    if (active) {
+                        rng = PathRng(p.seed, kStreamWos, p.point_offset + pt, p.path_offset + path);
+                        x = x0;
+                        step = 0;
+                    }
+                }
+                next += __popc(fin);
+            }
         }
         if (sum) {
             __syncwarp();
-            const double v = active ? (double)out : 0.0;
-            const double sv = warp_sum(v);
-            const double qv = warp_sum(v * v);
+            const double sv = warp_sum(acc);
+            const double qv = warp_sum(acc2);
             if (lane == 0) {
                 atomicAdd(sum + pt, sv);
                 if (sumsq) atomicAdd(sumsq + pt, qv);
@@ -179,9 +211,11 @@ __global__ void closest_point_kernel(SceneView<2> s, const float *__restrict__ p
 cudaError_t launch_wos_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points, double *sum,
                           double *sumsq, unsigned long long *queries, float *per_path, cudaStream_t st) {
     if (n_points == 0) return cudaSuccess;
-    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 31u) / 32u);
+    WalkParams q = p;
+    q.ppt = choose_ppt(n_points, p.n_paths);
+    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * q.ppt - 1u) / (32u * q.ppt));
     auto k = wos_kernel;
-    k<<<persistent_grid(k, units), kBlock, 0, st>>>(s, p, pts, n_points, sum, sumsq, queries, per_path);
+    k<<<persistent_grid(k, units), kBlock, 0, st>>>(s, q, pts, n_points, sum, sumsq, queries, per_path);
     return cudaGetLastError();
 }
 
