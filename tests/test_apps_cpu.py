@@ -88,3 +88,36 @@ def test_bad_config_reports_error(tmp_path):
         f.write('{"input_obj_file": "x.obj", ')
     r = A.run_app("general_2d", cfg, "--setup-only")
     assert r.returncode == 1 and "JSON" in r.stderr
+
+
+@pytest.mark.parametrize("all_points", [False, True])
+def test_simple_wob_and_wos_setup(tmp_path, all_points):
+    """apps/simple_wob_and_wos.cu up to the solve: the OBJ outline, the winding-number mask (or every
+    grid point with evaluate_at_all_points) and the printed configuration."""
+    obj = str(tmp_path / "star.obj")
+    pts = A.write_star_obj(obj)
+    out = str(tmp_path / "out")
+    cfg = str(tmp_path / "cfg.json")
+    A.write_config(cfg, obj, out, grid_res=40, is_wos=True, evaluate_at_all_points=all_points, eps=1e-4)
+    r = A.run_app("simple_wob_and_wos", cfg, "--setup-only")
+    assert r.returncode == 0, r.stderr
+    assert "( #line segments: 200 )" in r.stdout and "is WoS\t: 1" in r.stdout
+    assert "path length" not in r.stdout  # not used by walk on spheres
+    segs = np.stack([pts, np.roll(pts, -1, axis=0)], axis=1)
+    grid = W.idx_to_domain_point(40, 1.0, 2)
+    m = 1600 if all_points else int((W.winding_number_2d(segs, grid) < -0.5).sum())
+    assert f"evaluation points\t: {m}\n" in r.stdout
+    assert os.path.exists(os.path.join(out, "config.json"))
+
+
+def test_new_apps_reject_bad_configs(tmp_path):
+    cfg = str(tmp_path / "cfg.json")
+    with open(cfg, "w") as f:
+        f.write('{"input_obj_file": "x.obj", "output_dir": "o", "is_wos": 1}')
+    r = A.run_app("simple_wob_and_wos", cfg, "--setup-only")
+    assert r.returncode == 1 and "true or false" in r.stderr
+    with open(cfg, "w") as f:
+        f.write('{"output_dir": "o", "path_length": 4}')
+    for app in ("poisson_equation", "boundary_estimate"):
+        r = A.run_app(app, cfg)
+        assert r.returncode == 1 and "missing key" in r.stderr

@@ -130,3 +130,147 @@ def test_potential_flow_vpl_matches_api(engine, cuda, tmp_path):
     ref = (s / 4000).cpu().numpy().astype(np.float32)
     assert np.array_equal(u[keep], ref[:, 0]) and np.array_equal(g[keep], ref[:, 1:])
     scene.close()
+
+
+def test_poisson_equation_matches_api(engine, cuda, tmp_path):
+    """apps/poisson_equation.cu: the box with u = 1 and the constant source 5 through a volume cache;
+    the app's fields equal the API's solve, and the centre value matches the series solution of
+    Laplace(u) = 5 (the sign the estimator's volume term carries) on (-1, 1)^2."""
+    import json
+    out = str(tmp_path / "out")
+    cfg = str(tmp_path / "cfg.json")
+    with open(cfg, "w") as f:
+        json.dump({"output_dir": out, "path_length": 4, "num_sample_paths": 256, "num_volume_samples": 4,
+                   "grid_res": 32, "eps": 1e-4, "max_time": 1, "max_iterations": 2}, f)
+    r = A.run_app("poisson_equation", cfg)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n, u = A.read_field(os.path.join(out, "potential2.scalar"))
+    _, g = A.read_field(os.path.join(out, "gradient2.vector2"), 2)
+    assert n == 32 and np.all(np.isfinite(u)) and np.all(np.isfinite(g))
+    sq = np.array([[[-1, -1], [-1, 1]], [[-1, 1], [1, 1]], [[1, 1], [1, -1]], [[1, -1], [-1, -1]]], np.float32)
+    nrm = np.array([[-1, 0], [0, 1], [1, 0], [0, -1]], np.float32)
+    scene = engine.SceneHost(sq, nrm, np.ones((4, 2), np.float32), np.zeros(4, np.int32))
+    scene.set_volume_cache(32, 2.0, np.full(32 * 32, 5.0, np.float32))
+    grid = W.idx_to_domain_point(32, 2.0, 2)
+    p = engine.EstimatorParams(bie_model=1, path_length=4, num_sample_paths=512, num_volume_samples=4, eps=1e-4,
+                               seed=0)
+    s, _, _ = scene.solve_domain_host(p, grid)
+    assert np.allclose(u, s[:, 0] / 512, rtol=1e-4, atol=1e-5)
+    assert np.allclose(g, s[:, 1:] / 512, rtol=1e-4, atol=1e-4)
+    # u(0) = 1 - 5 * 0.294685 (torsion function of the square of side 2 at its centre)
+    N = 1 << 20
+    p = engine.EstimatorParams(bie_model=1, path_length=4, num_sample_paths=N, num_volume_samples=16, eps=1e-4,
+                               seed=1)
+    s, q, _ = scene.solve_domain_host(p, np.zeros((1, 2), np.float32))
+    m = s[0, 0] / N
+    se = np.sqrt((q[0, 0] / N - m * m) / N)
+    assert abs(m - (1.0 - 5.0 * 0.294685)) < 5 * se + 0.01, (m, se)
+    scene.close()
+
+
+def _circle720():
+    """The 720-segment circle of apps/boundary_estimate.cu:162-180, vertices in double then float."""
+    import math
+    v = np.array([[0.5 * math.sin((2 * math.pi) * i / 720), 0.5 * math.cos((2 * math.pi) * i / 720)]
+                  for i in range(721)]).astype(np.float32)
+    segs = np.stack([v[:-1], v[1:]], axis=1)
+    t = segs[:, 0] - segs[:, 1]
+    ln = np.sqrt(t[:, 0] * t[:, 0] + t[:, 1] * t[:, 1])
+    n_out = np.stack([t[:, 1] / ln, -(t[:, 0] / ln)], 1).astype(np.float32)
+    bv = np.zeros((720, 2), np.float32)
+    i = np.arange(720)
+    bv[(i % 240 == 0) | (i % 240 == 239)] = [1.0, 200.0]
+    bv[(i % 240 == 120) | (i % 240 == 119)] = [-1.0, -200.0]
+    return segs, n_out, bv
+
+
+def test_boundary_estimate_matches_api(engine, cuda, tmp_path):
+    """apps/boundary_estimate.cu: interior Neumann on the circle, forward single layer; the domain
+    fields and the boundary_solution file equal the API's solves on the same elements and points."""
+    import json
+    torch = cuda
+    out = str(tmp_path / "out")
+    cfg = str(tmp_path / "cfg.json")
+    with open(cfg, "w") as f:
+        json.dump({"output_dir": out, "path_length": 4, "num_sample_paths_domain": 128,
+                   "num_sample_paths_boundary": 512, "grid_res": 32, "max_time": 1, "max_iterations": 2}, f)
+    r = A.run_app("boundary_estimate", cfg)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n, u = A.read_field(os.path.join(out, "potential2.scalar"))
+    _, g = A.read_field(os.path.join(out, "gradient2.vector2"), 2)
+    raw = open(os.path.join(out, "boundary_solution2.scalar"), "rb").read()
+    assert int(np.frombuffer(raw[:4], np.uint32)[0]) == 720
+    ub = np.frombuffer(raw[4:], np.float32)
+    assert ub.size == 720 and np.all(np.isfinite(ub))
+    grid = W.idx_to_domain_point(32, 1.0, 2)
+    inside = np.sqrt(grid[:, 0] * grid[:, 0] + grid[:, 1] * grid[:, 1]) <= np.float32(0.5)
+    assert np.array_equal(~np.isnan(u), inside) and np.all(g[~inside] == 0)
+    segs, n_out, bv = _circle720()
+    scene = engine.SceneHost(segs, -n_out, bv, np.ones(720, np.int32))
+    eps = float(np.finfo(np.float32).eps)
+    p = engine.EstimatorParams(bie_model=0, estimator=1, problem=1, path_length=4, num_sample_paths=256, eps=eps,
+                               seed=0)
+    s, _, _ = scene.solve_domain_host(p, grid[inside])
+    assert np.allclose(u[inside], s[:, 0] / 256, rtol=1e-4, atol=1e-4)
+    assert np.allclose(g[inside], s[:, 1:] / 256, rtol=1e-4, atol=1e-3)
+    mid = ((segs[:, 0] + segs[:, 1]) / np.float32(2.0)).astype(np.float32)
+    t = lambda a, dt=torch.float32: torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dt)
+    sb = torch.zeros(720, dtype=torch.float64, device="cuda")
+    p = engine.EstimatorParams(bie_model=0, estimator=1, problem=1, path_length=4, num_sample_paths=1024, eps=eps,
+                               seed=0)
+    scene.solve_boundary(p, t(mid), t(n_out), t(np.full(720, 0.5)), t(np.zeros(720)), t(np.ones(720), torch.int32),
+                         t(np.zeros(720)), 720, sb)
+    torch.cuda.synchronize()
+    assert np.allclose(ub, sb.cpu().numpy() / 1024, rtol=1e-4, atol=1e-4)
+    scene.close()
+
+
+def _alternating_outline(pts):
+    """Segments of a closed outline with the data of apps/simple_wob_and_wos.cu:201-220: -1 / 1 on
+    alternate pieces of 1/40 of the length, computed in float like the app."""
+    segs = np.stack([pts, np.roll(pts, -1, axis=0)], axis=1).astype(np.float32)
+    d = segs[:, 0] - segs[:, 1]
+    ln = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]).astype(np.float32)
+    total = np.float32(0.0)
+    for x in ln:
+        total = np.float32(total + x)
+    acc = np.float32(0.0)
+    bv = np.zeros((len(segs), 2), np.float32)
+    for i, x in enumerate(ln):
+        sid = int(np.float32(np.float32(acc * np.float32(40.0)) / total))
+        bv[i] = 1.0 if sid % 2 == 1 else -1.0
+        acc = np.float32(acc + x)
+    return segs, W.segment_normals(segs), bv
+
+
+@pytest.mark.parametrize("is_wos", [False, True])
+def test_simple_wob_and_wos_matches_api(engine, cuda, tmp_path, is_wos):
+    """apps/simple_wob_and_wos.cu: the double-layer walk or walk on spheres on an outline with
+    alternating data; the app's field equals the API's solve on the same elements and points."""
+    torch = cuda
+    obj = str(tmp_path / "star.obj")
+    pts = A.write_star_obj(obj)
+    out = str(tmp_path / "out")
+    cfg = str(tmp_path / "cfg.json")
+    A.write_config(cfg, obj, out, grid_res=32, num_sample_paths=128, max_iterations=2, is_wos=is_wos, eps=1e-4)
+    r = A.run_app("simple_wob_and_wos", cfg)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n, u = A.read_field(os.path.join(out, "potential2.scalar"))
+    segs, nrm, bv = _alternating_outline(pts)
+    grid = W.idx_to_domain_point(32, 1.0, 2)
+    inside = W.winding_number_2d(segs, grid) < -0.5
+    assert n == 32 and np.array_equal(~np.isnan(u), inside)
+    assert set(np.unique(bv[:, 0])) == {-1.0, 1.0}
+    scene = engine.SceneHost(segs, nrm, bv, np.zeros(len(segs), np.int32))
+    if is_wos:
+        p = engine.EstimatorParams(num_sample_paths=256, eps=1e-4, seed=0)
+        s = torch.zeros(int(inside.sum()), dtype=torch.float64, device="cuda")
+        scene.solve_wos(p, torch.from_numpy(np.ascontiguousarray(grid[inside])).cuda(), int(inside.sum()), s)
+        torch.cuda.synchronize()
+        ref = s.cpu().numpy() / 256
+    else:
+        p = engine.EstimatorParams(bie_model=1, path_length=4, num_sample_paths=256, eps=1e-4, seed=0)
+        s, _, _ = scene.solve_domain_host(p, grid[inside])
+        ref = s[:, 0] / 256
+    assert np.allclose(u[inside], ref, rtol=1e-4, atol=1e-5)
+    scene.close()

@@ -41,6 +41,10 @@ struct Json {
         if (kind != String) throw std::runtime_error("config: expected a string");
         return str;
     }
+    bool boolean() const {
+        if (kind != Bool) throw std::runtime_error("config: expected true or false");
+        return b;
+    }
 };
 
 class JsonParser {

@@ -8,9 +8,8 @@
 //
 //   potential_flow_vpl <config.json>
 #include "../../include/wob_gb300.hpp"
+#include "app_cuda.hpp"
 #include "app_io.hpp"
-
-#include <cuda_runtime.h>
 
 #include <chrono>
 #include <cmath>
@@ -28,17 +27,8 @@ struct Circle {
     unsigned segments;
 };
 
-void cuda_check(cudaError_t e, const char *what) {
-    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <class T> struct DeviceArray {
-    T *p = nullptr;
-    explicit DeviceArray(size_t n) { cuda_check(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc"); }
-    ~DeviceArray() {
-        if (p) cudaFree(p);
-    }
-};
+using wobapp::cuda_check;
+using wobapp::DeviceArray;
 
 }  // namespace
 

@@ -36,7 +36,15 @@ def nvcc_path() -> str:
 
 
 APPS = os.path.join(HERE, "apps")
-APP_BINARIES = {"general_2d": 2, "general_3d": 3, "potential_flow_vpl": 2}
+# app -> (source under apps/, WOB_APP_DIM, links the CUDA runtime for device buffers)
+APP_BINARIES = {
+    "general_2d": ("general.cpp", 2, False),
+    "general_3d": ("general.cpp", 3, False),
+    "potential_flow_vpl": ("potential_flow_vpl.cpp", 2, True),
+    "poisson_equation": ("poisson_equation.cpp", 2, False),
+    "boundary_estimate": ("boundary_estimate.cpp", 2, True),
+    "simple_wob_and_wos": ("simple_wob_and_wos.cpp", 2, True),
+}
 
 
 def app_path(name: str) -> str:
@@ -51,18 +59,17 @@ def _deps() -> list[str]:
 
 
 def build_apps(force: bool = False) -> list[str]:
-    """The JSON apps (apps/general.cpp for dim 2 and 3), linked against the library."""
+    """The JSON apps (apps/*.cpp, one executable per reference app), linked against the library."""
     cxx = os.environ.get("CXX", "g++")
     deps = [os.path.join(APPS, f) for f in os.listdir(APPS)] + [os.path.join(INCLUDE, "wob_gb300.hpp"),
                                                                  os.path.join(INCLUDE, "wob_capi.h"), LIB]
     jobs, outs = [], []
     cuda = os.path.dirname(os.path.dirname(nvcc_path()))
-    for name, dim in APP_BINARIES.items():
+    for name, (src, dim, cudart) in APP_BINARIES.items():
         out = app_path(name)
         outs.append(out)
-        src = "potential_flow_vpl.cpp" if name == "potential_flow_vpl" else "general.cpp"
         extra = ["-I", os.path.join(cuda, "include"), "-L", os.path.join(cuda, "lib64"), "-lcudart",
-                 "-Wl,-rpath," + os.path.join(cuda, "lib64")] if name == "potential_flow_vpl" else []
+                 "-Wl,-rpath," + os.path.join(cuda, "lib64")] if cudart else []
         if force or _stale(out, deps):
             jobs.append([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall", f"-DWOB_APP_DIM={dim}",
                          "-I", INCLUDE, os.path.join(APPS, src), "-o", out + ".tmp", "-L", OUT,
