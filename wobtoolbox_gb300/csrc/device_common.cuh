@@ -173,9 +173,9 @@ template <int D> __device__ __forceinline__ BPoint<D> bp_zero() {
 // Scene view (device pointers; filled by the host, passed by value to kernels).
 // ------------------------------------------------------------------------------------------
 template <int D> struct SceneView {
-    const float4 *__restrict__ elems;   // D==2: 3 float4 / element, D==3: 5 float4
-    const float4 *__restrict__ isect;   // D==3: 3 float4 / element (a, a-b, a-c, (a-b)x(a-c))
-    const float4 *__restrict__ nodes;   // D==2: 5 float4 / node, D==3: 7 float4
+    const float4 *__restrict__ elems;  // D==2: 4 float4 / element, D==3: 6 (the last one padding)
+    const float4 *__restrict__ isect;  // D==3: 4 float4 / element (a, a-b, a-c, (a-b)x(a-c), padding)
+    const float4 *__restrict__ nodes;  // D==2: 6 float4 / node, D==3: 8 (the last one padding)
     const float *__restrict__ area_cdf;
     const uint4 *__restrict__ area_guide;
     const float *__restrict__ bv_cdf;
@@ -198,9 +198,25 @@ template <int D> struct Elem {
     int type;
 };
 
+// 32-byte read-only load (ld.global.nc.v8.f32, sm_100 and later); p must be 32-byte aligned. A
+// random gather costs about the same per load instruction for 16 and 32 bytes, so the records are
+// laid out for as few 32-byte loads as possible.
+struct F8 {
+    float4 a, b;
+};
+__device__ __forceinline__ F8 ldg8(const float4 *p) {
+    F8 r;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z), "=f"(r.b.w)
+        : "l"(p));
+    return r;
+}
+
 template <int D> __device__ __forceinline__ Elem<D> load_elem(const SceneView<D> &s, uint32_t i);
 template <> __device__ __forceinline__ Elem<2> load_elem<2>(const SceneView<2> &s, uint32_t i) {
-    const float4 q0 = __ldg(s.elems + 3 * i), q1 = __ldg(s.elems + 3 * i + 1), q2 = __ldg(s.elems + 3 * i + 2);
+    const float4 *p = s.elems + 4 * i;
+    const F8 r = ldg8(p);
+    const float4 q0 = r.a, q1 = r.b, q2 = __ldg(p + 2);
     Elem<2> e;
     e.v[0].v[0] = q0.x; e.v[0].v[1] = q0.y; e.v[1].v[0] = q0.z; e.v[1].v[1] = q0.w;
     e.n.v[0] = q1.x; e.n.v[1] = q1.y; e.bv[0] = q1.z; e.bv[1] = q1.w;
@@ -208,16 +224,16 @@ template <> __device__ __forceinline__ Elem<2> load_elem<2>(const SceneView<2> &
     return e;
 }
 template <> __device__ __forceinline__ Elem<3> load_elem<3>(const SceneView<3> &s, uint32_t i) {
-    const float4 *p = s.elems + 5 * i;
-    const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4);
+    const float4 *p = s.elems + 6 * i;
+    const F8 r0 = ldg8(p), r1 = ldg8(p + 2);
+    const float4 q0 = r0.a, q1 = r0.b, q2 = r1.a, q3 = r1.b, q4 = __ldg(p + 4);
     Elem<3> e;
     e.v[0].v[0] = q0.x; e.v[0].v[1] = q0.y; e.v[0].v[2] = q0.z;
     e.v[1].v[0] = q0.w; e.v[1].v[1] = q1.x; e.v[1].v[2] = q1.y;
     e.v[2].v[0] = q1.z; e.v[2].v[1] = q1.w; e.v[2].v[2] = q2.x;
     e.n.v[0] = q2.y; e.n.v[1] = q2.z; e.n.v[2] = q2.w;
-    e.bv[0] = q3.x; e.bv[1] = q3.y; e.bv[2] = q3.z;
-    e.alpha[0] = q3.w; e.alpha[1] = q4.x; e.alpha[2] = q4.y;
-    e.area = q4.z; e.type = __float_as_int(q4.w);
+    e.bv[0] = q3.x; e.bv[1] = q3.y; e.bv[2] = q3.z; e.type = __float_as_int(q3.w);
+    e.alpha[0] = q4.x; e.alpha[1] = q4.y; e.alpha[2] = q4.z; e.area = q4.w;
     return e;
 }
 
@@ -308,19 +324,21 @@ __device__ __forceinline__ bool isect_tri(const V<3> &o, const V<3> &d, const fl
 
 template <int D> __device__ __forceinline__ bool isect_elem(const SceneView<D> &s, uint32_t i, const V<D> &o, const V<D> &d, float &t);
 template <> __device__ __forceinline__ bool isect_elem<2>(const SceneView<2> &s, uint32_t i, const V<2> &o, const V<2> &d, float &t) {
-    const float4 q0 = __ldg(s.elems + 3 * i);
+    const float4 q0 = __ldg(s.elems + 4 * i);
     return isect_seg(o, d, q0.x, q0.y, q0.z, q0.w, t);
 }
 template <> __device__ __forceinline__ bool isect_elem<3>(const SceneView<3> &s, uint32_t i, const V<3> &o, const V<3> &d, float &t) {
-    const float4 *p = s.isect + 3 * i;
-    return isect_tri(o, d, __ldg(p), __ldg(p + 1), __ldg(p + 2), t);
+    const float4 *p = s.isect + 4 * i;
+    const F8 r = ldg8(p);
+    return isect_tri(o, d, r.a, r.b, __ldg(p + 2), t);
 }
 
 // Conservative line / box tests against the 4 children of a node; bit k of the result is set
 // when child k's (padded) box meets the infinite line.
 __device__ __forceinline__ uint32_t node_hits(const SceneView<2> &s, uint32_t node, const V<2> &o, const V<2> &d, float c0, uint4 &child) {
-    const float4 *p = s.nodes + 5 * node;
-    const float4 lx = __ldg(p), ly = __ldg(p + 1), hx = __ldg(p + 2), hy = __ldg(p + 3);
+    const float4 *p = s.nodes + 6 * node;
+    const F8 r0 = ldg8(p), r1 = ldg8(p + 2);
+    const float4 lx = r0.a, ly = r0.b, hx = r1.a, hy = r1.b;
     const float4 cf = __ldg(p + 4);
     child = make_uint4(__float_as_uint(cf.x), __float_as_uint(cf.y), __float_as_uint(cf.z), __float_as_uint(cf.w));
     const float dx = d.v[0], dy = d.v[1];
@@ -340,9 +358,10 @@ __device__ __forceinline__ uint32_t node_hits(const SceneView<2> &s, uint32_t no
 }
 
 __device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t node, const V<3> &o, const V<3> &inv, float, uint4 &child) {
-    const float4 *p = s.nodes + 7 * node;
-    const float4 lx = __ldg(p), ly = __ldg(p + 1), lz = __ldg(p + 2);
-    const float4 hx = __ldg(p + 3), hy = __ldg(p + 4), hz = __ldg(p + 5);
+    const float4 *p = s.nodes + 8 * node;
+    const F8 r0 = ldg8(p), r1 = ldg8(p + 2), r2 = ldg8(p + 4);
+    const float4 lx = r0.a, ly = r0.b, lz = r1.a;
+    const float4 hx = r1.b, hy = r2.a, hz = r2.b;
     const float4 cf = __ldg(p + 6);
     child = make_uint4(__float_as_uint(cf.x), __float_as_uint(cf.y), __float_as_uint(cf.z), __float_as_uint(cf.w));
     const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, lys[4] = {ly.x, ly.y, ly.z, ly.w}, lzs[4] = {lz.x, lz.y, lz.z, lz.w};

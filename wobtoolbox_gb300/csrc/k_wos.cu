@@ -30,7 +30,7 @@ struct Closest {
 
 // squared distance from p to segment i and the clamped parameter (apps/simple_wob_and_wos.cu:54-60)
 __device__ __forceinline__ float seg_dist2(const SceneView<2> &s, uint32_t i, const V<2> &p, float &t_out) {
-    const float4 q0 = __ldg(s.elems + 3 * i);
+    const float4 q0 = __ldg(s.elems + 4 * i);
     const float ax = q0.x, ay = q0.y;
     const float lx = q0.z - ax, ly = q0.w - ay;
     float t = ((p.v[0] - ax) * lx + (p.v[1] - ay) * ly) / (lx * lx + ly * ly);
@@ -67,8 +67,9 @@ __device__ __forceinline__ Closest closest_point(const SceneView<2> &s, const V<
             }
             continue;
         }
-        const float4 *q = s.nodes + 5 * code;
-        const float4 lx = __ldg(q), ly = __ldg(q + 1), hx = __ldg(q + 2), hy = __ldg(q + 3), cf = __ldg(q + 4);
+        const float4 *q = s.nodes + 6 * code;
+        const F8 r0 = ldg8(q), r1 = ldg8(q + 2);
+        const float4 lx = r0.a, ly = r0.b, hx = r1.a, hy = r1.b, cf = __ldg(q + 4);
         const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, lys[4] = {ly.x, ly.y, ly.z, ly.w};
         const float hxs[4] = {hx.x, hx.y, hx.z, hx.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
         const uint32_t cs[4] = {__float_as_uint(cf.x), __float_as_uint(cf.y), __float_as_uint(cf.z),
@@ -98,7 +99,7 @@ __device__ __forceinline__ Closest closest_point(const SceneView<2> &s, const V<
 
 // boundary value at the closest point: (g_b - g_a) t + g_a (apps/simple_wob_and_wos.cu:70-73)
 __device__ __forceinline__ float closest_value(const SceneView<2> &s, const Closest &c) {
-    const float4 q1 = __ldg(s.elems + 3 * c.elem + 1);
+    const float4 q1 = __ldg(s.elems + 4 * c.elem + 1);
     return (q1.w - q1.z) * c.t + q1.z;
 }
 

@@ -293,9 +293,8 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
             const float area = area3(v, v + 3, v + 6);
             for (int k = 0; k < 9; k++) r[k] = v[k];
             r[9] = nn[0]; r[10] = nn[1]; r[11] = nn[2];
-            r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2];
-            r[15] = al[0]; r[16] = al[1]; r[17] = al[2];
-            r[18] = area; r[19] = u2f((uint32_t)types[i]);
+            r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2]; r[15] = u2f((uint32_t)types[i]);
+            r[16] = al[0]; r[17] = al[1]; r[18] = al[2]; r[19] = area;
             areas[s] = area;
             bvw[s] = area * (std::fabs(bv[0]) + std::fabs(bv[1]) + std::fabs(bv[2])) / 3.0f;
             // intersection record: a, e1 = a - b, e2 = a - c, q = e1 x e2

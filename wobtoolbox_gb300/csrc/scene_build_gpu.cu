@@ -310,7 +310,7 @@ __global__ void k_collapse_write(uint32_t cnt, const uint32_t *__restrict__ fw, 
                                  uint32_t *nw, uint32_t *nb) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cnt) return;
-    constexpr int NF = D == 2 ? 20 : 28;
+    constexpr int NF = D == 2 ? 24 : 32;
     float *r = nodes + (size_t)fw[t] * NF;
     uint32_t ch[4];
     const int m = wide_children(fb[t], child, first, last, ch);
@@ -346,6 +346,7 @@ __global__ void k_collapse_write(uint32_t cnt, const uint32_t *__restrict__ fw, 
             r[4 * (D + a) + k] = hi[a];
         }
         r[4 * (2 * D) + k] = __uint_as_float(code);
+        r[4 * (2 * D + 1) + k] = 0.0f;  // padding to a 32-byte multiple
     }
 }
 
@@ -365,16 +366,17 @@ __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const fl
     if (alphas)
         for (int k = 0; k < D; k++) al[k] = alphas[(size_t)i * D + k];
     if constexpr (D == 2) {
-        float *r = elems + (size_t)s * 12;
+        float *r = elems + (size_t)s * 16;
         const float dx = v[2] - v[0], dy = v[3] - v[1];
         const float area = sqrtf(dx * dx + dy * dy);
         r[0] = v[0]; r[1] = v[1]; r[2] = v[2]; r[3] = v[3];
         r[4] = nn[0]; r[5] = nn[1]; r[6] = bv[0]; r[7] = bv[1];
         r[8] = al[0]; r[9] = al[1]; r[10] = area; r[11] = __int_as_float(types[i]);
+        r[12] = 0.0f; r[13] = 0.0f; r[14] = 0.0f; r[15] = 0.0f;
         areas[s] = area;
         bvw[s] = area * (fabsf(bv[0]) + fabsf(bv[1])) / 2.0f;
     } else {
-        float *r = elems + (size_t)s * 20;
+        float *r = elems + (size_t)s * 24;
         const float u0 = v[6] - v[0], u1 = v[7] - v[1], u2 = v[8] - v[2];
         const float w0 = v[3] - v[0], w1 = v[4] - v[1], w2 = v[5] - v[2];
         const float x = u1 * w2 - u2 * w1;
@@ -383,12 +385,12 @@ __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const fl
         const float area = sqrtf(x * x + y * y + z * z) / 2.0f;
         for (int k = 0; k < 9; k++) r[k] = v[k];
         r[9] = nn[0]; r[10] = nn[1]; r[11] = nn[2];
-        r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2];
-        r[15] = al[0]; r[16] = al[1]; r[17] = al[2];
-        r[18] = area; r[19] = __int_as_float(types[i]);
+        r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2]; r[15] = __int_as_float(types[i]);
+        r[16] = al[0]; r[17] = al[1]; r[18] = al[2]; r[19] = area;
+        r[20] = 0.0f; r[21] = 0.0f; r[22] = 0.0f; r[23] = 0.0f;
         areas[s] = area;
         bvw[s] = area * (fabsf(bv[0]) + fabsf(bv[1]) + fabsf(bv[2])) / 3.0f;
-        float *q = isect + (size_t)s * 12;
+        float *q = isect + (size_t)s * 16;
         const float e1x = v[0] - v[3], e1y = v[1] - v[4], e1z = v[2] - v[5];
         const float e2x = v[0] - v[6], e2y = v[1] - v[7], e2z = v[2] - v[8];
         q[0] = v[0]; q[1] = v[1]; q[2] = v[2];
@@ -397,6 +399,7 @@ __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const fl
         q[9] = e1y * e2z - e1z * e2y;
         q[10] = e1z * e2x - e1x * e2z;
         q[11] = e1x * e2y - e1y * e2x;
+        q[12] = 0.0f; q[13] = 0.0f; q[14] = 0.0f; q[15] = 0.0f;
     }
 }
 
@@ -514,7 +517,7 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
         for (uint32_t j = k >> 1; j > 0; j >>= 1) k_bitonic<<<blocks(n2), kT, 0, st>>>(n2, j, k, key, val);
     WOB_CK(cudaGetLastError());
 
-    constexpr int NF = D == 2 ? 20 : 28;
+    constexpr int NF = D == 2 ? 24 : 32;
     const uint32_t n_int = n > 1 ? n - 1 : 1;
     float *nodes = nullptr;
     WOB_CK(cudaMalloc(&nodes, (size_t)n_int * NF * 4));
@@ -588,15 +591,15 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
     out.depth = depth;
 
     // records, CDFs, guides
-    const int EF = D == 2 ? 12 : 20;
+    const int EF = D == 2 ? 16 : 24;
     float *elems = nullptr, *isect = nullptr, *area_cdf = nullptr, *bv_cdf = nullptr, *areas, *bvw, *totals;
     WOB_CK(cudaMalloc(&elems, (size_t)n * EF * 4));
     out.elems = elems;
     out.elems_bytes = (size_t)n * EF * 4;
     if (D == 3) {
-        WOB_CK(cudaMalloc(&isect, (size_t)n * 12 * 4));
+        WOB_CK(cudaMalloc(&isect, (size_t)n * 16 * 4));
         out.isect = isect;
-        out.isect_bytes = (size_t)n * 12 * 4;
+        out.isect_bytes = (size_t)n * 16 * 4;
     }
     WOB_CK(cudaMalloc(&area_cdf, (size_t)n * 4));
     out.area_cdf = area_cdf;

@@ -27,10 +27,17 @@ inline uint32_t make_leaf(uint32_t first, uint32_t count) {
     return 0x80000000u | ((count - 1u) << 28) | first;
 }
 
-// Packed record sizes in floats.
-inline int elem_record_floats(int dim) { return dim == 2 ? 12 : 20; }
-inline int node_record_floats(int dim) { return dim == 2 ? 20 : 28; }
-constexpr int kIsect3Floats = 12;
+// Packed record sizes in floats. Every record starts on a 32-byte boundary so the kernels read it
+// with 32-byte loads (ld.global.nc.v8.f32); a random gather costs about the same per load
+// instruction whatever its width, so fewer, wider loads per record are faster.
+//   element: 2D a, b, n, bv[2], alpha[2], area, type + 16 B padding (64 B);
+//            3D a, b, c, n, bv[3], type, alpha[3], area + 16 B padding (96 B)
+//   node: 2D lo_x[4] lo_y[4] hi_x[4] hi_y[4] child[4] + 16 B padding (96 B);
+//         3D adds lo_z, hi_z (112 B + 16 B padding)
+//   intersection record (3D): a, a - b, a - c, (a - b) x (a - c) + 16 B padding (64 B)
+inline int elem_record_floats(int dim) { return dim == 2 ? 16 : 24; }
+inline int node_record_floats(int dim) { return dim == 2 ? 24 : 32; }
+constexpr int kIsect3Floats = 16;
 
 struct HostScene {
     int dim = 0;
