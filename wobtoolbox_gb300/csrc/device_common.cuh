@@ -455,6 +455,29 @@ template <int D> __device__ __forceinline__ BPoint<D> uniform_point(const Elem<D
     return r;
 }
 
+// The position alone of the uniform sample on stored element i with draws u (what a resampling
+// candidate's target needs): uniform_point's interpolation, reading only the vertices.
+template <int D> __device__ __forceinline__ V<D> uniform_position(const SceneView<D> &s, uint32_t i, const float *u) {
+    V<D> r;
+    if constexpr (D == 2) {
+        const float4 q0 = __ldg(s.elems + 4 * i);
+        const float u2 = u[1];
+        r.v[0] = interp2(q0.x, q0.z, u2);
+        r.v[1] = interp2(q0.y, q0.w, u2);
+    } else {
+        const float4 *p = s.elems + 6 * i;
+        const F8 q = ldg8(p);
+        const float cz = __ldg(reinterpret_cast<const float *>(p + 2));
+        const float u2 = u[1], u3 = u[2];
+        const float sq = sqrtf(u2);
+        const float k1 = 1.0f - sq, k2 = sq * (1.0f - u3), k3 = u3 * sq;
+        r.v[0] = interp3(q.a.x, q.a.w, q.b.z, k1, k2, k3);
+        r.v[1] = interp3(q.a.y, q.b.x, q.b.w, k1, k2, k3);
+        r.v[2] = interp3(q.a.z, q.b.y, cz, k1, k2, k3);
+    }
+    return r;
+}
+
 template <int D> __device__ __forceinline__ BPoint<D> sample_uniform(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
     float u[D];
 #pragma unroll

@@ -112,22 +112,17 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
 
     // Walker::sample_ris with the reference of the selected candidate.
     __device__ __forceinline__ BPoint<D> sample_ris_ref(const BPoint<D> &yp, float &inv_pdf, PRef &ref) {
-        BPoint<D> y = bp_zero<D>();
-        ref.e = kRefZero;
-        ref.k0 = ref.k1 = ref.k2 = 0.0f;
-        float w_sum = 0.0f;
-        uint32_t M = 0;
-        for (uint32_t i = 0; i < this->p.n_resampling; i++) {
-            float ip;
-            PRef ri;
-            const BPoint<D> xi = sample_uniform_ref<D>(this->s, this->rng, ip, ri);
-            const float wi = this->ris_target(yp.type, yp, xi) * ip;
-            w_sum = w_sum + wi;
-            M += 1;
-            if (this->rng.uniform() <= wi / w_sum) {
-                y = xi;
-                ref = ri;
-            }
+        uint32_t sel, M;
+        float su[D], w_sum;
+        this->ris_select(yp, sel, su, w_sum, M);
+        BPoint<D> y;
+        if (sel != 0xFFFFFFFFu) {
+            y = uniform_point<D>(load_elem<D>(this->s, sel), su);
+            ref = uniform_ref<D>(sel, su);
+        } else {
+            y = bp_zero<D>();
+            ref.e = kRefZero;
+            ref.k0 = ref.k1 = ref.k2 = 0.0f;
         }
         inv_pdf = w_sum / fmax_ref(this->ris_target(yp.type, yp, y) * (float)M, kEps10);
         return y;

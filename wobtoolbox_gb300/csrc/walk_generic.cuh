@@ -305,24 +305,62 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> st
     __device__ __forceinline__ bool direct_neumann() const { return strat() == kStratDirectNeumann; }
     __device__ __forceinline__ bool sl_neumann() const { return strat() == kStratFwdSlNeumann; }
 
-    __device__ __forceinline__ float ris_target(int type, const BPoint<D> &yp, const BPoint<D> &c) const {
-        if (type == kDirichlet) return fabsf(K.G(c.p, yp.p));
-        if (type == kNeumann) return fabsf(K.dG_dny(yp.p, c.p, yp.n));
-        return fabsf(K.dG_dny(yp.p, c.p, yp.n) + yp.alpha * K.G(c.p, yp.p));
+    __device__ __forceinline__ float ris_target_at(int type, const BPoint<D> &yp, const V<D> &c) const {
+        if (type == kDirichlet) return fabsf(K.G(c, yp.p));
+        if (type == kNeumann) return fabsf(K.dG_dny(yp.p, c, yp.n));
+        return fabsf(K.dG_dny(yp.p, c, yp.n) + yp.alpha * K.G(c, yp.p));
     }
-    // Streaming RIS over K uniform candidates (scene.cuh:542-584, 847-889).
-    __device__ __forceinline__ BPoint<D> sample_ris(const BPoint<D> &yp, float &inv_pdf) {
-        BPoint<D> y = bp_zero<D>();
-        float w_sum = 0.0f;
-        uint32_t M = 0;
-        for (uint32_t i = 0; i < p.n_resampling; i++) {
-            float ip;
-            const BPoint<D> xi = sample_uniform<D>(s, rng, ip);
-            const float wi = ris_target(yp.type, yp, xi) * ip;
+    __device__ __forceinline__ float ris_target(int type, const BPoint<D> &yp, const BPoint<D> &c) const {
+        return ris_target_at(type, yp, c.p);
+    }
+    // Streaming RIS over K uniform candidates (scene.cuh:542-584, 847-889). A candidate's target
+    // needs only its position, so the loop reads only the vertices of each candidate's element and
+    // keeps the selected candidate's element (sel, 0xFFFFFFFF if none) and draws (su). The draws
+    // are taken in the reference's order -- candidate i's D draws, then its selection draw -- but
+    // candidate i + 1's draws and guide-table load are issued before candidate i's target is
+    // evaluated, so two dependent load chains are in flight instead of one.
+    __device__ __forceinline__ void ris_select(const BPoint<D> &yp, uint32_t &sel, float *su, float &w_sum,
+                                               uint32_t &M) {
+        sel = 0xFFFFFFFFu;
+#pragma unroll
+        for (int k = 0; k < D; k++) su[k] = 0.0f;
+        w_sum = 0.0f;
+        M = 0;
+        const uint32_t K = p.n_resampling;
+        if (K == 0) return;
+        float u[D];
+#pragma unroll
+        for (int k = 0; k < D; k++) u[k] = rng.uniform();
+        uint4 g = __ldg(s.area_guide + guide_bin(s.area_G, u[0]));
+        for (uint32_t i = 0; i < K; i++) {
+            const uint32_t idx = cdf_resolve(s.area_cdf, g, u[0]);
+            const V<D> pos = uniform_position<D>(s, idx, u);
+            const float r_sel = rng.uniform();
+            float un[D];
+#pragma unroll
+            for (int k = 0; k < D; k++) un[k] = 0.0f;
+            if (i + 1 < K) {
+#pragma unroll
+                for (int k = 0; k < D; k++) un[k] = rng.uniform();
+                g = __ldg(s.area_guide + guide_bin(s.area_G, un[0]));
+            }
+            const float wi = ris_target_at(yp.type, yp, pos) * s.total_area;
             w_sum = w_sum + wi;
             M += 1;
-            if (rng.uniform() <= wi / w_sum) y = xi;
+            if (r_sel <= wi / w_sum) {
+                sel = idx;
+#pragma unroll
+                for (int k = 0; k < D; k++) su[k] = u[k];
+            }
+#pragma unroll
+            for (int k = 0; k < D; k++) u[k] = un[k];
         }
+    }
+    __device__ __forceinline__ BPoint<D> sample_ris(const BPoint<D> &yp, float &inv_pdf) {
+        uint32_t sel, M;
+        float su[D], w_sum;
+        ris_select(yp, sel, su, w_sum, M);
+        const BPoint<D> y = sel != 0xFFFFFFFFu ? uniform_point<D>(load_elem<D>(s, sel), su) : bp_zero<D>();
         inv_pdf = w_sum / fmax_ref(ris_target(yp.type, yp, y) * (float)M, kEps10);
         return y;
     }
