@@ -65,6 +65,7 @@ struct wob_scene_s {
     wobgb::HostScene host;
     DevBuf elems, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
     DevBuf vol_values, vol_cdf, vol_guide;
+    DevBuf lg_bins, lg_off, lg_ent;  // 2D line grid
     DevBuf cv_table;  // control-variate density per stored element
     DevBuf rhs;       // multi-RHS data [n][dim][n_rhs], storage order
     DevBuf rhs_cv;    // multi-RHS control variate [n][n_rhs], storage order
@@ -93,6 +94,11 @@ struct wob_scene_s {
         v.vol_guide = (const uint4 *)vol_guide.ptr;
         v.err = (uint32_t *)err.ptr;
         v.cv_table = (const float *)cv_table.ptr;
+        v.lg_bins = (const float4 *)lg_bins.ptr;
+        v.lg_off = (const uint32_t *)lg_off.ptr;
+        v.lg_ent = (const uint16_t *)lg_ent.ptr;
+        v.lg_K = lg_bins.ptr ? host.line_grid.K : 0u;
+        v.lg_M = host.line_grid.M;
         v.n_elems = host.n;
         v.n_nodes = host.n_nodes;
         v.area_G = area_G;
@@ -108,7 +114,7 @@ struct wob_scene_s {
     }
     void release_all() {
         for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
-                          &vol_cdf, &vol_guide, &cv_table, &rhs, &rhs_cv, &ws})
+                          &vol_cdf, &vol_guide, &cv_table, &rhs, &rhs_cv, &ws, &lg_bins, &lg_off, &lg_ent})
             b->release();
         if (ws_stream) cudaStreamDestroy(ws_stream);
         ws_stream = nullptr;
@@ -285,7 +291,10 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
         (e = upload(s->area_guide, h.area_guide.data(), h.area_guide.size() * 4)) != cudaSuccess ||
         (e = upload(s->bv_cdf, h.bv_cdf.data(), h.bv_cdf.size() * 4)) != cudaSuccess ||
         (e = upload(s->bv_guide, h.bv_guide.data(), h.bv_guide.size() * 4)) != cudaSuccess ||
-        (e = upload(s->err, &zero, 4)) != cudaSuccess) {
+        (e = upload(s->err, &zero, 4)) != cudaSuccess ||
+        (e = upload(s->lg_bins, h.line_grid.bins.data(), h.line_grid.bins.size() * 4)) != cudaSuccess ||
+        (e = upload(s->lg_off, h.line_grid.offsets.data(), h.line_grid.offsets.size() * 4)) != cudaSuccess ||
+        (e = upload(s->lg_ent, h.line_grid.entries.data(), h.line_grid.entries.size() * 2)) != cudaSuccess) {
         s->release_all();
         delete s;
         return fail_cuda(e, "uploading the scene");
@@ -366,7 +375,7 @@ int wob_scene_get_info(wob_scene s, wob_scene_info *info) {
     info->has_volume_cache = s->has_volume ? 1 : 0;
     size_t bytes = 0;
     for (const DevBuf *b : {&s->elems, &s->isect, &s->nodes, &s->area_cdf, &s->area_guide, &s->bv_cdf, &s->bv_guide,
-                            &s->vol_values, &s->vol_cdf, &s->vol_guide})
+                            &s->vol_values, &s->vol_cdf, &s->vol_guide, &s->lg_bins, &s->lg_off, &s->lg_ent})
         bytes += b->bytes;
     info->bytes_on_device = (uint32_t)(bytes > 0xFFFFFFFFu ? 0xFFFFFFFFu : bytes);
     return WOB_OK;

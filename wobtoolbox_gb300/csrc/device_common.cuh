@@ -184,6 +184,10 @@ template <int D> struct SceneView {
     const float *__restrict__ vol_cdf;
     const uint4 *__restrict__ vol_guide;
     const float *__restrict__ cv_table;  // control-variate density per stored element (or null)
+    const float4 *__restrict__ lg_bins;  // 2D line grid (LineGrid, scene_host.hpp): K x {cmin, cmax, inv_w, 0}
+    const uint32_t *__restrict__ lg_off; // K x (M + 1) list starts
+    const uint16_t *__restrict__ lg_ent; // stored element indices
+    uint32_t lg_K, lg_M;                 // lg_K == 0: no line grid
     uint32_t *err;                       // device error word (kErr* bits)
     uint32_t n_elems, n_nodes, area_G, bv_G;
     uint32_t vol_n, vol_G, vol_res, traversal_limit;
@@ -379,12 +383,50 @@ __device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t no
     return mask;
 }
 
+// 2D line query through the line grid: the line's direction bin (diamond angle of the direction
+// taken in the upper half-plane) and offset cell give the candidate segments in storage order,
+// each tested exactly. Returns false (nothing done) when d is not a unit vector within 1e-6, the
+// precondition of the grid's offset bounds; the caller then traverses the BVH.
+__device__ __forceinline__ bool line_grid_query(const SceneView<2> &s, const V<2> &o, const V<2> &d, uint32_t *hits,
+                                                uint32_t &count) {
+    const float q = d.v[0] * d.v[0] + d.v[1] * d.v[1];
+    if (!(fabsf(q - 1.0f) <= 1e-6f)) return false;
+    const bool flip = d.v[1] < 0.0f || (d.v[1] == 0.0f && d.v[0] < 0.0f);
+    const float dx = flip ? -d.v[0] : d.v[0], dy = flip ? -d.v[1] : d.v[1];
+    const float t = dy / (fabsf(dx) + dy);
+    const float pa = dx >= 0.0f ? t : 2.0f - t;
+    uint32_t k = (uint32_t)(pa * (0.5f * (float)s.lg_K));
+    k = k < s.lg_K ? k : s.lg_K - 1;
+    count = 0;
+    const float c = -dy * o.v[0] + dx * o.v[1];
+    const float4 b = __ldg(s.lg_bins + k);
+    if (!(c >= b.x && c <= b.y)) return true;
+    const float f = (c - b.x) * b.z;
+    uint32_t j = f >= (float)s.lg_M ? s.lg_M : (uint32_t)f;
+    j = j < s.lg_M ? j : s.lg_M - 1;
+    const uint32_t *off = s.lg_off + (size_t)k * (s.lg_M + 1) + j;
+    const uint32_t e0 = __ldg(off), e1 = __ldg(off + 1);
+    for (uint32_t e = e0; e < e1; e++) {
+        const uint32_t i = __ldg(s.lg_ent + e);
+        float tt;
+        if (isect_elem<2>(s, i, o, d, tt)) {
+            if (count < kHitBuffer) hits[count] = i;
+            count++;
+        }
+    }
+    return true;
+}
+
 // All hits of the infinite line o + t d, in storage order (depth-first, children in order, so
-// leaves come in increasing element order). Writes the first kHitBuffer element indices to hits
-// and returns the total count. On a stack overflow or runaway traversal it flags s.err and
-// returns what it has.
+// leaves come in increasing element order; or the line grid's cell lists, in storage order).
+// Writes the first kHitBuffer element indices to hits and returns the total count. On a stack
+// overflow or runaway traversal it flags s.err and returns what it has.
 template <int D>
 __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D> &o, const V<D> &d, uint32_t *hits) {
+    if constexpr (D == 2) {
+        uint32_t n_grid;
+        if (s.lg_K != 0u && line_grid_query(s, o, d, hits, n_grid)) return n_grid;
+    }
     uint32_t stack[kStackSize];
     int sp = 0;
     stack[sp++] = 0u;  // root node

@@ -184,6 +184,95 @@ std::string build_volume_cdf(int dim, uint32_t res, const float *values, std::ve
     return "";
 }
 
+namespace {
+
+// Direction angle (radians) of diamond angle pa in [0, 2]: (1 - pa, pa) for pa <= 1, else
+// (1 - pa, 2 - pa).
+double diamond_to_angle(double pa) {
+    return pa <= 1.0 ? std::atan2(pa, 1.0 - pa) : std::atan2(2.0 - pa, 1.0 - pa);
+}
+
+float round_down(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+float round_up(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
+// The cell of offset c in a bin; the device evaluates the same float expression.
+inline uint32_t line_cell(float c, float cmin, float inv_w, uint32_t M) {
+    const float f = (c - cmin) * inv_w;
+    const uint32_t j = f >= (float)M ? M : (uint32_t)f;
+    return j < M ? j : M - 1;
+}
+
+}  // namespace
+
+void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, LineGrid &grid) {
+    grid = LineGrid();
+    if (n == 0 || n > kLineGridMaxElems) return;
+    const uint32_t K = n <= 2048 ? 512u : n <= 8192 ? 256u : 128u;
+    uint32_t M = 64;
+    while (M < n / 2 && M < 4096) M <<= 1;
+    const int EF = elem_record_floats(2);
+    std::vector<float> lo(n), hi(n);
+    std::vector<uint32_t> c0(n), c1(n);
+    grid.K = K;
+    grid.M = M;
+    grid.bins.assign(4 * (size_t)K, 0.0f);
+    grid.offsets.assign((size_t)K * (M + 1), 0u);
+    std::vector<uint32_t> count(M);
+    for (uint32_t k = 0; k < K; k++) {
+        const double f0 = diamond_to_angle(2.0 * k / K), f1 = diamond_to_angle(2.0 * (k + 1) / K);
+        const double nx0 = -std::sin(f0), ny0 = std::cos(f0), nx1 = -std::sin(f1), ny1 = std::cos(f1);
+        const double dphi = f1 - f0;
+        const double bend = dphi * dphi / 8.0 + kLineGridAngleSlack;
+        float cmin = std::numeric_limits<float>::infinity(), cmax = -cmin;
+        for (uint32_t i = 0; i < n; i++) {
+            const float *r = elems.data() + (size_t)i * EF;
+            const double ax = r[0], ay = r[1], bx = r[2], by = r[3];
+            const double ga0 = nx0 * ax + ny0 * ay, ga1 = nx1 * ax + ny1 * ay;
+            const double gb0 = nx0 * bx + ny0 * by, gb1 = nx1 * bx + ny1 * by;
+            const double rad = std::max(std::hypot(ax, ay), std::hypot(bx, by)) * bend + (double)pad;
+            lo[i] = round_down(std::min(std::min(ga0, ga1), std::min(gb0, gb1)) - rad);
+            hi[i] = round_up(std::max(std::max(ga0, ga1), std::max(gb0, gb1)) + rad);
+            cmin = std::min(cmin, lo[i]);
+            cmax = std::max(cmax, hi[i]);
+        }
+        float inv_w = cmax > cmin ? (float)M / (cmax - cmin) : 0.0f;
+        if (!std::isfinite(inv_w)) inv_w = 0.0f;
+        float *b = grid.bins.data() + 4 * (size_t)k;
+        b[0] = cmin;
+        b[1] = cmax;
+        b[2] = inv_w;
+        std::fill(count.begin(), count.end(), 0u);
+        size_t listed = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            c0[i] = line_cell(lo[i], cmin, inv_w, M);
+            c1[i] = line_cell(hi[i], cmin, inv_w, M);
+            listed += c1[i] - c0[i] + 1;
+        }
+        if (grid.entries.size() + listed > kLineGridMaxEntries) {  // long segments: the BVH is the better index
+            grid = LineGrid();
+            return;
+        }
+        for (uint32_t i = 0; i < n; i++)
+            for (uint32_t j = c0[i]; j <= c1[i]; j++) count[j]++;
+        uint32_t *off = grid.offsets.data() + (size_t)k * (M + 1);
+        const uint32_t base = (uint32_t)grid.entries.size();
+        off[0] = base;
+        for (uint32_t j = 0; j < M; j++) off[j + 1] = off[j] + count[j];
+        grid.entries.resize(off[M]);
+        std::vector<uint32_t> fill(off, off + M);
+        for (uint32_t i = 0; i < n; i++)
+            for (uint32_t j = c0[i]; j <= c1[i]; j++) grid.entries[fill[j]++] = (uint16_t)i;
+    }
+}
+
 std::string build_host_scene(int dim, uint32_t n, const float *verts, const float *normals,
                              const float *bvals, const float *alphas, const int32_t *types,
                              HostScene &out) {
@@ -317,6 +406,7 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
     out.bv_valid = out.total_bv > 0.0f && std::isfinite(out.total_bv);
     if (out.bv_valid) out.bv_guide = build_guide(out.bv_cdf);
     else out.bv_guide.assign(4, 0u);
+    if (dim == 2) build_line_grid_2d(out.elems, n, pad, out.line_grid);
     return "";
 }
 

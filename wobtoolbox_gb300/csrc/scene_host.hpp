@@ -39,6 +39,29 @@ inline int elem_record_floats(int dim) { return dim == 2 ? 16 : 24; }
 inline int node_record_floats(int dim) { return dim == 2 ? 24 : 32; }
 constexpr int kIsect3Floats = 16;
 
+// 2D line grid: all segments an infinite line can meet, by direction and offset. The directions
+// (half-turn, diamond angle pa in [0, 2]) are cut into K bins; for bin k and a segment, the offsets
+// c = n . p (n = (-sin phi, cos phi)) its points take over the bin's directions form an interval,
+// widened by the curvature of the sinusoids, an angle slack and the scene's padding; the offsets of
+// bin k, [cmin, cmax], are cut into M cells, and a cell lists, in storage order, every segment whose
+// interval meets it. A line of bin k with offset c can only meet the segments listed in c's cell,
+// so testing those exactly gives the same hits, in the same order, as testing all segments.
+// Cells come from cell(c) = min((int)((c - cmin) * inv_w), M - 1) on host and device alike (a
+// monotone function of c), so a segment is listed in every cell that an offset of its interval
+// can fall in.
+struct LineGrid {
+    uint32_t K = 0, M = 0;             // K == 0: no grid (the BVH answers line queries)
+    std::vector<float> bins;           // K * 4: cmin, cmax, inv_w, 0
+    std::vector<uint32_t> offsets;     // K * (M + 1): start of each cell's list in entries
+    std::vector<uint16_t> entries;     // stored element indices
+};
+constexpr uint32_t kLineGridMaxElems = 16384;   // larger 2D scenes use the BVH alone
+constexpr size_t kLineGridMaxEntries = 1u << 25;  // 64 MB of lists at most
+constexpr double kLineGridAngleSlack = 1e-6;   // rad: rounding of a query's bin and direction
+
+// The line grid of a 2D scene's stored element records (empty if the scene is too large).
+void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, LineGrid &grid);
+
 struct HostScene {
     int dim = 0;
     uint32_t n = 0;
@@ -51,6 +74,7 @@ struct HostScene {
     float total_area = 0.0f, total_bv = 0.0f;
     bool bv_valid = false;                 // |g| sampling defined (total |g| finite and > 0)
     uint32_t n_nodes = 0, depth = 0;
+    LineGrid line_grid;                    // 2D only
 };
 
 // Returns "" on success, else a message. Arrays as documented for wob_scene_create.
