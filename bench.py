@@ -417,7 +417,8 @@ def run_ours(args):
                        "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
                        "rmse_u_vs_exact": rmse, "error_spread": error_spread, "paths_per_point_total": n_paths_total,
                        "parallelism": f"replicas x{world}, points x independent path streams",
-                       "autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]}},
+                       "autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
+                       "line_grid": {"bins": scene.info()["line_grid_bins"], "cells": scene.info()["line_grid_cells"]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if peaks else

@@ -81,6 +81,8 @@ typedef struct wob_scene_info {
     float total_boundary_value;         /* Scene::total_boundary_value (scene.cuh:294) */
     int32_t has_volume_cache;
     uint32_t bytes_on_device;
+    uint32_t line_grid_bins;            /* 2D host-built scenes: direction bins of the line grid (0: none) */
+    uint32_t line_grid_cells;           /* offset cells per direction bin */
 } wob_scene_info;
 
 /* Last error message of the calling thread ("" when none). */

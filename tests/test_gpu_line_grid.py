@@ -106,6 +106,8 @@ def test_line_grid_matches_brute_force(engine, oracle, cuda, name):
     nrm = W.segment_normals(segs)
     bv = np.zeros((len(segs), 2), F32)
     scene = engine.SceneHost(segs, nrm, bv, np.zeros(len(segs), np.int32))
+    info = scene.info()
+    assert info["line_grid_bins"] >= 64 and info["line_grid_cells"] >= 64, info
     o, d = _lines(segs, 7)
     n = len(o)
     counts = torch.zeros(n, dtype=torch.int32, device="cuda")

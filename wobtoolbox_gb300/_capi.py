@@ -59,7 +59,7 @@ class wob_scene_info(C.Structure):
     _fields_ = [
         ("dim", C.c_int32), ("n_elems", C.c_uint32), ("n_nodes", C.c_uint32), ("bvh_depth", C.c_uint32),
         ("total_area", C.c_float), ("total_boundary_value", C.c_float), ("has_volume_cache", C.c_int32),
-        ("bytes_on_device", C.c_uint32),
+        ("bytes_on_device", C.c_uint32), ("line_grid_bins", C.c_uint32), ("line_grid_cells", C.c_uint32),
     ]
 
 

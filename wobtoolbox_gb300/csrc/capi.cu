@@ -378,6 +378,8 @@ int wob_scene_get_info(wob_scene s, wob_scene_info *info) {
                             &s->vol_values, &s->vol_cdf, &s->vol_guide, &s->lg_bins, &s->lg_off, &s->lg_ent})
         bytes += b->bytes;
     info->bytes_on_device = (uint32_t)(bytes > 0xFFFFFFFFu ? 0xFFFFFFFFu : bytes);
+    info->line_grid_bins = s->lg_bins.ptr ? s->host.line_grid.K : 0u;
+    info->line_grid_cells = s->lg_bins.ptr ? s->host.line_grid.M : 0u;
     return WOB_OK;
 }
 

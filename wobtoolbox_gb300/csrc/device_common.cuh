@@ -406,7 +406,30 @@ __device__ __forceinline__ bool line_grid_query(const SceneView<2> &s, const V<2
     j = j < s.lg_M ? j : s.lg_M - 1;
     const uint32_t *off = s.lg_off + (size_t)k * (s.lg_M + 1) + j;
     const uint32_t e0 = __ldg(off), e1 = __ldg(off + 1);
-    for (uint32_t e = e0; e < e1; e++) {
+    // four candidates per iteration: their index and segment loads in flight together, hits
+    // appended in list order
+    uint32_t e = e0;
+    for (; e + 3 < e1; e += 4) {
+        uint32_t id[4];
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) id[u] = __ldg(s.lg_ent + e + u);
+#pragma unroll
+        for (int u = 0; u < 4; u++) q[u] = __ldg(s.elems + 4 * id[u]);
+        bool h[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            float tt;
+            h[u] = isect_seg(o, d, q[u].x, q[u].y, q[u].z, q[u].w, tt);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (h[u]) {
+                if (count < kHitBuffer) hits[count] = id[u];
+                count++;
+            }
+    }
+    for (; e < e1; e++) {
         const uint32_t i = __ldg(s.lg_ent + e);
         float tt;
         if (isect_elem<2>(s, i, o, d, tt)) {

@@ -56,7 +56,8 @@ struct LineGrid {
     std::vector<uint16_t> entries;     // stored element indices
 };
 constexpr uint32_t kLineGridMaxElems = 16384;   // larger 2D scenes use the BVH alone
-constexpr size_t kLineGridMaxEntries = 1u << 25;  // 64 MB of lists at most
+constexpr size_t kLineGridMaxEntries = 1u << 24;  // 32 MB of lists at most
+constexpr size_t kLineGridEntriesPerElem = 8192;  // 16 KB of lists per segment at most
 constexpr double kLineGridAngleSlack = 1e-6;   // rad: rounding of a query's bin and direction
 
 // The line grid of a 2D scene's stored element records (empty if the scene is too large).
