@@ -63,7 +63,7 @@ void set_last_error(const char *msg) { g_last_error = msg; }
 struct wob_scene_s {
     int device = 0;
     wobgb::HostScene host;
-    DevBuf elems, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
+    DevBuf elems, elem_aux, isect, nodes, area_cdf, area_guide, bv_cdf, bv_guide, err;
     DevBuf vol_values, vol_cdf, vol_guide;
     DevBuf lg_bins, lg_off, lg_ent;  // 2D line grid
     DevBuf cv_table;  // control-variate density per stored element
@@ -83,6 +83,9 @@ struct wob_scene_s {
     template <int D> wobgb::SceneView<D> view() const {
         wobgb::SceneView<D> v{};
         v.elems = (const float4 *)elems.ptr;
+        v.elem_aux = (const float4 *)elem_aux.ptr;
+        v.alpha_const = host.alpha_const ? 1u : 0u;
+        v.alpha_value = host.alpha_value;
         v.isect = (const float4 *)isect.ptr;
         v.nodes = (const float4 *)nodes.ptr;
         v.area_cdf = (const float *)area_cdf.ptr;
@@ -113,7 +116,7 @@ struct wob_scene_s {
         return v;
     }
     void release_all() {
-        for (DevBuf *b : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
+        for (DevBuf *b : {&elems, &elem_aux, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
                           &vol_cdf, &vol_guide, &cv_table, &rhs, &rhs_cv, &ws, &lg_bins, &lg_off, &lg_ent})
             b->release();
         if (ws_stream) cudaStreamDestroy(ws_stream);
@@ -285,6 +288,7 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
     s->bv_G = (uint32_t)(h.bv_guide.size() / 4);
     const uint32_t zero = 0;
     if ((e = upload(s->elems, h.elems.data(), h.elems.size() * 4)) != cudaSuccess ||
+        (e = upload(s->elem_aux, h.elem_aux.data(), h.elem_aux.size() * 4)) != cudaSuccess ||
         (e = upload(s->isect, h.isect.data(), h.isect.size() * 4)) != cudaSuccess ||
         (e = upload(s->nodes, h.nodes.data(), h.nodes.size() * 4)) != cudaSuccess ||
         (e = upload(s->area_cdf, h.area_cdf.data(), h.area_cdf.size() * 4)) != cudaSuccess ||
@@ -326,6 +330,7 @@ int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, co
         d.bytes = bytes;
     };
     take(s->elems, b.elems, b.elems_bytes);
+    take(s->elem_aux, b.elem_aux, b.elem_aux_bytes);
     take(s->isect, b.isect, b.isect_bytes);
     take(s->nodes, b.nodes, b.nodes_bytes);
     take(s->area_cdf, b.area_cdf, b.area_cdf_bytes);
@@ -374,7 +379,7 @@ int wob_scene_get_info(wob_scene s, wob_scene_info *info) {
     info->total_boundary_value = s->host.total_bv;
     info->has_volume_cache = s->has_volume ? 1 : 0;
     size_t bytes = 0;
-    for (const DevBuf *b : {&s->elems, &s->isect, &s->nodes, &s->area_cdf, &s->area_guide, &s->bv_cdf, &s->bv_guide,
+    for (const DevBuf *b : {&s->elems, &s->elem_aux, &s->isect, &s->nodes, &s->area_cdf, &s->area_guide, &s->bv_cdf, &s->bv_guide,
                             &s->vol_values, &s->vol_cdf, &s->vol_guide, &s->lg_bins, &s->lg_off, &s->lg_ent})
         bytes += b->bytes;
     info->bytes_on_device = (uint32_t)(bytes > 0xFFFFFFFFu ? 0xFFFFFFFFu : bytes);

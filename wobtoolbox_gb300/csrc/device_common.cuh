@@ -173,7 +173,8 @@ template <int D> __device__ __forceinline__ BPoint<D> bp_zero() {
 // Scene view (device pointers; filled by the host, passed by value to kernels).
 // ------------------------------------------------------------------------------------------
 template <int D> struct SceneView {
-    const float4 *__restrict__ elems;  // D==2: 4 float4 / element, D==3: 6 (the last one padding)
+    const float4 *__restrict__ elems;     // 4 float4 / element (2D: the last one padding)
+    const float4 *__restrict__ elem_aux;  // D==3: 1 float4 / element (alpha[3], area)
     const float4 *__restrict__ isect;  // D==3: 4 float4 / element (a, a-b, a-c, (a-b)x(a-c), padding)
     const float4 *__restrict__ nodes;  // D==2: 6 float4 / node, D==3: 8 (the last one padding)
     const float *__restrict__ area_cdf;
@@ -190,6 +191,8 @@ template <int D> struct SceneView {
     uint32_t lg_K, lg_M;                 // lg_K == 0: no line grid
     uint32_t *err;                       // device error word (kErr* bits)
     uint32_t n_elems, n_nodes, area_G, bv_G;
+    uint32_t alpha_const;  // D==3: every vertex alpha is alpha_value (elem_aux not read for alphas)
+    float alpha_value;
     uint32_t vol_n, vol_G, vol_res, traversal_limit;
     float total_area, total_bv, vol_size;
 };
@@ -227,17 +230,22 @@ template <> __device__ __forceinline__ Elem<2> load_elem<2>(const SceneView<2> &
     e.alpha[0] = q2.x; e.alpha[1] = q2.y; e.area = q2.z; e.type = __float_as_int(q2.w);
     return e;
 }
+// The 3D record's alphas come from the scene constant when all are equal; the area (used only by
+// |g| sampling, which reads it itself) is left NaN.
 template <> __device__ __forceinline__ Elem<3> load_elem<3>(const SceneView<3> &s, uint32_t i) {
-    const float4 *p = s.elems + 6 * i;
+    const float4 *p = s.elems + 4 * i;
     const F8 r0 = ldg8(p), r1 = ldg8(p + 2);
-    const float4 q0 = r0.a, q1 = r0.b, q2 = r1.a, q3 = r1.b, q4 = __ldg(p + 4);
+    const float4 q0 = r0.a, q1 = r0.b, q2 = r1.a, q3 = r1.b;
+    float4 q4;
+    if (s.alpha_const) q4 = make_float4(s.alpha_value, s.alpha_value, s.alpha_value, __int_as_float(0x7fc00000));
+    else q4 = __ldg(s.elem_aux + i);
     Elem<3> e;
     e.v[0].v[0] = q0.x; e.v[0].v[1] = q0.y; e.v[0].v[2] = q0.z;
     e.v[1].v[0] = q0.w; e.v[1].v[1] = q1.x; e.v[1].v[2] = q1.y;
     e.v[2].v[0] = q1.z; e.v[2].v[1] = q1.w; e.v[2].v[2] = q2.x;
     e.n.v[0] = q2.y; e.n.v[1] = q2.z; e.n.v[2] = q2.w;
     e.bv[0] = q3.x; e.bv[1] = q3.y; e.bv[2] = q3.z; e.type = __float_as_int(q3.w);
-    e.alpha[0] = q4.x; e.alpha[1] = q4.y; e.alpha[2] = q4.z; e.area = q4.w;
+    e.alpha[0] = q4.x; e.alpha[1] = q4.y; e.alpha[2] = q4.z; e.area = __int_as_float(0x7fc00000);
     return e;
 }
 
@@ -530,7 +538,7 @@ template <int D> __device__ __forceinline__ V<D> uniform_position(const SceneVie
         r.v[0] = interp2(q0.x, q0.z, u2);
         r.v[1] = interp2(q0.y, q0.w, u2);
     } else {
-        const float4 *p = s.elems + 6 * i;
+        const float4 *p = s.elems + 4 * i;
         const F8 q = ldg8(p);
         const float cz = __ldg(reinterpret_cast<const float *>(p + 2));
         const float u2 = u[1], u3 = u[2];
@@ -682,7 +690,7 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_boundary_value(cons
         r.bv = interp3(e.bv[0], e.bv[1], e.bv[2], k1, k2, k3);
         r.type = e.type;
         r.alpha = interp3(e.alpha[0], e.alpha[1], e.alpha[2], k1, k2, k3);
-        inv_pdf = e.area / pmf;
+        inv_pdf = __ldg(reinterpret_cast<const float *>(s.elem_aux + idx) + 3) / pmf;
     }
     return r;
 }

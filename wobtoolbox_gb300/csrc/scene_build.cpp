@@ -414,6 +414,7 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
     const int EF = elem_record_floats(dim);
     out.elems.assign((size_t)n * EF, 0.0f);
     if (dim == 3) out.isect.assign((size_t)n * kIsect3Floats, 0.0f);
+    if (dim == 3) out.elem_aux.assign((size_t)n * kElemAux3Floats, 0.0f);
     std::vector<float> areas(n), bvw(n);
     for (uint32_t s = 0; s < n; s++) {
         const uint32_t i = out.order[s];
@@ -436,7 +437,8 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
             for (int k = 0; k < 9; k++) r[k] = v[k];
             r[9] = nn[0]; r[10] = nn[1]; r[11] = nn[2];
             r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2]; r[15] = u2f((uint32_t)types[i]);
-            r[16] = al[0]; r[17] = al[1]; r[18] = al[2]; r[19] = area;
+            float *x = out.elem_aux.data() + (size_t)s * kElemAux3Floats;
+            x[0] = al[0]; x[1] = al[1]; x[2] = al[2]; x[3] = area;
             areas[s] = area;
             bvw[s] = area * (std::fabs(bv[0]) + std::fabs(bv[1]) + std::fabs(bv[2])) / 3.0f;
             // intersection record: a, e1 = a - b, e2 = a - c, q = e1 x e2
@@ -450,6 +452,14 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
             q[10] = e1z * e2x - e1x * e2z;
             q[11] = e1x * e2y - e1y * e2x;
         }
+    }
+
+    if (dim == 3) {
+        out.alpha_value = alphas ? alphas[0] : 0.0f;
+        out.alpha_const = true;
+        if (alphas)
+            for (size_t i = 0; i < (size_t)n * 3; i++)
+                if (f2u(alphas[i]) != f2u(out.alpha_value)) out.alpha_const = false;
     }
 
     kahan_cdf(areas, out.area_cdf, out.total_area);

@@ -355,7 +355,7 @@ template <int D>
 __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const float *__restrict__ verts,
                           const float *__restrict__ normals, const float *__restrict__ bvals,
                           const float *__restrict__ alphas, const int32_t *__restrict__ types, float *elems,
-                          float *isect, float *areas, float *bvw) {
+                          float *elem_aux, float *isect, float *areas, float *bvw) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = val[s];
@@ -376,7 +376,8 @@ __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const fl
         areas[s] = area;
         bvw[s] = area * (fabsf(bv[0]) + fabsf(bv[1])) / 2.0f;
     } else {
-        float *r = elems + (size_t)s * 24;
+        float *r = elems + (size_t)s * 16;
+        float *aux = elem_aux + (size_t)s * 4;
         const float u0 = v[6] - v[0], u1 = v[7] - v[1], u2 = v[8] - v[2];
         const float w0 = v[3] - v[0], w1 = v[4] - v[1], w2 = v[5] - v[2];
         const float x = u1 * w2 - u2 * w1;
@@ -386,8 +387,7 @@ __global__ void k_records(uint32_t n, const uint32_t *__restrict__ val, const fl
         for (int k = 0; k < 9; k++) r[k] = v[k];
         r[9] = nn[0]; r[10] = nn[1]; r[11] = nn[2];
         r[12] = bv[0]; r[13] = bv[1]; r[14] = bv[2]; r[15] = __int_as_float(types[i]);
-        r[16] = al[0]; r[17] = al[1]; r[18] = al[2]; r[19] = area;
-        r[20] = 0.0f; r[21] = 0.0f; r[22] = 0.0f; r[23] = 0.0f;
+        aux[0] = al[0]; aux[1] = al[1]; aux[2] = al[2]; aux[3] = area;
         areas[s] = area;
         bvw[s] = area * (fabsf(bv[0]) + fabsf(bv[1]) + fabsf(bv[2])) / 3.0f;
         float *q = isect + (size_t)s * 16;
@@ -591,12 +591,16 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
     out.depth = depth;
 
     // records, CDFs, guides
-    const int EF = D == 2 ? 16 : 24;
-    float *elems = nullptr, *isect = nullptr, *area_cdf = nullptr, *bv_cdf = nullptr, *areas, *bvw, *totals;
+    const int EF = 16;
+    float *elems = nullptr, *elem_aux = nullptr, *isect = nullptr, *area_cdf = nullptr, *bv_cdf = nullptr, *areas,
+          *bvw, *totals;
     WOB_CK(cudaMalloc(&elems, (size_t)n * EF * 4));
     out.elems = elems;
     out.elems_bytes = (size_t)n * EF * 4;
     if (D == 3) {
+        WOB_CK(cudaMalloc(&elem_aux, (size_t)n * 4 * 4));
+        out.elem_aux = elem_aux;
+        out.elem_aux_bytes = (size_t)n * 4 * 4;
         WOB_CK(cudaMalloc(&isect, (size_t)n * 16 * 4));
         out.isect = isect;
         out.isect_bytes = (size_t)n * 16 * 4;
@@ -610,7 +614,8 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
     WOB_CK(tmp.alloc(&areas, n));
     WOB_CK(tmp.alloc(&bvw, n));
     WOB_CK(tmp.alloc(&totals, 2));
-    k_records<D><<<blocks(n), kT, 0, st>>>(n, val, verts, normals, bvals, alphas, types, elems, isect, areas, bvw);
+    k_records<D><<<blocks(n), kT, 0, st>>>(n, val, verts, normals, bvals, alphas, types, elems, elem_aux, isect, areas,
+                                           bvw);
     k_kahan_cdf<<<1, 32, 0, st>>>(n, areas, bvw, area_cdf, bv_cdf, totals);
     WOB_CK(cudaGetLastError());
     float ht[2];
@@ -647,7 +652,7 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
 }  // namespace
 
 void DeviceSceneBuild::release() {
-    for (void **p : {&elems, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide}) {
+    for (void **p : {&elems, &elem_aux, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }

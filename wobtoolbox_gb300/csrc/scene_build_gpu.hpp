@@ -12,10 +12,10 @@ namespace wobgb {
 // Device buffers of a scene built on the GPU (owned by the caller after a successful build) and
 // the figures the host keeps.
 struct DeviceSceneBuild {
-    void *elems = nullptr, *isect = nullptr, *nodes = nullptr, *area_cdf = nullptr, *area_guide = nullptr,
-         *bv_cdf = nullptr, *bv_guide = nullptr;
-    size_t elems_bytes = 0, isect_bytes = 0, nodes_bytes = 0, area_cdf_bytes = 0, area_guide_bytes = 0,
-           bv_cdf_bytes = 0, bv_guide_bytes = 0;
+    void *elems = nullptr, *elem_aux = nullptr, *isect = nullptr, *nodes = nullptr, *area_cdf = nullptr,
+         *area_guide = nullptr, *bv_cdf = nullptr, *bv_guide = nullptr;
+    size_t elems_bytes = 0, elem_aux_bytes = 0, isect_bytes = 0, nodes_bytes = 0, area_cdf_bytes = 0,
+           area_guide_bytes = 0, bv_cdf_bytes = 0, bv_guide_bytes = 0;
     uint32_t n_nodes = 0, depth = 0, area_G = 0, bv_G = 0;
     float total_area = 0.0f, total_bv = 0.0f;
     bool bv_valid = false, all_dirichlet = true;

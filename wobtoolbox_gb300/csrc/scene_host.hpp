@@ -31,11 +31,14 @@ inline uint32_t make_leaf(uint32_t first, uint32_t count) {
 // with 32-byte loads (ld.global.nc.v8.f32); a random gather costs about the same per load
 // instruction whatever its width, so fewer, wider loads per record are faster.
 //   element: 2D a, b, n, bv[2], alpha[2], area, type + 16 B padding (64 B);
-//            3D a, b, c, n, bv[3], type, alpha[3], area + 16 B padding (96 B)
+//            3D a, b, c, n, bv[3], type (64 B), and in a second array alpha[3], area (16 B),
+//            read only when the scene's Robin alphas are not all the same value (a sample then
+//            costs two 32-byte loads)
 //   node: 2D lo_x[4] lo_y[4] hi_x[4] hi_y[4] child[4] + 16 B padding (96 B);
 //         3D adds lo_z, hi_z (112 B + 16 B padding)
 //   intersection record (3D): a, a - b, a - c, (a - b) x (a - c) + 16 B padding (64 B)
-inline int elem_record_floats(int dim) { return dim == 2 ? 16 : 24; }
+inline int elem_record_floats(int dim) { return dim == 2 ? 16 : 16; }
+constexpr int kElemAux3Floats = 4;
 inline int node_record_floats(int dim) { return dim == 2 ? 24 : 32; }
 constexpr int kIsect3Floats = 16;
 
@@ -68,6 +71,9 @@ struct HostScene {
     uint32_t n = 0;
     std::vector<uint32_t> order;           // order[i] = caller index of stored element i
     std::vector<float> elems;              // n * elem_record_floats(dim)
+    std::vector<float> elem_aux;           // 3D only: n * kElemAux3Floats (alpha[3], area)
+    bool alpha_const = false;              // 3D: every vertex alpha equals alpha_value (bitwise)
+    float alpha_value = 0.0f;
     std::vector<float> isect;              // 3D only: n * kIsect3Floats
     std::vector<float> nodes;              // n_nodes * node_record_floats(dim)
     std::vector<float> area_cdf, bv_cdf;   // n each
