@@ -465,12 +465,20 @@ uint64_t oracle_vpl_paths(int dim, uint32_t n_elems, const float *verts, const f
 
 // VPL aggregation (apps/potential_flow_with_vpl.cu:43-75): sum[pt] += sum_i mu_i (G A, dG/dx A),
 // the engine's blocking: FP32 partial sums over tiles of 256 VPLs, tile t added in FP64 into split
-// t mod 8 (in tile order), the 8 splits added in order.
+// t mod 8 (in tile order), the 8 splits added in order. The pair is the engine's form of
+// G (equation_kernel.cuh:74-79, 115-121) with per-VPL constants, r = y - x, q = |r|^2:
+//   2D: ku = mu (-A/(4 pi)), kw = mu A/(2 pi); mu G A = ku log(max(q, eps^2)) (log(max(|r|, eps))
+//       = log(max(q, eps^2)) / 2); mu w = kw / q (q >= eps^2), kw / (|r| eps) (0 < q < eps^2), 0;
+//   3D: ku = mu A/(4 pi); mu G A = ku / max(|r|, eps); mu w = ku / (|r| max(q, eps)), 0 at q = 0;
+// and mu dG/dx A = mu w (y - x).
 void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, const float *vpl_mu, uint32_t n_vpl,
                           const float *points, uint32_t n_points, double *sum, int n_threads) {
     set_threads(n_threads);
     auto run = [&](auto dimtag) {
         constexpr int D = decltype(dimtag)::value;
+        const float cu = D == 2 ? -0x1.45f306p-4f * area : 0x1.45f306p-4f * area;
+        const float cw = 0x1.45f306p-3f * area;
+        const float eps2 = eps * eps;
 #pragma omp parallel for schedule(dynamic, 16)
         for (int64_t ii = 0; ii < (int64_t)n_points; ii++) {
             Vec<D> x;
@@ -485,22 +493,20 @@ void oracle_vpl_aggregate(int dim, float area, float eps, const float *vpl_p, co
                     Vec<D> y;
                     for (int k = 0; k < D; k++) y.v[k] = vpl_p[(size_t)(t0 + j) * D + k];
                     const float mu = vpl_mu[t0 + j];
-                    // u = G(y, x) A and dG/dx(y, x) A = w (y - x) with one division (the engine's form)
+                    const float ku = mu * cu, kw = mu * cw;
                     const Vec<D> r = y - x;
                     float q = 0.0f;
                     for (int k = 0; k < D; k++) q = q + r.v[k] * r.v[k];
-                    const float nr = std::sqrt(q);
-                    const float mm = fmax_ref(nr, eps);
-                    float u, w;
+                    float g;
                     if (D == 2) {
-                        u = (-0x1.45f306p-3f * log_own(mm)) * area;
-                        w = nr > 0.0f ? (0x1.45f306p-3f * area) / (nr * mm) : 0.0f;
+                        part[0] = part[0] + ku * log_own(fmax_ref(q, eps2));
+                        g = q >= eps2 ? kw / q : (q > 0.0f ? kw / (std::sqrt(q) * eps) : 0.0f);
                     } else {
-                        u = (1.0f / (0x1.921fb6p+3f * mm)) * area;
-                        w = nr > 0.0f ? (0x1.45f306p-4f * area) / (nr * fmax_ref(q, eps)) : 0.0f;
+                        const float nr = std::sqrt(q);
+                        part[0] = part[0] + ku / fmax_ref(nr, eps);
+                        g = q > 0.0f ? ku / (nr * fmax_ref(q, eps)) : 0.0f;
                     }
-                    part[0] = part[0] + mu * u;
-                    for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (w * (y.v[k] - x.v[k]));
+                    for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + g * r.v[k];
                 }
                 for (int c = 0; c <= D; c++) split[t % 8][c] += (double)part[c];
             }

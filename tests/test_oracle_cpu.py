@@ -235,3 +235,35 @@ def test_oracle_bvh_filter_is_exact(oracle, dim):
     _, _, b1, pp1 = oracle.solve_domain(el, p, pts, per_path=True)
     _, _, b2, pp2 = oracle.solve_domain(el, p, pts, per_path=True, accel=True)
     assert b1 == b2 and np.array_equal(pp1, pp2)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_vpl_aggregate_form_matches_fundamental_solution(oracle, dim):
+    """The aggregation's pair form (per-VPL constants, log(max(q, eps^2)) / 2 for log(max(r, eps)),
+    one division for the gradient) is the same function as mu G(y, x) A and mu dG/dx(y, x) A of
+    equation_kernel.cuh:74-81, 115-121, evaluated here in float64, including points on a VPL and
+    within eps of one."""
+    rng = np.random.default_rng(dim)
+    eps = 1e-4
+    area = 3.7
+    vp = rng.uniform(-1, 1, (700, dim)).astype(np.float32)
+    mu = rng.standard_normal(700).astype(np.float32)
+    pts = rng.uniform(-1.2, 1.2, (60, dim)).astype(np.float32)
+    pts[0] = vp[5]                                    # on a VPL: that pair adds G(eps) and no gradient
+    pts[1] = vp[9] + np.float32(3e-5)                 # within eps of a VPL
+    got = oracle.vpl_aggregate(dim, area, eps, vp, mu, pts)
+    r = vp[None].astype(np.float64) - pts[:, None].astype(np.float64)
+    n = np.linalg.norm(r, axis=2)
+    m = np.maximum(n, eps)
+    if dim == 2:
+        G = -np.log(m) / (2 * np.pi)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            w = np.where(n > 0, 1.0 / (2 * np.pi * n * m), 0.0)
+    else:
+        G = 1.0 / (4 * np.pi * m)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            w = np.where(n > 0, 1.0 / (4 * np.pi * n * np.maximum(n * n, eps)), 0.0)
+    ref = np.concatenate([(mu * G * area).sum(1)[:, None], (mu[None, :, None] * w[..., None] * r * area).sum(1)], 1)
+    err = np.abs(got - ref)
+    assert np.all(err[:, 0] <= 1e-5 * np.abs(mu[None] * G * area).sum(1) + 1e-9)
+    assert np.all(err[:, 1:] <= 1e-5 * np.abs(mu[None, :, None] * w[..., None] * r * area).sum(1) + 1e-9)

@@ -40,31 +40,19 @@ __global__ void __launch_bounds__(kBlock) vpl_paths_kernel(SceneView<D> s, WalkP
     }
 }
 
-// One (point, VPL) pair: u = G(y, x) A and the factor w of dG/dx(y, x) A = w (y - x), from
-// r = y - x, n = |r|, m = max(n, eps) (equation_kernel.cuh:74-79, 115-121):
-//   2D: G = -log(m) / (2 pi),  dG/dx = r / (2 pi n m);   3D: G = 1 / (4 pi m),  dG/dx = r / (4 pi n max(n^2, eps)),
-// the gradient with one division instead of normalising r and dividing by m (the engine's walk
-// kernels evaluate Green<D>::dG_dx literally; the oracle restates this form for the aggregation).
-// w = 0 at n = 0, where the normalised direction is the zero vector.
-template <int D>
-__device__ __forceinline__ void vpl_pair(const V<D> &y, const V<D> &x, float area, float eps, float &u, float &w) {
-    const V<D> r = vsub(y, x);
-    const float q = vsqnorm(r);
-    const float n = sqrtf(q);
-    const float m = fmax_ref(n, eps);
-    if constexpr (D == 2) {
-        u = (-0x1.45f306p-3f * log_own(m)) * area;
-        w = n > 0.0f ? (0x1.45f306p-3f * area) / (n * m) : 0.0f;
-    } else {
-        u = (1.0f / (0x1.921fb6p+3f * m)) * area;
-        w = n > 0.0f ? (0x1.45f306p-4f * area) / (n * fmax_ref(q, eps)) : 0.0f;
-    }
-}
-
 // One block serves 32 points with 8 warps; warp w sums the tiles t = w, w + 8, ... (all lanes read
-// the same VPL at a time: one broadcast load), so 8 threads share a point's pairs and the grid
-// fills the GPU even for a few ten thousand points. The 8 per-warp FP64 partial sums of a point
-// are then added in warp order.
+// the same VPL at a time: one shared-memory broadcast), so 8 threads share a point's pairs and the
+// grid fills the GPU even for a few ten thousand points. The 8 per-warp FP64 partial sums of a
+// point are then added in warp order.
+//
+// A pair (point x, VPL y with value mu) adds mu G(y, x) A and mu dG/dx(y, x) A = mu w (y - x), with
+// r = y - x, q = |r|^2 (equation_kernel.cuh:74-79, 115-121), in this form (the oracle restates it):
+//   2D: mu G A = ku log(max(q, eps^2)), ku = mu (-A / (4 pi)) -- log(max(|r|, eps)) / (2 pi)
+//       written as log(max(q, eps^2)) / (4 pi); mu w = kw / q for q >= eps^2, kw / (|r| eps) for
+//       0 < q < eps^2, 0 at q = 0, kw = mu A / (2 pi);
+//   3D: mu G A = ku / max(|r|, eps), mu w = ku / (|r| max(q, eps)) (0 at q = 0), ku = mu A / (4 pi).
+// ku and kw are computed once per VPL when its tile is staged in shared memory ({y, ku, kw} in 2D,
+// {y, ku} in 3D), so a pair costs one log or one more division and no per-pair scaling.
 constexpr int kVplSplit = 8;
 
 template <int D>
@@ -73,6 +61,7 @@ __global__ void __launch_bounds__(32 * kVplSplit) vpl_aggregate_kernel(const flo
                                                                        float area, float eps,
                                                                        const float *__restrict__ pts, uint32_t n_points,
                                                                        double *__restrict__ sum) {
+    __shared__ float4 tile[kVplSplit][kVplTile];
     __shared__ double red[kVplSplit][32][D + 1];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t pt = blockIdx.x * 32u + lane;
@@ -80,22 +69,50 @@ __global__ void __launch_bounds__(32 * kVplSplit) vpl_aggregate_kernel(const flo
     V<D> x = vzero<D>();
     if (active)
         for (int k = 0; k < D; k++) x.v[k] = __ldg(pts + (size_t)pt * D + k);
+    const float cu = D == 2 ? -0x1.45f306p-4f * area : 0x1.45f306p-4f * area;  // -A/(4 pi) or A/(4 pi)
+    const float cw = 0x1.45f306p-3f * area;                                      // A/(2 pi)
+    const float eps2 = eps * eps;
     double acc[D + 1];
     for (int c = 0; c <= D; c++) acc[c] = 0.0;
     const uint32_t n_tiles = (n_vpl + kVplTile - 1) / kVplTile;
     for (uint32_t t = w; t < n_tiles; t += kVplSplit) {
         const uint32_t t0 = t * kVplTile;
         const uint32_t m = min((uint32_t)kVplTile, n_vpl - t0);
+        __syncwarp();
+        for (uint32_t j = lane; j < m; j += 32) {
+            const float mu = __ldg(vpl_mu + t0 + j);
+            float4 e;
+            e.x = __ldg(vpl_p + (size_t)(t0 + j) * D);
+            e.y = __ldg(vpl_p + (size_t)(t0 + j) * D + 1);
+            if constexpr (D == 2) {
+                e.z = mu * cu;
+                e.w = mu * cw;
+            } else {
+                e.z = __ldg(vpl_p + (size_t)(t0 + j) * D + 2);
+                e.w = mu * cu;
+            }
+            tile[w][j] = e;
+        }
+        __syncwarp();
         float part[D + 1];
         for (int c = 0; c <= D; c++) part[c] = 0.0f;
         for (uint32_t j = 0; j < m; j++) {
-            V<D> y;
-            for (int k = 0; k < D; k++) y.v[k] = __ldg(vpl_p + (size_t)(t0 + j) * D + k);
-            const float mu = __ldg(vpl_mu + t0 + j);
-            float u, w;
-            vpl_pair<D>(y, x, area, eps, u, w);
-            part[0] = part[0] + mu * u;
-            for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + mu * (w * (y.v[k] - x.v[k]));
+            const float4 e = tile[w][j];
+            V<D> r;
+            r.v[0] = e.x - x.v[0];
+            r.v[1] = e.y - x.v[1];
+            if constexpr (D == 3) r.v[2] = e.z - x.v[2];
+            const float q = vsqnorm(r);
+            float g;
+            if constexpr (D == 2) {
+                part[0] = part[0] + e.z * log_own(fmax_ref(q, eps2));
+                g = q >= eps2 ? e.w / q : (q > 0.0f ? e.w / (sqrtf(q) * eps) : 0.0f);
+            } else {
+                const float n = sqrtf(q);
+                part[0] = part[0] + e.w / fmax_ref(n, eps);
+                g = q > 0.0f ? e.w / (n * fmax_ref(q, eps)) : 0.0f;
+            }
+            for (int k = 0; k < D; k++) part[1 + k] = part[1 + k] + g * r.v[k];
         }
         for (int c = 0; c <= D; c++) acc[c] += (double)part[c];
     }
