@@ -102,7 +102,10 @@ int wob_device_info(int *device, int *sm_count);
  *   robin_alphas    [n_elems][dim]        per-vertex alpha; may be NULL (all zero)
  *   boundary_types  [n_elems]             WOB_DIRICHLET / WOB_NEUMANN / WOB_ROBIN
  * The scene stores elements in BVH leaf order (as the reference's CDFs are, scene.cuh:275-279);
- * wob_scene_get_element_order() returns that order.
+ * wob_scene_get_element_order() returns that order. 2D scenes of up to 16384 segments also get a
+ * line grid (direction bins x offset cells listing candidate segments in storage order) that
+ * answers the walks' infinite-line queries with the same hits as the BVH; its shape is in
+ * wob_scene_info, and it uses up to min(16 M, 8192 n) two-byte list entries of device memory.
  */
 int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const float *normals,
                      const float *boundary_values, const float *robin_alphas,
