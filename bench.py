@@ -47,12 +47,11 @@ SEED = 0
 # record (76 B) plus one sampling-table entry (8 B).
 BYTES_PER_BOUNCE = 2 * (76 + 8)
 # DRAM bytes (read + write) of one full-size walk launch of this workload, measured by ncu on the
-# timed launch itself (dram__bytes_read.sum + dram__bytes_write.sum, one pass; 15,138,560 +
-# 327,740,160 B, profiles/launches_robin3d_default_bench.md). The scene (5.2 MB of records, 1.3 MB
-# of guides) stays in L2, so DRAM traffic is the scene once plus the points and sums and the
-# write-backs of register spills, not a per-bounce quantity; it applies to the default (full)
-# workload only.
-TRAFFIC_BYTES_PER_LAUNCH = 15_138_560 + 327_740_160
+# timed launch itself (dram__bytes_read.sum + dram__bytes_write.sum, one pass; 15,653,120 +
+# 931,584 B, profiles/launches_robin3d_default_bench.md). The scene (5.2 MB of records, 1.3 MB of
+# guides) stays in L2, so DRAM traffic is the scene once plus the points and sums, not a
+# per-bounce quantity; it applies to the default (full) workload only.
+TRAFFIC_BYTES_PER_LAUNCH = 15_653_120 + 931_584
 WORKLOAD = ("3D interior Robin (du/dn + 2u = h), direct BIE, backward estimator, uniform sampling; "
             "displaced icosphere 81920 triangles; 512x512 z=0 slice over [-1.3,1.3]^2, inside points; "
             "4096 paths x 16 bounces per point per step")
