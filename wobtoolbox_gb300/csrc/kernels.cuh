@@ -31,11 +31,12 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 //
 // A unit is 32 * ppt consecutive paths of one point: lane l runs paths l, l + 32, ... and keeps
 // its running (sum, sum of squares) in FP64, so the FP64 warp reduction and the atomics happen
-// once per unit instead of once per 32 paths. For the uniform-sampling walk the running sums live
-// in shared memory (one slot per thread, touched once per path) instead of 16 registers live
-// through the walk (measured: 33.4 -> 34.0 G bounces/s on the 3D Robin benchmark); the other
-// walks keep them in registers, because they rely on L1 hits that the shared-memory carve-out
-// would take (the 2D line-grid walk lost 7 %).
+// once per unit instead of once per 32 paths. For the uniform-sampling and the backward
+// single-layer walks the running sums live in shared memory (one slot per thread, touched once
+// per path) instead of 16 registers live through the walk (measured: 33.4 -> 34.0 G bounces/s on
+// the 3D Robin benchmark, 201 -> 198 ms per iteration of the single-layer walk on 1.3 M
+// triangles); the line-query walks keep them in registers, because they rely on L1 hits that the
+// shared-memory carve-out would take (the 2D line-grid walk lost 7 %).
 template <int D, int kBie, int kStrat, bool kVol, bool kPerPath, int kMinB = 1>
 __global__ void __launch_bounds__(kBlock, kMinB) domain_kernel(SceneView<D> s, WalkParams p, const float *__restrict__ pts,
                                                         uint32_t n_points, double *__restrict__ sum,
@@ -48,7 +49,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) domain_kernel(SceneView<D> s, W
     const uint32_t span = 32u * p.ppt;
     const uint32_t slabs = (p.n_paths + span - 1u) / span;
     const uint64_t units = (uint64_t)n_points * slabs;
-    constexpr bool kSharedSums = kStrat == kStratUniform;
+    constexpr bool kSharedSums = kStrat == kStratUniform || kStrat == kStratSingleLayer;
     constexpr int kSlots = kSharedSums ? kBlock : 1;
     __shared__ double acc_s[2 * (D + 1)][kSlots];  // [c]: running sum, [D + 1 + c]: sum of squares
     double acc_r[2 * (D + 1)];
