@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -32,6 +33,19 @@ int fail(int code, const std::string &msg) {
 int fail_cuda(cudaError_t e, const char *what) {
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? WOB_ERR_OUT_OF_MEMORY : WOB_ERR_CUDA;
+}
+// Runs an entry point's body; a C++ exception (host allocation failure in the scene, table or
+// staging builds) becomes a status instead of crossing the C ABI.
+template <class F> int guarded(F &&body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        return fail(WOB_ERR_OUT_OF_MEMORY, "out of host memory");
+    } catch (const std::exception &ex) {
+        return fail(WOB_ERR_INVALID_ARGUMENT, ex.what());
+    } catch (...) {
+        return fail(WOB_ERR_INVALID_ARGUMENT, "unexpected error");
+    }
 }
 
 // A device allocation freed with the scene.
@@ -115,6 +129,7 @@ struct wob_scene_s {
         v.vol_size = vol_size;
         return v;
     }
+    ~wob_scene_s() { release_all(); }
     void release_all() {
         for (DevBuf *b : {&elems, &elem_aux, &isect, &nodes, &area_cdf, &area_guide, &bv_cdf, &bv_guide, &err, &vol_values,
                           &vol_cdf, &vol_guide, &cv_table, &rhs, &rhs_cv, &ws, &lg_bins, &lg_off, &lg_ent})
@@ -136,6 +151,7 @@ struct wob_batch_s {
     uint32_t cls_first[3] = {0, 0, 0}, cls_count[3] = {0, 0, 0};
     uint64_t cls_units[3] = {0, 0, 0};
     DevBuf table;
+    ~wob_batch_s() { table.release(); }
 };
 
 namespace {
@@ -264,23 +280,22 @@ int wob_device_info(int *device, int *sm_count) {
     return WOB_OK;
 }
 
-int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const float *normals,
-                     const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
-                     wob_scene *out) {
+static int scene_create_impl(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                             const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                             wob_scene *out) {
     if (!out) return fail(WOB_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    wob_scene_s *s = new wob_scene_s();
+    std::unique_ptr<wob_scene_s> owner(new wob_scene_s());
+    wob_scene_s *s = owner.get();
     std::string err = wobgb::build_host_scene(dim, n_elems, vertices, normals, boundary_values, robin_alphas,
                                               boundary_types, s->host);
     if (!err.empty()) {
-        delete s;
         return fail(WOB_ERR_INVALID_ARGUMENT, err);
     }
     for (uint32_t i = 0; i < n_elems; i++)
         if (boundary_types[i] != WOB_DIRICHLET) s->all_dirichlet = false;
     cudaError_t e = cudaGetDevice(&s->device);
     if (e != cudaSuccess) {
-        delete s;
         return fail_cuda(e, "cudaGetDevice");
     }
     const wobgb::HostScene &h = s->host;
@@ -300,29 +315,35 @@ int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const flo
         (e = upload(s->lg_off, h.line_grid.offsets.data(), h.line_grid.offsets.size() * 4)) != cudaSuccess ||
         (e = upload(s->lg_ent, h.line_grid.entries.data(), h.line_grid.entries.size() * 2)) != cudaSuccess) {
         s->release_all();
-        delete s;
         return fail_cuda(e, "uploading the scene");
     }
-    *out = s;
+    *out = owner.release();
     return WOB_OK;
 }
 
-int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, const float *normals,
-                            const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
-                            void *stream, wob_scene *out) {
+int wob_scene_create(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                     const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                     wob_scene *out) {
+    return guarded([&] {
+        return scene_create_impl(dim, n_elems, vertices, normals, boundary_values, robin_alphas, boundary_types, out);
+    });
+}
+
+static int scene_create_device_impl(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                                    const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                                    void *stream, wob_scene *out) {
     if (!out) return fail(WOB_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    wob_scene_s *s = new wob_scene_s();
+    std::unique_ptr<wob_scene_s> owner(new wob_scene_s());
+    wob_scene_s *s = owner.get();
     cudaError_t e = cudaGetDevice(&s->device);
     if (e != cudaSuccess) {
-        delete s;
         return fail_cuda(e, "cudaGetDevice");
     }
     wobgb::DeviceSceneBuild b;
     std::string err = wobgb::build_device_scene(dim, n_elems, vertices, normals, boundary_values, robin_alphas,
                                                 boundary_types, (cudaStream_t)stream, b, e);
     if (!err.empty()) {
-        delete s;
         return e != cudaSuccess ? fail_cuda(e, "building the scene on the device") : fail(WOB_ERR_INVALID_ARGUMENT, err);
     }
     auto take = [](DevBuf &d, void *p, size_t bytes) {
@@ -352,11 +373,19 @@ int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, co
     const uint32_t zero = 0;
     if ((e = upload(s->err, &zero, 4)) != cudaSuccess) {
         s->release_all();
-        delete s;
         return fail_cuda(e, "allocating the error word");
     }
-    *out = s;
+    *out = owner.release();
     return WOB_OK;
+}
+
+int wob_scene_create_device(int dim, uint32_t n_elems, const float *vertices, const float *normals,
+                            const float *boundary_values, const float *robin_alphas, const int32_t *boundary_types,
+                            void *stream, wob_scene *out) {
+    return guarded([&] {
+        return scene_create_device_impl(dim, n_elems, vertices, normals, boundary_values, robin_alphas, boundary_types,
+                                        stream, out);
+    });
 }
 
 int wob_scene_destroy(wob_scene s) {
@@ -394,7 +423,7 @@ int wob_scene_get_element_order(wob_scene s, uint32_t *order) {
     return WOB_OK;
 }
 
-int wob_scene_set_volume_cache(wob_scene s, uint32_t grid_res, float domain_size, const float *values) {
+static int scene_set_volume_cache_impl(wob_scene s, uint32_t grid_res, float domain_size, const float *values) {
     if (!s || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and values are required");
     if (grid_res < 1) return fail(WOB_ERR_INVALID_ARGUMENT, "grid_res must be >= 1");
     if (!(domain_size > 0.0f) || !(domain_size < 3.0e38f)) return fail(WOB_ERR_INVALID_ARGUMENT, "domain_size must be positive and finite");
@@ -422,6 +451,10 @@ int wob_scene_set_volume_cache(wob_scene s, uint32_t grid_res, float domain_size
     s->vol_G = (uint32_t)(guide.size() / 4);
     s->vol_size = domain_size;
     return WOB_OK;
+}
+
+int wob_scene_set_volume_cache(wob_scene s, uint32_t grid_res, float domain_size, const float *values) {
+    return guarded([&] { return scene_set_volume_cache_impl(s, grid_res, domain_size, values); });
 }
 
 int wob_scene_clear_volume_cache(wob_scene s) {
@@ -467,8 +500,8 @@ int wob_debug_domain_paths(wob_scene s, const wob_params *params, const float *p
     return solve_domain_impl(s, params, points, n_points, nullptr, nullptr, nullptr, values, stream);
 }
 
-int wob_solve_domain_host(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
-                          double *sumsq, uint64_t *bounces) {
+static int solve_domain_host_impl(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                                  double *sumsq, uint64_t *bounces) {
     if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
     wobgb::WalkParams w;
     int st = check_params(s, params, w);
@@ -525,6 +558,11 @@ int wob_solve_domain_host(wob_scene s, const wob_params *params, const float *po
     if (bounces) *bounces += b;
     if (errw) return fail(WOB_ERR_DEVICE_LIMIT, "a BVH traversal hit its stack or step bound");
     return WOB_OK;
+}
+
+int wob_solve_domain_host(wob_scene s, const wob_params *params, const float *points, uint32_t n_points, double *sum,
+                          double *sumsq, uint64_t *bounces) {
+    return guarded([&] { return solve_domain_host_impl(s, params, points, n_points, sum, sumsq, bounces); });
 }
 
 static int solve_boundary_impl(wob_scene s, const wob_params *params, const float *p, const float *n,
@@ -729,8 +767,8 @@ int wob_tunable_variant(wob_scene s, const wob_params *params, int32_t *variant)
     return WOB_OK;
 }
 
-int wob_batch_create(const wob_scene *scenes, const wob_params *params, const uint32_t *n_points, uint32_t n_scenes,
-                     wob_batch *out) {
+static int batch_create_impl(const wob_scene *scenes, const wob_params *params, const uint32_t *n_points, uint32_t n_scenes,
+                             wob_batch *out) {
     if (!out || !scenes || !params || !n_points || n_scenes == 0)
         return fail(WOB_ERR_INVALID_ARGUMENT, "scenes, params, n_points and out are required, n_scenes >= 1");
     *out = nullptr;
@@ -764,7 +802,8 @@ int wob_batch_create(const wob_scene *scenes, const wob_params *params, const ui
         points += n_points[i];
         if (points > 0xFFFFFFFFull) return fail(WOB_ERR_INVALID_ARGUMENT, "a batch holds at most 2^32 - 1 points");
     }
-    wob_batch_s *b = new wob_batch_s();
+    std::unique_ptr<wob_batch_s> owner(new wob_batch_s());
+    wob_batch_s *b = owner.get();
     b->device = device;
     b->dim = dim;
     b->n_scenes = n_scenes;
@@ -794,11 +833,15 @@ int wob_batch_create(const wob_scene *scenes, const wob_params *params, const ui
     cudaError_t e = dim == 2 ? upload(b->table, t2.data(), t2.size() * sizeof(t2[0]))
                              : upload(b->table, t3.data(), t3.size() * sizeof(t3[0]));
     if (e != cudaSuccess) {
-        delete b;
         return fail_cuda(e, "uploading the batch table");
     }
-    *out = b;
+    *out = owner.release();
     return WOB_OK;
+}
+
+int wob_batch_create(const wob_scene *scenes, const wob_params *params, const uint32_t *n_points, uint32_t n_scenes,
+                     wob_batch *out) {
+    return guarded([&] { return batch_create_impl(scenes, params, n_points, n_scenes, out); });
 }
 
 int wob_batch_solve(wob_batch b, const float *points, double *sum, double *sumsq, uint64_t *bounces,
@@ -865,7 +908,7 @@ int wob_solve_domain_cv(wob_scene s, const wob_params *params, uint32_t n_potent
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate walk");
 }
 
-int wob_scene_set_rhs(wob_scene s, const float *values, uint32_t n_rhs) {
+static int scene_set_rhs_impl(wob_scene s, const float *values, uint32_t n_rhs) {
     if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
     if (n_rhs > wobgb::kMaxRhs) return fail(WOB_ERR_INVALID_ARGUMENT, "n_rhs must be at most WOB_MAX_RHS (64)");
     DeviceGuard g(s->device);
@@ -894,6 +937,10 @@ int wob_scene_set_rhs(wob_scene s, const float *values, uint32_t n_rhs) {
     }
     s->n_rhs = n_rhs;
     return WOB_OK;
+}
+
+int wob_scene_set_rhs(wob_scene s, const float *values, uint32_t n_rhs) {
+    return guarded([&] { return scene_set_rhs_impl(s, values, n_rhs); });
 }
 
 namespace {

@@ -291,8 +291,9 @@ void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, 
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     const unsigned n_threads = std::min<unsigned>(hw, K);
     std::vector<std::thread> pool;
-    for (unsigned t = 0; t < n_threads; t++)
-        pool.emplace_back([&, t]() {
+    std::vector<char> failed(n_threads, 0);
+    auto work = [&](unsigned t) {
+        try {
             std::vector<float> lo(n), hi(n);
             std::vector<uint32_t> c0(n), c1(n);
             for (uint32_t k = t; k < K; k += n_threads) {
@@ -308,8 +309,18 @@ void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, 
                 for (uint32_t i = 0; i < n; i++)
                     for (uint32_t j = c0[i]; j <= c1[i]; j++) list[fill[j]++] = (uint16_t)i;
             }
-        });
+        } catch (...) {  // out of host memory: this scene does without a grid
+            failed[t] = 1;
+        }
+    };
+    try {
+        for (unsigned t = 0; t < n_threads; t++) pool.emplace_back(work, t);
+    } catch (...) {  // no threads to be had: build the remaining bins here
+        for (unsigned t = (unsigned)pool.size(); t < n_threads; t++) work(t);
+    }
     for (std::thread &th : pool) th.join();
+    for (char f : failed)
+        if (f) return;
     size_t total = 0;
     for (uint32_t k = 0; k < K; k++) total += lists[k].size();
     if (total > kLineGridMaxEntries) return;
