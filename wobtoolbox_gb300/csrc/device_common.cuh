@@ -476,7 +476,27 @@ __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D>
         const uint32_t code = stack[--sp];
         if (code & 0x80000000u) {
             const uint32_t first = code & 0x0FFFFFFFu, cnt = ((code >> 28) & 7u) + 1u;
-            for (uint32_t i = first; i < first + cnt; i++) {
+            uint32_t i = first;
+            if constexpr (D == 3) {
+                // two triangles at a time: both records' loads in flight, hits appended in order
+                for (; i + 1 < first + cnt; i += 2) {
+                    const float4 *q0 = s.isect + 4 * i, *q1 = q0 + 4;
+                    const F8 a0 = ldg8(q0), a1 = ldg8(q1);
+                    const float4 b0 = __ldg(q0 + 2), b1 = __ldg(q1 + 2);
+                    float t0, t1;
+                    const bool h0 = isect_tri(o, d, a0.a, a0.b, b0, t0);
+                    const bool h1 = isect_tri(o, d, a1.a, a1.b, b1, t1);
+                    if (h0) {
+                        if (count < kHitBuffer) hits[count] = i;
+                        count++;
+                    }
+                    if (h1) {
+                        if (count < kHitBuffer) hits[count] = i + 1;
+                        count++;
+                    }
+                }
+            }
+            for (; i < first + cnt; i++) {
                 float t;
                 if (isect_elem<D>(s, i, o, d, t)) {
                     if (count < kHitBuffer) hits[count] = i;
