@@ -452,6 +452,41 @@ __device__ __forceinline__ bool line_grid_query(const SceneView<2> &s, const V<2
 // leaves come in increasing element order; or the line grid's cell lists, in storage order).
 // Writes the first kHitBuffer element indices to hits and returns the total count. On a stack
 // overflow or runaway traversal it flags s.err and returns what it has.
+// The hits of one leaf (its elements are consecutive in storage order), appended in order; 3D
+// leaves are tested two triangles at a time with both records' loads in flight.
+template <int D>
+__device__ __forceinline__ uint32_t leaf_hits(const SceneView<D> &s, uint32_t code, const V<D> &o, const V<D> &d,
+                                              uint32_t *hits, uint32_t count) {
+    const uint32_t first = code & 0x0FFFFFFFu, cnt = ((code >> 28) & 7u) + 1u;
+    uint32_t i = first;
+    if constexpr (D == 3) {
+        for (; i + 1 < first + cnt; i += 2) {
+            const float4 *q0 = s.isect + 4 * i, *q1 = q0 + 4;
+            const F8 a0 = ldg8(q0), a1 = ldg8(q1);
+            const float4 b0 = __ldg(q0 + 2), b1 = __ldg(q1 + 2);
+            float t0, t1;
+            const bool h0 = isect_tri(o, d, a0.a, a0.b, b0, t0);
+            const bool h1 = isect_tri(o, d, a1.a, a1.b, b1, t1);
+            if (h0) {
+                if (count < kHitBuffer) hits[count] = i;
+                count++;
+            }
+            if (h1) {
+                if (count < kHitBuffer) hits[count] = i + 1;
+                count++;
+            }
+        }
+    }
+    for (; i < first + cnt; i++) {
+        float t;
+        if (isect_elem<D>(s, i, o, d, t)) {
+            if (count < kHitBuffer) hits[count] = i;
+            count++;
+        }
+    }
+    return count;
+}
+
 template <int D>
 __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D> &o, const V<D> &d, uint32_t *hits) {
     if constexpr (D == 2) {
@@ -471,38 +506,42 @@ __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D>
         aux.v[0] = 1.0f / d.v[0]; aux.v[1] = 1.0f / d.v[1]; aux.v[2] = 1.0f / d.v[2];
     }
     uint32_t steps = 0;
+    if constexpr (D == 3) {
+        // Leaves are postponed: a lane pops nodes (testing them) until it holds kLeafBatch leaves
+        // or its stack is empty, then tests the held leaves in the order they were popped, so the
+        // lanes of a warp run node tests together and triangle tests together instead of
+        // alternating between them; the hits and their order are those of the plain depth-first
+        // loop.
+        constexpr int kLeafBatch = 8;
+        uint32_t leaves[kLeafBatch];
+        bool stop = false;
+        while (sp > 0 && !stop) {
+            int nl = 0;
+            while (sp > 0 && nl < kLeafBatch) {
+                if (++steps > s.traversal_limit) { atomicOr(s.err, kErrTraversalLimit); stop = true; break; }
+                const uint32_t code = stack[--sp];
+                if (code & 0x80000000u) {
+                    leaves[nl++] = code;
+                    continue;
+                }
+                uint4 ch;
+                const uint32_t mask = node_hits(s, code, o, aux, c0, ch);
+                const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
+                if (sp + 4 > (int)kStackSize) { atomicOr(s.err, kErrStackOverflow); stop = true; break; }
+#pragma unroll
+                for (int k = 3; k >= 0; k--)
+                    if ((mask >> k) & 1u)
+                        if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
+            }
+            for (int l = 0; l < nl; l++) count = leaf_hits<D>(s, leaves[l], o, d, hits, count);
+        }
+        return count;
+    }
     while (sp > 0) {
         if (++steps > s.traversal_limit) { atomicOr(s.err, kErrTraversalLimit); break; }
         const uint32_t code = stack[--sp];
         if (code & 0x80000000u) {
-            const uint32_t first = code & 0x0FFFFFFFu, cnt = ((code >> 28) & 7u) + 1u;
-            uint32_t i = first;
-            if constexpr (D == 3) {
-                // two triangles at a time: both records' loads in flight, hits appended in order
-                for (; i + 1 < first + cnt; i += 2) {
-                    const float4 *q0 = s.isect + 4 * i, *q1 = q0 + 4;
-                    const F8 a0 = ldg8(q0), a1 = ldg8(q1);
-                    const float4 b0 = __ldg(q0 + 2), b1 = __ldg(q1 + 2);
-                    float t0, t1;
-                    const bool h0 = isect_tri(o, d, a0.a, a0.b, b0, t0);
-                    const bool h1 = isect_tri(o, d, a1.a, a1.b, b1, t1);
-                    if (h0) {
-                        if (count < kHitBuffer) hits[count] = i;
-                        count++;
-                    }
-                    if (h1) {
-                        if (count < kHitBuffer) hits[count] = i + 1;
-                        count++;
-                    }
-                }
-            }
-            for (; i < first + cnt; i++) {
-                float t;
-                if (isect_elem<D>(s, i, o, d, t)) {
-                    if (count < kHitBuffer) hits[count] = i;
-                    count++;
-                }
-            }
+            count = leaf_hits<D>(s, code, o, d, hits, count);
         } else {
             uint4 ch;
             const uint32_t mask = node_hits(s, code, o, aux, c0, ch);
