@@ -9,13 +9,13 @@
 
 namespace wobgb {
 
-// One unit (32 * ppt paths of one point) of a batched scene with the walker variant W.
+// One unit (32 * ppt paths of one point) of a batched scene with the walker variant W; view and
+// p are the scene's view and parameters staged in shared memory by the warp.
 template <int D, class W>
-__device__ __forceinline__ void batch_unit(const BatchEntry<D> &e, uint32_t lane, uint64_t local,
-                                           const float *__restrict__ pts, double *__restrict__ sum,
-                                           double *__restrict__ sumsq, uint64_t path_offset_add,
-                                           unsigned long long &my_bounces) {
-    const WalkParams p = e.params;
+__device__ __forceinline__ void batch_unit(const BatchEntry<D> &e, const SceneView<D> &view, const WalkParams &p,
+                                           uint32_t lane, uint64_t local, const float *__restrict__ pts,
+                                           double *__restrict__ sum, double *__restrict__ sumsq,
+                                           uint64_t path_offset_add, unsigned long long &my_bounces) {
     const uint32_t pt = (uint32_t)(local / e.slabs);
     const uint32_t span = 32u * p.ppt;
     const uint32_t first = (uint32_t)(local % e.slabs) * span;
@@ -30,7 +30,7 @@ __device__ __forceinline__ void batch_unit(const BatchEntry<D> &e, uint32_t lane
         const uint32_t path = first + k * 32u + lane;
         if (path < p.n_paths) {
             float out[D + 1];
-            W w(e.view, p, kStreamDomain, p.point_offset + pt, p.path_offset + path_offset_add + path);
+            W w(view, p, kStreamDomain, p.point_offset + pt, p.path_offset + path_offset_add + path);
             w.domain(x, out);
             my_bounces += w.bounces;
 #pragma unroll
@@ -63,10 +63,13 @@ __global__ void __launch_bounds__(kBlock) batch_domain_kernel(const BatchEntry<D
                                                               double *__restrict__ sumsq,
                                                               unsigned long long *__restrict__ bounces,
                                                               uint64_t path_offset_add) {
-    const uint32_t lane = threadIdx.x & 31u;
+    __shared__ SceneView<D> s_view[kBlock / 32];
+    __shared__ WalkParams s_params[kBlock / 32];
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long my_bounces = 0;
+    uint32_t staged = 0xFFFFFFFFu;
     for (uint64_t u = warp; u < total_units; u += n_warps) {
         uint32_t lo = 0, hi = n_scenes - 1;
         while (lo < hi) {
@@ -75,7 +78,19 @@ __global__ void __launch_bounds__(kBlock) batch_domain_kernel(const BatchEntry<D
             else hi = mid - 1;
         }
         const BatchEntry<D> &e = table[lo];
-        batch_unit<D, W>(e, lane, u - e.unit_begin, pts, sum, sumsq, path_offset_add, my_bounces);
+        if (lo != staged) {  // the warp's scene changed: stage its view and parameters
+            __syncwarp();
+            const uint32_t *sv = reinterpret_cast<const uint32_t *>(&e.view);
+            uint32_t *dv = reinterpret_cast<uint32_t *>(&s_view[wib]);
+            for (uint32_t i = lane; i < sizeof(SceneView<D>) / 4; i += 32) dv[i] = sv[i];
+            const uint32_t *sp = reinterpret_cast<const uint32_t *>(&e.params);
+            uint32_t *dp = reinterpret_cast<uint32_t *>(&s_params[wib]);
+            for (uint32_t i = lane; i < sizeof(WalkParams) / 4; i += 32) dp[i] = sp[i];
+            __syncwarp();
+            staged = lo;
+        }
+        batch_unit<D, W>(e, s_view[wib], s_params[wib], lane, u - e.unit_begin, pts, sum, sumsq, path_offset_add,
+                         my_bounces);
     }
     if (bounces) {
         __syncwarp();
@@ -100,13 +115,13 @@ cudaError_t launch_batch_impl(const BatchEntry<D> *table, uint32_t n_scenes, uin
                               uint64_t path_offset_add, cudaStream_t stream) {
     if (total_units == 0 || n_scenes == 0) return cudaSuccess;
     if (cls == 1u)
-        return launch_class<D, Walker<D, kSingleLayer, kStratSingleLayer, false>>(table, n_scenes, total_units, pts, sum,
+        return launch_class<D, Walker<D, kSingleLayer, kStratSingleLayer, false, true>>(table, n_scenes, total_units, pts, sum,
                                                                                    sumsq, bounces, path_offset_add, stream);
     if (cls == 2u)
-        return launch_class<D, Walker<D, kSingleLayer, kStratFwdSlNeumann, false>>(table, n_scenes, total_units, pts,
+        return launch_class<D, Walker<D, kSingleLayer, kStratFwdSlNeumann, false, true>>(table, n_scenes, total_units, pts,
                                                                                     sum, sumsq, bounces, path_offset_add,
                                                                                     stream);
-    return launch_class<D, Walker<D, -1, kStratRuntime, true>>(table, n_scenes, total_units, pts, sum, sumsq, bounces,
+    return launch_class<D, Walker<D, -1, kStratRuntime, true, true>>(table, n_scenes, total_units, pts, sum, sumsq, bounces,
                                                                 path_offset_add, stream);
 }
 

@@ -8,6 +8,8 @@
 
 #include "device_common.cuh"
 
+#include <type_traits>
+
 namespace wobgb {
 
 struct WalkParams {
@@ -101,10 +103,14 @@ __host__ __device__ __forceinline__ int strategy_of(int bie, int est, int proble
 }
 
 // The scene view and parameters are held by value: a kernel parameter whose address is taken
-// is copied to local memory, a by-value copy stays in registers / the parameter bank.
-template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true> struct Walker {
-    const SceneView<D> s;
-    const WalkParams p;
+// is copied to local memory, a by-value copy stays in registers / the parameter bank. With
+// kByRef the walker holds references instead, for a view and parameters staged in shared memory
+// (the batched launch), which cost a shared-memory load per use instead of registers.
+template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bool kByRef = false> struct Walker {
+    using ViewT = std::conditional_t<kByRef, const SceneView<D> &, const SceneView<D>>;
+    using ParamsT = std::conditional_t<kByRef, const WalkParams &, const WalkParams>;
+    ViewT s;
+    ParamsT p;
     PathRng rng;
     Green<D> K;
     uint32_t bounces;
