@@ -116,6 +116,9 @@ struct wob_scene_s {
         v.lg_ent = (const uint16_t *)lg_ent.ptr;
         v.lg_K = lg_bins.ptr ? host.line_grid.K : 0u;
         v.lg_M = host.line_grid.M;
+        v.lg_cx = host.line_grid.cx;
+        v.lg_cy = host.line_grid.cy;
+        v.lg_far = host.line_grid.far;
         v.n_elems = host.n;
         v.n_nodes = host.n_nodes;
         v.area_G = area_G;

@@ -189,6 +189,7 @@ template <int D> struct SceneView {
     const uint32_t *__restrict__ lg_off; // K x (M + 1) list starts
     const uint16_t *__restrict__ lg_ent; // stored element indices
     uint32_t lg_K, lg_M;                 // lg_K == 0: no line grid
+    float lg_cx, lg_cy, lg_far;          // offset centre; origins farther (L1) take the BVH
     uint32_t *err;                       // device error word (kErr* bits)
     uint32_t n_elems, n_nodes, area_G, bv_G;
     uint32_t alpha_const;  // D==3: every vertex alpha is alpha_value (elem_aux not read for alphas)
@@ -393,12 +394,15 @@ __device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t no
 
 // 2D line query through the line grid: the line's direction bin (diamond angle of the direction
 // taken in the upper half-plane) and offset cell give the candidate segments in storage order,
-// each tested exactly. Returns false (nothing done) when d is not a unit vector within 1e-6, the
-// precondition of the grid's offset bounds; the caller then traverses the BVH.
+// each tested exactly. Returns false (nothing done) when d is not a unit vector within 1e-6 or
+// the origin lies farther than lg_far from the grid's centre, the preconditions of the grid's
+// offset bounds; the caller then traverses the BVH.
 __device__ __forceinline__ bool line_grid_query(const SceneView<2> &s, const V<2> &o, const V<2> &d, uint32_t *hits,
                                                 uint32_t &count) {
     const float q = d.v[0] * d.v[0] + d.v[1] * d.v[1];
     if (!(fabsf(q - 1.0f) <= 1e-6f)) return false;
+    const float ox = o.v[0] - s.lg_cx, oy = o.v[1] - s.lg_cy;
+    if (!(fabsf(ox) + fabsf(oy) <= s.lg_far)) return false;
     const bool flip = d.v[1] < 0.0f || (d.v[1] == 0.0f && d.v[0] < 0.0f);
     const float dx = flip ? -d.v[0] : d.v[0], dy = flip ? -d.v[1] : d.v[1];
     const float t = dy / (fabsf(dx) + dy);
@@ -406,7 +410,7 @@ __device__ __forceinline__ bool line_grid_query(const SceneView<2> &s, const V<2
     uint32_t k = (uint32_t)(pa * (0.5f * (float)s.lg_K));
     k = k < s.lg_K ? k : s.lg_K - 1;
     count = 0;
-    const float c = -dy * o.v[0] + dx * o.v[1];
+    const float c = -dy * ox + dx * oy;
     const float4 b = __ldg(s.lg_bins + k);
     if (!(c >= b.x && c <= b.y)) return true;
     const float f = (c - b.x) * b.z;

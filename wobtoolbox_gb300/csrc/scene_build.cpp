@@ -217,9 +217,9 @@ namespace {
 
 // The offset intervals of all segments over direction bin k of K and their cells among M:
 // fills c0 / c1 and the bin header {cmin, cmax, inv_w, 0}; returns the number of list entries.
-size_t line_bin(const std::vector<float> &elems, uint32_t n, float pad, uint32_t K, uint32_t M, uint32_t k,
-                std::vector<float> &lo, std::vector<float> &hi, std::vector<uint32_t> &c0, std::vector<uint32_t> &c1,
-                float *header) {
+size_t line_bin(const std::vector<float> &elems, uint32_t n, float pad, float cx, float cy, uint32_t K, uint32_t M,
+                uint32_t k, std::vector<float> &lo, std::vector<float> &hi, std::vector<uint32_t> &c0,
+                std::vector<uint32_t> &c1, float *header) {
     const int EF = elem_record_floats(2);
     const double f0 = diamond_to_angle(2.0 * k / K), f1 = diamond_to_angle(2.0 * (k + 1) / K);
     const double nx0 = -std::sin(f0), ny0 = std::cos(f0), nx1 = -std::sin(f1), ny1 = std::cos(f1);
@@ -228,7 +228,7 @@ size_t line_bin(const std::vector<float> &elems, uint32_t n, float pad, uint32_t
     float cmin = std::numeric_limits<float>::infinity(), cmax = -cmin;
     for (uint32_t i = 0; i < n; i++) {
         const float *r = elems.data() + (size_t)i * EF;
-        const double ax = r[0], ay = r[1], bx = r[2], by = r[3];
+        const double ax = (double)r[0] - cx, ay = (double)r[1] - cy, bx = (double)r[2] - cx, by = (double)r[3] - cy;
         const double ga0 = nx0 * ax + ny0 * ay, ga1 = nx1 * ax + ny1 * ay;
         const double gb0 = nx0 * bx + ny0 * by, gb1 = nx1 * bx + ny1 * by;
         const double rad = std::max(std::hypot(ax, ay), std::hypot(bx, by)) * bend + (double)pad;
@@ -253,14 +253,16 @@ size_t line_bin(const std::vector<float> &elems, uint32_t n, float pad, uint32_t
 }
 
 // Estimated list entries of a K x M grid from 16 evenly spaced bins.
-double line_grid_estimate(const std::vector<float> &elems, uint32_t n, float pad, uint32_t K, uint32_t M) {
+double line_grid_estimate(const std::vector<float> &elems, uint32_t n, float pad, float cx, float cy, uint32_t K,
+                          uint32_t M) {
     std::vector<float> lo(n), hi(n);
     std::vector<uint32_t> c0(n), c1(n);
     float header[4];
     const uint32_t step = std::max<uint32_t>(1u, K / 16);
     double sum = 0.0;
     uint32_t cnt = 0;
-    for (uint32_t k = step / 2; k < K; k += step, cnt++) sum += (double)line_bin(elems, n, pad, K, M, k, lo, hi, c0, c1, header);
+    for (uint32_t k = step / 2; k < K; k += step, cnt++)
+        sum += (double)line_bin(elems, n, pad, cx, cy, K, M, k, lo, hi, c0, c1, header);
     return cnt ? sum / cnt * K : 0.0;
 }
 
@@ -276,11 +278,27 @@ double line_grid_estimate(const std::vector<float> &elems, uint32_t n, float pad
 void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, LineGrid &grid) {
     grid = LineGrid();
     if (n == 0 || n > kLineGridMaxElems) return;
+    // offsets about the centre of the scene's box; a line through a point farther than 8 (extent +
+    // max |coordinate|) from it takes the BVH, so the query's float offset stays within the
+    // padding of the exact one
+    const int EF = elem_record_floats(2);
+    float bmin[2] = {std::numeric_limits<float>::infinity(), std::numeric_limits<float>::infinity()};
+    float bmax[2] = {-bmin[0], -bmin[1]};
+    for (uint32_t i = 0; i < n; i++)
+        for (int v = 0; v < 2; v++)
+            for (int k = 0; k < 2; k++) {
+                bmin[k] = std::min(bmin[k], elems[(size_t)i * EF + 2 * v + k]);
+                bmax[k] = std::max(bmax[k], elems[(size_t)i * EF + 2 * v + k]);
+            }
+    const float cx = (float)(0.5 * ((double)bmin[0] + bmax[0])), cy = (float)(0.5 * ((double)bmin[1] + bmax[1]));
+    const float ext = std::max(bmax[0] - bmin[0], bmax[1] - bmin[1]);
+    const float mag =
+        std::max(std::max(std::fabs(bmin[0]), std::fabs(bmax[0])), std::max(std::fabs(bmin[1]), std::fabs(bmax[1])));
     uint32_t K = 128, M = 64;
     while (K < n && K < 1024) K <<= 1;
     while (M < 2 * n && M < 4096) M <<= 1;
     const double budget = std::min((double)kLineGridMaxEntries, (double)kLineGridEntriesPerElem * n);
-    while (K >= 64 && M >= 64 && line_grid_estimate(elems, n, pad, K, M) > budget) {
+    while (K >= 64 && M >= 64 && line_grid_estimate(elems, n, pad, cx, cy, K, M) > budget) {
         if (M > K) M >>= 1;
         else K >>= 1;
     }
@@ -297,7 +315,8 @@ void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, 
             std::vector<float> lo(n), hi(n);
             std::vector<uint32_t> c0(n), c1(n);
             for (uint32_t k = t; k < K; k += n_threads) {
-                const size_t listed = line_bin(elems, n, pad, K, M, k, lo, hi, c0, c1, bins.data() + 4 * (size_t)k);
+                const size_t listed = line_bin(elems, n, pad, cx, cy, K, M, k, lo, hi, c0, c1,
+                                               bins.data() + 4 * (size_t)k);
                 std::vector<uint32_t> &count = counts[k];
                 count.assign(M + 1, 0u);
                 for (uint32_t i = 0; i < n; i++)
@@ -326,6 +345,9 @@ void build_line_grid_2d(const std::vector<float> &elems, uint32_t n, float pad, 
     if (total > kLineGridMaxEntries) return;
     grid.K = K;
     grid.M = M;
+    grid.cx = cx;
+    grid.cy = cy;
+    grid.far = 8.0f * (ext + mag);
     grid.bins = std::move(bins);
     grid.offsets.resize((size_t)K * (M + 1));
     grid.entries.resize(total);

@@ -44,7 +44,7 @@ constexpr int kIsect3Floats = 16;
 
 // 2D line grid: all segments an infinite line can meet, by direction and offset. The directions
 // (half-turn, diamond angle pa in [0, 2]) are cut into K bins; for bin k and a segment, the offsets
-// c = n . p (n = (-sin phi, cos phi)) its points take over the bin's directions form an interval,
+// c = n . (p - centre) (n = (-sin phi, cos phi)) its points take over the bin's directions form an interval,
 // widened by the curvature of the sinusoids, an angle slack and the scene's padding; the offsets of
 // bin k, [cmin, cmax], are cut into M cells, and a cell lists, in storage order, every segment whose
 // interval meets it. A line of bin k with offset c can only meet the segments listed in c's cell,
@@ -54,6 +54,8 @@ constexpr int kIsect3Floats = 16;
 // can fall in.
 struct LineGrid {
     uint32_t K = 0, M = 0;             // K == 0: no grid (the BVH answers line queries)
+    float cx = 0.0f, cy = 0.0f;        // offsets are taken about this point (the scene's box centre)
+    float far = 0.0f;                  // lines through points farther than this (L1 from the centre) take the BVH
     std::vector<float> bins;           // K * 4: cmin, cmax, inv_w, 0
     std::vector<uint32_t> offsets;     // K * (M + 1): start of each cell's list in entries
     std::vector<uint16_t> entries;     // stored element indices
