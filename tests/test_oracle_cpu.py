@@ -267,3 +267,50 @@ def test_vpl_aggregate_form_matches_fundamental_solution(oracle, dim):
     err = np.abs(got - ref)
     assert np.all(err[:, 0] <= 1e-5 * np.abs(mu[None] * G * area).sum(1) + 1e-9)
     assert np.all(err[:, 1:] <= 1e-5 * np.abs(mu[None, :, None] * w[..., None] * r * area).sum(1) + 1e-9)
+
+
+@pytest.mark.parametrize("combo", [(0, 0, 0, 0, 1), (0, 0, 1, 1, 1), (2, 1, 0, 2, 1), (0, 1, 0, 3, 8), (2, 0, 0, 3, 1)])
+def test_estimators_unbiased_2d(oracle, combo):
+    """2D counterparts of the 3D z-tests: single layer interior Dirichlet (backward) and Neumann
+    (forward), direct exterior Robin, single layer exterior mixed with resampling (8 candidates),
+    direct interior mixed — on a 3-lobed star against e^x cos y / x / |x|^2."""
+    import wobtoolbox_gb300 as wob
+    bie, dom, est, prob, ris = combo
+    sc = S.scene2d(prob, bool(dom), n_seg=200)
+    el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    n = 8192
+    p = wob.EstimatorParams(bie_model=bie, domain=dom, estimator=est, problem=prob, path_length=8,
+                            num_sample_paths=n, seed=21, num_resampling_candidates=ris,
+                            eps=1e-5 if bie == 0 else float(np.finfo(np.float32).eps),
+                            first_kind_equation_scaling_constant=2.0 if prob == 3 else 1.0)
+    pts = sc["points"][:5]
+    s, q, _, _ = oracle.solve_domain(el, p, pts)
+    mean = s / n
+    var = q / n - mean ** 2
+    ex = sc["u"](pts)
+    comps = [1, 2] if (prob == 1 and dom == 0) else [0]
+    for c in comps:
+        z = _z_test(mean[:, c], ex[:, c], var[:, c], n)
+        bias = np.abs(mean[:, c] - ex[:, c])
+        ok = (np.abs(z) < 5.0) | (bias < 0.05 * np.abs(ex[:, c]) + 2e-3)
+        assert np.all(ok), (c, z, mean[:, c], ex[:, c])
+
+
+def test_volume_source_box_center(oracle):
+    """apps/poisson_equation.cu's problem: u = 1 on the box (-1, 1)^2 and the constant source 5
+    through a volume cache; at the centre u = 1 - 5 * 0.294685 (the square's torsion function at
+    its centre, with the sign the estimator's volume term carries)."""
+    import wobtoolbox_gb300 as wob
+    sq = np.array([[[-1, -1], [-1, 1]], [[-1, 1], [1, 1]], [[1, 1], [1, -1]], [[1, -1], [-1, -1]]], np.float32)
+    nrm = np.array([[-1, 0], [0, 1], [1, 0], [0, -1]], np.float32)
+    res = 128
+    el = oracle.Elements(sq, nrm, np.ones((4, 2), np.float32), np.zeros(4, np.int32),
+                         volume=(res, 2.0, np.full(res * res, 5.0, np.float32)))
+    n = 40000
+    p = wob.EstimatorParams(bie_model=1, path_length=4, num_sample_paths=n, num_volume_samples=16, eps=1e-4, seed=2)
+    pts = np.zeros((8, 2), np.float32)  # eight independent estimates (point index seeds the stream)
+    s, q, _, _ = oracle.solve_domain(el, p, pts)
+    mean = s[:, 0] / n
+    se = np.sqrt((q[:, 0] / n - mean ** 2) / n)
+    m, e = mean.mean(), se.mean() / np.sqrt(len(mean))
+    assert abs(m - (1.0 - 5.0 * 0.294685)) < 5 * e + 0.01, (m, e)
