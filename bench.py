@@ -352,8 +352,10 @@ def run_ours(args):
     kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     local_s = sum(kernel_ms) / 1e3
     bounces_local = int(d_b.item())
-    if scene.poll_error():
-        raise RuntimeError("device traversal limit hit")
+    # every rank learns of a traversal-limit hit on any rank before the collectives below, so all
+    # ranks stop together instead of some waiting in all_reduce
+    if max_over_ranks(float(scene.poll_error()), world):
+        raise RuntimeError("device traversal limit hit on some rank")
     total_s = max_over_ranks(local_s, world)
     bounces_all = sum_over_ranks(bounces_local, world)
     value = bounces_all / total_s

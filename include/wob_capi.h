@@ -198,10 +198,19 @@ int wob_get_domain_config(int32_t variant, int32_t *config);
  * It stages points, running sums and the bounce counter through a 16 MiB static device array
  * that every GPU loading the library holds until the process exits, so n_points is limited to
  * wob_noalloc_max_points(dim) (about 220k points in 3D, 300k in 2D); larger requests fail with
- * WOB_ERR_INVALID_ARGUMENT. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. All calls on a device
- * share the one array: calls are serialised within a process, calls from several processes or
- * threads that overlap on the GPU race on it. It calls no cudaMalloc / cudaFree.
+ * WOB_ERR_INVALID_ARGUMENT. It calls no cudaMalloc / cudaFree.
+ *
+ * Set-up: the first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and keeps it. Under lazy module loading (the CUDA default) that lookup is also when the runtime
+ * loads the module and reserves the array, so make the first call on each device at set-up time,
+ * before any stream capture and before a phase that must not allocate. The kept address belongs
+ * to the device's context: do not call this entry point for a device after cudaDeviceReset on it.
+ *
+ * Sharing: each process (each CUDA context) has its own copy of the array. Within a process every
+ * call uses the same array, which keeps the previous call's contents (the sums are reloaded from
+ * the caller's arrays and the counter cleared on each call); calls that overlapped on the GPU would
+ * race on it, so one process-wide lock is held from staging until the call's stream is
+ * synchronised. Calls never overlap, and calls for different devices wait for each other.
  */
 int wob_solve_domain_host_noalloc(wob_scene scene, const wob_params *params, const float *points,
                                   uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,

@@ -250,7 +250,11 @@ uint32_t noalloc_max_points(int D) {
 }
 
 // Device address of the scratch array on `device` (which must be current). The host-side name
-// g_noalloc_scratch is only a stand-in: its address has to be looked up once per device.
+// g_noalloc_scratch is only a stand-in: its address has to be looked up once per device. The
+// lookup also makes the runtime load this module on the device if it has not yet (lazy module
+// loading), which is when the array's memory is reserved. The cached address belongs to the
+// device's current context; a cudaDeviceReset destroys that context, and the address must not be
+// used after it.
 int noalloc_scratch(int device, void **out) {
     if (device < 0 || device >= kNoAllocMaxDevices) return fail(WOB_ERR_UNSUPPORTED, "device index out of range for the no-allocation scratch");
     if (!g_noalloc_addr[device]) {
@@ -641,8 +645,9 @@ int wob_noalloc_max_points(int dim, uint32_t *max_points) {
     return WOB_OK;
 }
 
-int wob_solve_domain_host_noalloc(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
-                                  double *sum, double *sumsq, uint64_t *bounces, void *stream) {
+static int solve_domain_host_noalloc_impl(wob_scene s, const wob_params *params, const float *points,
+                                         uint32_t n_points, double *sum, double *sumsq, uint64_t *bounces,
+                                         void *stream) {
     if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
     wobgb::WalkParams w;
     int st = check_params(s, params, w);
@@ -692,6 +697,13 @@ int wob_solve_domain_host_noalloc(wob_scene s, const wob_params *params, const f
     if (bounces) *bounces += b;
     if (errw) return fail(WOB_ERR_DEVICE_LIMIT, "a BVH traversal hit its stack or step bound");
     return WOB_OK;
+}
+
+int wob_solve_domain_host_noalloc(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
+                                  double *sum, double *sumsq, uint64_t *bounces, void *stream) {
+    return guarded([&] {
+        return solve_domain_host_noalloc_impl(s, params, points, n_points, sum, sumsq, bounces, stream);
+    });
 }
 
 int wob_autotune_domain(wob_scene s, const wob_params *params, const float *points, uint32_t n_points,
