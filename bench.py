@@ -454,6 +454,12 @@ def run_ours(args):
                                    "sample": f"the full workload: {len(sc['points'])} points x {p.num_sample_paths} "
                                              f"paths x {p.path_length} bounces ({dt:.1f} s)"}
     scene.close()
+    if rank == 0 and args.workload == "robin3d" and not args.small and not args.no_time_to_rmse:
+        # the metric's second half: time to RMSE 1e-3 against the analytic solution, plain vs the
+        # learned residual control variate, on the exterior Neumann workload (327,680 triangles)
+        ttr = cv_time_to_rmse(dev, plain_budget=12.0, cv_budget=4.0)
+        ttr["cv_curve"] = ttr["cv_curve"][::max(1, len(ttr["cv_curve"]) // 8)]
+        out["time_to_rmse"] = ttr
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -563,24 +569,28 @@ def run_batch(args):
         s.close()
 
 
-def run_cv(args):
-    """Learned control variate vs plain WoB, time to RMSE: 3D exterior Neumann problem on a displaced
-    icosphere with 327,680 triangles, u = sum_{k<3} q_k / (4 pi |x - s_k|) with s_k inside (radius
-    <= 0.5) and q_k ~ U[-1, 1]; forward single-layer estimator (the reference's choice for exterior
-    Neumann, data/config_general_3d_exterior_Neumann.json), 4 bounces. The network (32 Fourier
-    features of (x, n), 4 x 64 SiLU, scalar) is trained for 2000 Adam steps on 65,536 boundary
-    points x 256-path walk estimates of the density; evaluation at the 256^2 points of the z = 0
-    slice over [-2, 2]^2 outside the surface. Both estimators run progressive iterations; the RMSE
-    against the exact solution after each one is recorded against cumulative GPU time."""
+def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, plain_budget=20.0, cv_budget=5.0,
+                    train_steps=2000, near_factor=3.0, seed=SEED):
+    """Time to RMSE `target` against the analytic solution, plain forward WoB vs the learned
+    residual control variate, on the exterior Neumann workload: displaced icosphere (0.15 sum
+    c_lm Y_lm, l <= 4) subdivided `subdiv` times (7: 327,680 triangles), Neumann data of
+    u = sum_{k<3} q_k / (4 pi |x - s_k|) with s_k inside at radius <= 0.5 and q_k ~ U[-1, 1];
+    forward single-layer estimator (data/config_general_3d_exterior_Neumann.json), 4 bounces;
+    evaluation at the 256^2 points of the z = 0 slice over [-2, 2]^2 outside the surface.
+
+    Both estimators run progressive iterations (plain_paths / cv_paths new paths per point each) and
+    the RMSE of the running estimate is taken after each; times are wall-clock on a synchronised
+    device, excluding only the RMSE evaluation. The control variate's clock starts before its
+    training labels: labels (65,536 boundary points x 256-path walk estimates of the density),
+    2000 device Adam steps of the 32-frequency 4 x 64 SiLU network, the network at every
+    triangle's centroid, the residual Neumann data, the residual scene, the control variate's
+    potential at the points, then the residual walks. Returns a dict."""
     import torch
     import wobtoolbox_gb300 as wob
     from wobtoolbox_gb300 import cv
     from wobtoolbox_gb300 import workloads as W
-    rank, world, local = dist_init(args)
-    wob.load()
-    dev = torch.device("cuda", torch.cuda.current_device())
-    rng = np.random.default_rng(SEED)
-    V, F, coeffs = W.displaced_icosphere(args.cv_subdiv, 0.15, 4, SEED)
+    rng = np.random.default_rng(seed)
+    V, F, _ = W.displaced_icosphere(subdiv, 0.15, 4, seed)
     verts, normals = W.mesh_elements(V, F)
     dirs = rng.standard_normal((3, 3))
     dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
@@ -588,9 +598,7 @@ def run_cv(args):
     q = rng.uniform(-1, 1, 3)
     uv = W.point_sources(verts.reshape(-1, 3), src, q).reshape(len(F), 3, 4)
     g = (uv[..., 1:] * normals[:, None, :].astype(np.float64)).sum(-1).astype(np.float32)
-    types = np.ones(len(F), np.int32)
-    scene = wob.SceneHost(verts, normals, g, types)
-    # evaluation points: z = 0 slice, outside the surface (half-line parity on the GPU)
+    scene = wob.SceneHost(verts, normals, g, np.ones(len(F), np.int32))
     cand = W.slice_points_z0(256, 4.0)
     d_c = torch.from_numpy(cand).to(dev)
     d_dir = torch.from_numpy(probe_dirs(len(cand))).to(dev)
@@ -603,102 +611,98 @@ def run_cv(args):
     outside = (((t > 0) & valid).sum(1) % 2 == 0).cpu().numpy()
     del hits, hp
     pts = np.ascontiguousarray(cand[outside])
-    exact = W.point_sources(pts, src, q)[:, 0]
+    exact_u = W.point_sources(pts, src, q)[:, 0]
     n_pts = len(pts)
     d_pts = torch.from_numpy(pts).to(dev)
     base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.ExteriorDomain,
-                               estimator=wob.ForwardEstimator, problem=wob.NeumannProblem, path_length=4, seed=SEED)
-    paths = args.cv_paths
-    stream = torch.cuda.current_stream()
+                               estimator=wob.ForwardEstimator, problem=wob.NeumannProblem, path_length=4, seed=seed)
 
-    def progressive(solve, budget_s):
-        s = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
-        b = torch.zeros(1, dtype=torch.int64, device=dev)
-        curve, total_ms, k = [], 0.0, 0
-        while total_ms / 1e3 < budget_s and k < 4096:
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            solve(dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths), s, b)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            total_ms += e0.elapsed_time(e1)
+    def clock():
+        torch.cuda.synchronize()
+        return time.perf_counter()
+
+    def progressive(sc, paths, budget_s, t_start, offset_u=None):
+        s_ = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
+        b_ = torch.zeros(1, dtype=torch.int64, device=dev)
+        curve, k, elapsed = [], 0, 0.0
+        t_hit = None
+        while elapsed < budget_s and k < 100000:
+            t0 = clock()
+            sc.solve_domain(dataclasses.replace(base, num_sample_paths=paths, path_offset=k * paths), d_pts, n_pts,
+                            s_, None, b_)
+            elapsed += clock() - t0
             k += 1
-            u = s[:, 0].cpu().numpy() / (k * paths)
-            curve.append((total_ms / 1e3, float(np.sqrt(np.mean((u - exact) ** 2))), k * paths))
-        return curve, int(b.item())
-
-    def time_to(curve, target):
-        for t_s, r, _ in curve:
+            u = s_[:, 0].cpu().numpy() / (k * paths)
+            if offset_u is not None:
+                u = u + offset_u
+            r = float(np.sqrt(np.mean((u - exact_u) ** 2)))
+            curve.append((t_start + elapsed, r, k * paths))
             if r <= target:
-                return t_s
-        return None
+                t_hit = t_start + elapsed
+                break
+        return curve, t_hit, int(b_.item())
 
-    # warm up both kernels
+    # warm-up of the walk kernel and of the training graph (not timed)
     tmp = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
     scene.solve_domain(dataclasses.replace(base, num_sample_paths=32), d_pts, n_pts, tmp)
-    plain_curve, plain_b = progressive(lambda p, s, b: scene.solve_domain(p, d_pts, n_pts, s, None, b, stream),
-                                       args.cv_budget)
-    t0 = time.perf_counter()
-    mlp, info = cv.train_density_cv(scene, base, n_train=65536, train_paths=256, steps=2000, batch=8192, lr=2e-3,
-                                    freq_sigma=args.cv_sigma, seed=SEED)
-    table = cv.element_cv_table(mlp, scene)
-    cv.set_control_variate(scene, table)
-    t_setup = time.perf_counter() - t0
-    cv.solve_domain_cv(scene, dataclasses.replace(base, num_sample_paths=32), d_pts, n_pts, tmp,
-                       n_potential=args.cv_npot, n_kernel=args.cv_nker)
-    cv_curve, cv_b = progressive(lambda p, s, b: cv.solve_domain_cv(scene, p, d_pts, n_pts, s, None, b,
-                                                                      n_potential=args.cv_npot,
-                                                                      n_kernel=args.cv_nker, stream=stream),
-                                 args.cv_budget)
-    final_plain, final_cv = plain_curve[-1][1], cv_curve[-1][1]
-    target = max(1e-3, max(min(r for _, r, _ in plain_curve), min(r for _, r, _ in cv_curve)) * 1.0001)
-    tp, tc = time_to(plain_curve, target), time_to(cv_curve, target)
+    warm, _ = cv.train_density_cv(scene, base, n_train=8192, train_paths=16, steps=20, batch=8192, lr=2e-3, seed=99)
+    warm.close()
+    torch.cuda.synchronize()
 
-    def rmse_at(curve, t_s):
-        best = None
-        for tt, r, _ in curve:
-            if tt <= t_s:
-                best = r
-        return best
-
-    t_eq = min(plain_curve[-1][0], cv_curve[-1][0])
-    # plain walk against its algorithmic bytes: one line query per bounce, N_node = 116.31,
-    # N_prim = 13.38 (oracle/roofline_constants.py): 32 N_node + 76 N_prim + 12 bytes per bounce
-    bpb = 32 * 116.31 + 76 * 13.38 + 12
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            hbm = float(json.load(f).get("hbm_gbs", 6800.0))
-    except OSError:
-        hbm = 6800.0
-    plain_rate = plain_b / plain_curve[-1][0]
+    plain_curve, t_plain, plain_b = progressive(scene, plain_paths, plain_budget, 0.0)
+    t0 = clock()
+    mlp, info = cv.train_density_cv(scene, base, n_train=65536, train_paths=256, steps=train_steps, batch=8192,
+                                    lr=2e-3, freq_sigma=1.0, seed=seed)
+    t1 = clock()
+    rscene, sigma = cv.residual_control_variate(scene, mlp, wob.ExteriorDomain, near_factor=near_factor)
+    t2 = clock()
+    pot = cv.control_variate_potential(scene, sigma, d_pts, n_pts, near_factor=near_factor)
+    u_cv = pot[:, 0].double().cpu().numpy()
+    t3 = clock()
+    setup = t3 - t0
+    cv_curve, t_cv, cv_b = progressive(rscene, cv_paths, cv_budget, setup, offset_u=u_cv)
+    rate = plain_b / max(plain_curve[-1][0], 1e-9)
     out = {
-        "metric": "time to RMSE vs analytic, plain vs learned-CV WoB (3D exterior Neumann, 327,680 triangles)",
-        "value": (tp / tc) if (tp and tc) else None, "unit": "x (plain time / CV time to the common RMSE target)",
-        "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": "exterior Neumann, forward single layer, 4 bounces; CV: 32 Fourier features, "
-                               "4x64 SiLU, 2000 Adam steps on 65,536 x 256-path density estimates",
-                   "triangles": int(len(F)), "points": n_pts, "paths_per_iteration": paths,
-                   "cv_potential_samples": args.cv_npot, "cv_kernel_samples": args.cv_nker,
-                   "rmse_target": target, "plain_time_to_target_s": tp, "cv_time_to_target_s": tc,
-                   "cv_setup_s (labels + training + table)": t_setup, "train_info": {k: v for k, v in info.items()
-                                                                                   if k != "history"},
-                   "rmse_at_equal_time": {"t_s": t_eq, "plain": rmse_at(plain_curve, t_eq),
-                                          "cv": rmse_at(cv_curve, t_eq)},
-                   "final": {"plain": plain_curve[-1], "cv": cv_curve[-1]},
-                   "plain_bounces": plain_b, "cv_bounces": cv_b,
-                   "plain_curve": plain_curve[::max(1, len(plain_curve) // 12)],
-                   "cv_curve": cv_curve[::max(1, len(cv_curve) // 12)]},
-        "roofline": {"bound": "hbm", "kernel": "plain forward single-layer walk (3D line queries)",
-                     "achieved": bpb * plain_rate / 1e9, "peak": hbm, "unit": "GB/s",
-                     "frac": bpb * plain_rate / 1e9 / hbm, "algorithmic_bytes_per_bounce": bpb,
-                     "bounces_per_s": plain_rate, "traffic": None,
-                     "note": "the 327,680-triangle scene (about 50 MB of records and nodes) is L2-resident"},
+        "target_rmse": target, "plain_s": t_plain, "cv_s": t_cv,
+        "plain_over_cv": (t_plain / t_cv) if (t_plain and t_cv) else None,
+        "cv_setup_s": {"labels": info["t_labels_s"], "training_2000_adam_steps": info["t_train_s"],
+                       "labels_and_training": t1 - t0, "residual_data_and_scene": t2 - t1, "potential": t3 - t2,
+                       "total": setup},
+        "cv_walk_s": (t_cv - setup) if t_cv else None,
+        "paths_per_point": {"plain": plain_curve[-1][2], "cv": cv_curve[-1][2]},
+        "final_rmse": {"plain": plain_curve[-1][1], "cv": cv_curve[-1][1]},
+        "triangles": int(len(F)), "points": n_pts, "plain_bounces_per_s": rate,
+        "train_loss_first_last": [info["history"][0][1], info["history"][-1][1]],
+        "plain_curve": plain_curve[::max(1, len(plain_curve) // 8)], "cv_curve": cv_curve,
+        "clock": "wall time on a synchronised device; RMSE evaluation excluded; CV time includes its setup",
+    }
+    mlp.close()
+    rscene.close()
+    scene.close()
+    return out
+
+
+def run_cv(args):
+    """Learned control variate vs plain WoB, time to RMSE 1e-3 against the analytic solution on
+    the exterior Neumann workload (cv_time_to_rmse)."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    rank, world, local = dist_init(args)
+    wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    res = cv_time_to_rmse(dev, subdiv=args.cv_subdiv, plain_paths=args.cv_paths, plain_budget=args.cv_budget,
+                          cv_budget=args.cv_budget, near_factor=args.cv_near)
+    out = {
+        "metric": "time to RMSE 1e-3 vs analytic, plain vs learned-CV WoB (3D exterior Neumann)",
+        "value": res["plain_over_cv"], "unit": "x (plain time / CV time including its setup)", "n_gpus": world,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "exterior Neumann, forward single layer, 4 bounces, displaced icosphere; residual "
+                               "control variate: 32 Fourier features, 4x64 SiLU, 2000 Adam steps on 65,536 x "
+                               "256-path density estimates"},
+        "time_to_rmse": res,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
-    mlp.close()
-    scene.close()
 
 
 def mixed_rhs_scene(subdiv, n_rhs, seed=SEED, dev=None):
@@ -1161,11 +1165,11 @@ def main():
     ap.add_argument("--batch-points-min", type=int, default=1000)
     ap.add_argument("--batch-points-max", type=int, default=64000)
     ap.add_argument("--cv-subdiv", type=int, default=7, help="icosphere subdivision of --workload cv3d")
-    ap.add_argument("--cv-paths", type=int, default=256, help="paths per point per iteration of --workload cv3d")
-    ap.add_argument("--cv-budget", type=float, default=20.0, help="GPU seconds per estimator of --workload cv3d")
-    ap.add_argument("--cv-npot", type=int, default=16)
-    ap.add_argument("--cv-nker", type=int, default=16)
-    ap.add_argument("--cv-sigma", type=float, default=1.0)
+    ap.add_argument("--cv-paths", type=int, default=256, help="plain paths per point per iteration of --workload cv3d")
+    ap.add_argument("--cv-budget", type=float, default=20.0, help="seconds per estimator of --workload cv3d")
+    ap.add_argument("--cv-near", type=float, default=3.0, help="near-field factor of the control-variate tables")
+    ap.add_argument("--no-time-to-rmse", action="store_true",
+                    help="skip the plain vs learned-CV time-to-RMSE leg of the default workload")
     ap.add_argument("--mrhs-subdiv", type=int, default=8, help="icosphere subdivision of --workload mrhs3d")
     ap.add_argument("--mrhs-rhs", type=int, default=64)
     ap.add_argument("--mrhs-points", type=int, default=1000000)

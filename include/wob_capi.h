@@ -352,6 +352,37 @@ int wob_solve_domain_cv(wob_scene scene, const wob_params *params, uint32_t n_po
                         double *sumsq, uint64_t *bounces, float *per_path, void *stream);
 
 /*
+ * Residual control variate for the single-layer Neumann estimators (no counterpart in the
+ * reference; it reuses the reference's forward walk, estimator.cuh:405-454, unchanged). The
+ * control variate is a density sigma~ that is constant on each stored triangle (device array
+ * [n_elems], storage order; e.g. the MLP below at the triangle centroids). The single-layer
+ * density solves sigma = c g + T sigma with c = +2 inside, -2 outside and T(x, y) = -c dG/dn_x
+ * (bie_models.cuh:262-316), so r = sigma - sigma~ solves the same equation with the data
+ * g + delta, delta = (T sigma~ - sigma~) / c, and u = S sigma~ + S r.
+ *
+ * wob_cv_residual_data: delta_j at the centroid of every stored triangle (device [n_elems]).
+ * wob_cv_potential: S sigma~ and its gradient at points (device [n][3] in, [n][4] out: u, grad u).
+ * Both sum over all triangles: the centroid rule beyond near_factor times a triangle's longest
+ * edge, the closed form of a uniformly charged triangle (Wilton et al. 1984) nearer. 3D scenes.
+ * wob_scene_clone: an independent copy of a scene (geometry, records, tables, volume cache).
+ * wob_scene_add_boundary_offsets: adds delta_j to the vertex values of stored element j (delta on
+ * the device when delta_on_device != 0, else on the host) and rebuilds the |g| sampling tables;
+ * synchronises the stream. The plain forward estimator on such a clone, plus S sigma~ from
+ * wob_cv_potential, estimates u; the residual's sampling weight shrinks with |sigma - sigma~|,
+ * which is where the variance reduction comes from.
+ * wob_scene_element_frames: (centroid, normal) of every stored element, the network's input there:
+ * device [n_elems][6] (2D scenes: (x, y, 0, nx, ny, 0)).
+ */
+int wob_cv_residual_data(wob_scene scene, const float *sigma, int domain, float near_factor, float *delta,
+                         void *stream);
+int wob_cv_potential(wob_scene scene, const float *sigma, float near_factor, const float *points,
+                     uint32_t n_points, float *out, void *stream);
+int wob_scene_clone(wob_scene scene, wob_scene *out);
+int wob_scene_add_boundary_offsets(wob_scene scene, const float *delta, uint32_t n_elems, int delta_on_device,
+                                   void *stream);
+int wob_scene_element_frames(wob_scene scene, float *out, void *stream);
+
+/*
  * Fourier-feature MLP trained with the engine's own CUDA kernels: (x, n) in R^6 ->
  * [sin, cos](2 pi B (x, n)) with B n_freq x 6 ~ N(0, freq_sigma^2) -> hidden_layers x (64, SiLU)
  * -> out_dim. 2 n_freq must be 64. Parameters in FP32 (Adam master copy); every GEMM runs on
@@ -371,6 +402,22 @@ int wob_mlp_gradient(wob_mlp mlp, const float *inputs, const float *targets, uin
                      float *loss, void *stream);
 int wob_mlp_adam_step(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, float lr,
                       float *loss, void *stream);
+/*
+ * wob_mlp_train: `steps` Adam steps (b1 0.9, b2 0.999, eps 1e-8; learning rate lr with a cosine
+ * decay to 0 over the steps) on batches of `batch` rows drawn uniformly with replacement from the
+ * n training rows (inputs [n][6], targets [n][out_dim], device) by Philox4x32-10 keyed with
+ * `seed`. The loop runs on the device: one step (batch draw, forward, backward, Adam update) is
+ * captured once as a CUDA graph and replayed, so no host work happens per step; for 4 hidden
+ * layers and 32 frequencies the step is one fused kernel with the network in shared memory and a
+ * block-ordered (deterministic) gradient sum. loss_history (device [steps] or NULL) receives each
+ * step's batch loss. Ordered after the caller's stream; returns when the last step has run.
+ * wob_mlp_gradient_fused: the gradient and loss that one fused step computes, for the given rows
+ * in order (no batch draw, no update) -- the fused step's check against wob_mlp_gradient.
+ */
+int wob_mlp_train(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, uint32_t steps,
+                  uint32_t batch, float lr, uint64_t seed, float *loss_history, void *stream);
+int wob_mlp_gradient_fused(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, float *grad,
+                           float *loss, void *stream);
 
 /*
  * All hits of the infinite lines origin + t dir (the query of scene.cuh:483-486 / 787-790).

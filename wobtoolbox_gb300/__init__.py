@@ -216,6 +216,29 @@ class SceneHost:
         o = self.element_order
         return (v[o], nrm[o], bv[o], ty[o], None if al is None else al[o])
 
+    def clone_with_offsets(self, delta, stream=None) -> "SceneHost":
+        """An independent copy of this scene whose stored element j has delta[j] added to each of
+        its vertex boundary values (delta: device tensor or host array, [n_elems], storage order),
+        with the |g| sampling tables rebuilt (wob_scene_clone + wob_scene_add_boundary_offsets)."""
+        lib = load()
+        h = C.c_void_p()
+        check(lib.wob_scene_clone(self._h, C.byref(h)))
+        obj = SceneHost.__new__(SceneHost)
+        obj._h, obj.dim, obj.n_elems, obj.n_rhs = h, self.dim, self.n_elems, 0
+        obj.element_order = self.element_order.copy()
+        on_dev = hasattr(delta, "is_cuda") and delta.is_cuda
+        d_host = (delta.detach().cpu().numpy() if on_dev else np.asarray(delta)).astype(np.float32).reshape(-1)
+        if on_dev:
+            check(lib.wob_scene_add_boundary_offsets(h, _ptr(delta), self.n_elems, 1, _stream_ptr(stream)))
+        else:
+            d_c = np.ascontiguousarray(d_host)
+            check(lib.wob_scene_add_boundary_offsets(h, d_c.ctypes.data, self.n_elems, 0, _stream_ptr(stream)))
+        v, nrm, bv, ty, al = self._host
+        bv2 = bv.copy()
+        bv2[self.element_order] = bv[self.element_order] + d_host[:, None]  # the same float32 adds
+        obj._host = (v, nrm, bv2, ty, al)
+        return obj
+
     def info(self) -> dict:
         inf = _capi.wob_scene_info()
         check(load().wob_scene_get_info(self._h, C.byref(inf)))

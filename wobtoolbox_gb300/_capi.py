@@ -30,9 +30,11 @@ EXPORTED = [
     "wob_debug_boundary_paths", "wob_solve_domain_host_noalloc", "wob_noalloc_max_points",
     "wob_autotune_domain", "wob_tunable_variant", "wob_set_domain_config", "wob_get_domain_config",
     "wob_batch_create", "wob_batch_solve", "wob_batch_destroy", "wob_solve_unknown_boundary",
-    "wob_scene_set_control_variate", "wob_solve_domain_cv", "wob_mlp_create", "wob_mlp_destroy",
+    "wob_scene_set_control_variate", "wob_solve_domain_cv", "wob_cv_residual_data", "wob_cv_potential",
+    "wob_scene_clone", "wob_scene_add_boundary_offsets", "wob_scene_element_frames", "wob_mlp_create", "wob_mlp_destroy",
     "wob_mlp_num_params", "wob_mlp_get_params", "wob_mlp_set_params", "wob_mlp_forward", "wob_mlp_gradient",
-    "wob_mlp_adam_step", "wob_scene_set_rhs", "wob_solve_domain_multi", "wob_solve_unknown_boundary_multi",
+    "wob_mlp_adam_step", "wob_mlp_train", "wob_mlp_gradient_fused", "wob_scene_set_rhs", "wob_solve_domain_multi",
+    "wob_solve_unknown_boundary_multi",
     "wob_scene_set_rhs_control_variate", "wob_solve_domain_multi_cv", "wob_scene_create_device",
     "wob_vpl_paths", "wob_vpl_aggregate", "wob_solve_wos", "wob_closest_point",
 ]
@@ -104,6 +106,11 @@ def load() -> C.CDLL:
         "wob_batch_destroy": (C.c_int, [vp]),
         "wob_solve_unknown_boundary": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp]),
         "wob_scene_set_control_variate": (C.c_int, [vp, vp, u32]),
+        "wob_cv_residual_data": (C.c_int, [vp, vp, C.c_int, f32, vp, vp]),
+        "wob_cv_potential": (C.c_int, [vp, vp, f32, vp, u32, vp, vp]),
+        "wob_scene_clone": (C.c_int, [vp, P(vp)]),
+        "wob_scene_add_boundary_offsets": (C.c_int, [vp, vp, u32, C.c_int, vp]),
+        "wob_scene_element_frames": (C.c_int, [vp, vp, vp]),
         "wob_solve_domain_cv": (C.c_int, [vp, P(wob_params), u32, u32, vp, u32, vp, vp, vp, vp, vp]),
         "wob_mlp_create": (C.c_int, [u32, u32, u32, f32, u64, P(vp)]),
         "wob_mlp_destroy": (C.c_int, [vp]),
@@ -113,6 +120,8 @@ def load() -> C.CDLL:
         "wob_mlp_forward": (C.c_int, [vp, vp, u32, vp, vp]),
         "wob_mlp_gradient": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
         "wob_mlp_adam_step": (C.c_int, [vp, vp, vp, u32, f32, vp, vp]),
+        "wob_mlp_train": (C.c_int, [vp, vp, vp, u32, u32, u32, f32, u64, vp, vp]),
+        "wob_mlp_gradient_fused": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
         "wob_scene_set_rhs": (C.c_int, [vp, vp, u32]),
         "wob_solve_domain_multi": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp, vp, vp, vp]),
         "wob_solve_unknown_boundary_multi": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp,

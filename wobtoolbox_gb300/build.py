@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -16,7 +17,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine())  # objects per host architecture
 LIB = os.path.join(OUT, "libwob_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
@@ -24,7 +25,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["capi.cu", "kernels_dispatch.cu", "k2_generic_domain.cu", "k2_generic_boundary.cu", "k3_generic_domain.cu",
               "k3_generic_boundary.cu", "k2_fast.cu", "k3_fast.cu", "k_batch.cu", "k_cv.cu",
               "k2_multi_rhs.cu", "k3_multi_rhs.cu", "mlp.cu", "scene_build_gpu.cu",
-              "k_vpl.cu", "k_wos.cu", "k_sl.cu"]
+              "k_vpl.cu", "k_wos.cu", "k_sl.cu", "k_cv_tables.cu", "mlp_train.cu"]
+# Units outside the bit-exact walk, compiled with FMA contraction: the control-variate tables
+# (checked against a float64 restatement with a tolerance, not path for path).
+CONTRACTED_SOURCES = {"k_cv_tables.cu"}
 CPP_SOURCES = ["scene_build.cpp"]
 
 
@@ -95,9 +99,17 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + proc.stdout + proc.stderr)
 
 
-def cu_flags(extra: list[str] | None = None) -> list[str]:
-    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
-                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE] + (extra or [])
+def cu_flags(extra: list[str] | None = None, contract: bool = False) -> list[str]:
+    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=true" if contract else "-fmad=false",
+                   "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE] + (extra or [])
+
+
+def _obj_stale(obj: str, src: str, headers: list[str]) -> bool:
+    """An object is rebuilt when it is missing or older than its source, a header or this file."""
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in [src] + headers)
 
 
 def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
@@ -112,17 +124,24 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     cxx = os.environ.get("CXX", "g++")
     jobs = []
     objs = []
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))]
+    headers += [os.path.join(INCLUDE, "wob_capi.h"), os.path.abspath(__file__)]
     for src in CU_SOURCES:
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(obj)
+        if not (force or ptxas_info) and not _obj_stale(obj, os.path.join(CSRC, src), headers):
+            continue
         extra = ["-Xptxas", "-v"] if ptxas_info else []
-        jobs.append([nvcc] + cu_flags(extra) + ["-c", os.path.join(CSRC, src), "-o", obj])
+        jobs.append([nvcc] + cu_flags(extra, contract=src in CONTRACTED_SOURCES) +
+                    ["-c", os.path.join(CSRC, src), "-o", obj])
     for src in CPP_SOURCES:
         obj = os.path.join(BUILD, src.replace(".cpp", ".o"))
         objs.append(obj)
+        if not force and not _obj_stale(obj, os.path.join(CSRC, src), headers):
+            continue
         jobs.append([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c",
                      os.path.join(CSRC, src), "-o", obj])
-    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         futs = [ex.submit(subprocess.run, j, capture_output=True, text=True) for j in jobs]
         for j, f in zip(jobs, futs):
             proc = f.result()

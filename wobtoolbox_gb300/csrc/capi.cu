@@ -890,6 +890,170 @@ int wob_batch_destroy(wob_batch b) {
     return WOB_OK;
 }
 
+// ---- residual control variate (k_cv_tables.cu)
+
+namespace {
+// Copies a device buffer of the scene into a new allocation (empty buffers stay empty).
+cudaError_t clone_buf(DevBuf &dst, const DevBuf &src) {
+    dst.release();
+    if (!src.ptr || src.bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&dst.ptr, src.bytes);
+    if (e != cudaSuccess) return e;
+    dst.bytes = src.bytes;
+    return cudaMemcpy(dst.ptr, src.ptr, src.bytes, cudaMemcpyDeviceToDevice);
+}
+
+int scene_clone_impl(wob_scene src, wob_scene *out) {
+    if (!src || !out) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and out are required");
+    *out = nullptr;
+    DeviceGuard g(src->device);
+    std::unique_ptr<wob_scene_s> owner(new wob_scene_s());
+    wob_scene_s *s = owner.get();
+    s->device = src->device;
+    s->host = src->host;
+    s->has_volume = src->has_volume;
+    s->area_G = src->area_G;
+    s->bv_G = src->bv_G;
+    s->vol_res = src->vol_res;
+    s->vol_n = src->vol_n;
+    s->vol_G = src->vol_G;
+    s->vol_size = src->vol_size;
+    s->all_dirichlet = src->all_dirichlet;
+    cudaError_t e = cudaSuccess;
+    const std::pair<DevBuf *, const DevBuf *> bufs[] = {
+        {&s->elems, &src->elems}, {&s->elem_aux, &src->elem_aux}, {&s->isect, &src->isect}, {&s->nodes, &src->nodes},
+        {&s->area_cdf, &src->area_cdf}, {&s->area_guide, &src->area_guide}, {&s->bv_cdf, &src->bv_cdf},
+        {&s->bv_guide, &src->bv_guide}, {&s->vol_values, &src->vol_values}, {&s->vol_cdf, &src->vol_cdf},
+        {&s->vol_guide, &src->vol_guide}, {&s->lg_bins, &src->lg_bins}, {&s->lg_off, &src->lg_off},
+        {&s->lg_ent, &src->lg_ent}};
+    for (const auto &b : bufs)
+        if ((e = clone_buf(*b.first, *b.second)) != cudaSuccess) {
+            s->release_all();
+            return fail_cuda(e, "copying the scene");
+        }
+    const uint32_t zero = 0;
+    if ((e = upload(s->err, &zero, 4)) != cudaSuccess) {
+        s->release_all();
+        return fail_cuda(e, "allocating the error word");
+    }
+    *out = owner.release();
+    return WOB_OK;
+}
+
+int scene_add_boundary_offsets_impl(wob_scene s, const float *delta, uint32_t n, int on_device, void *stream) {
+    if (!s || !delta) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and delta are required");
+    if (n != s->host.n) return fail(WOB_ERR_INVALID_ARGUMENT, "need one offset per element");
+    if (s->host.elems.empty()) return fail(WOB_ERR_UNSUPPORTED, "the scene keeps no host records (built on the device)");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<float> d(n);
+    cudaError_t e;
+    if (on_device) {
+        if ((e = cudaMemcpyAsync(d.data(), delta, (size_t)n * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return fail_cuda(e, "reading the offsets");
+    } else {
+        std::memcpy(d.data(), delta, (size_t)n * 4);
+    }
+    for (uint32_t i = 0; i < n; i++)
+        if (!(d[i] == d[i]) || d[i] > 3.0e38f || d[i] < -3.0e38f)
+            return fail(WOB_ERR_INVALID_ARGUMENT, "offsets must be finite");
+    wobgb::HostScene &h = s->host;
+    const int EF = wobgb::elem_record_floats(h.dim);
+    const int first = h.dim == 2 ? 6 : 12;
+    for (uint32_t i = 0; i < n; i++)
+        for (int k = 0; k < h.dim; k++) h.elems[(size_t)i * EF + first + k] = h.elems[(size_t)i * EF + first + k] + d[i];
+    wobgb::rebuild_bv_tables(h);
+    s->bv_G = (uint32_t)(h.bv_guide.size() / 4);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess ||
+        (e = cudaMemcpy(s->elems.ptr, h.elems.data(), h.elems.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = upload(s->bv_cdf, h.bv_cdf.data(), h.bv_cdf.size() * 4)) != cudaSuccess ||
+        (e = upload(s->bv_guide, h.bv_guide.data(), h.bv_guide.size() * 4)) != cudaSuccess)
+        return fail_cuda(e, "uploading the new boundary values");
+    return WOB_OK;
+}
+
+// Triangle sources of sigma~ in a scratch allocation freed on return.
+struct CvSources {
+    DevBuf src, near2;
+};
+int cv_sources(wob_scene s, const float *sigma, float near_factor, CvSources &cs, cudaStream_t st) {
+    if (s->host.dim != 3) return fail(WOB_ERR_UNSUPPORTED, "the control-variate tables are implemented for 3D scenes");
+    if (!sigma) return fail(WOB_ERR_INVALID_ARGUMENT, "sigma is required");
+    if (!(near_factor >= 0.0f) || !(near_factor < 1e6f)) return fail(WOB_ERR_INVALID_ARGUMENT, "near_factor must be in [0, 1e6)");
+    const size_t n = s->host.n;
+    cudaError_t e;
+    if ((e = cudaMalloc(&cs.src.ptr, n * 16)) != cudaSuccess || (e = cudaMalloc(&cs.near2.ptr, n * 4)) != cudaSuccess)
+        return fail_cuda(e, "allocating the control-variate sources");
+    cs.src.bytes = n * 16;
+    cs.near2.bytes = n * 4;
+    e = wobgb::launch_cv_sources(s->view<3>(), sigma, near_factor, (float4 *)cs.src.ptr, (float *)cs.near2.ptr, st);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate sources");
+}
+}  // namespace
+
+int wob_scene_element_frames(wob_scene s, float *out, void *stream) {
+    if (!s || !out) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and out are required");
+    DeviceGuard g(s->device);
+    cudaError_t e = s->host.dim == 2 ? wobgb::launch_element_frames<2>(s->view<2>(), out, (cudaStream_t)stream)
+                                     : wobgb::launch_element_frames<3>(s->view<3>(), out, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the element frames");
+}
+
+int wob_scene_clone(wob_scene scene, wob_scene *out) {
+    return guarded([&] { return scene_clone_impl(scene, out); });
+}
+
+int wob_scene_add_boundary_offsets(wob_scene scene, const float *delta, uint32_t n_elems, int delta_on_device,
+                                   void *stream) {
+    return guarded([&] { return scene_add_boundary_offsets_impl(scene, delta, n_elems, delta_on_device, stream); });
+}
+
+int wob_cv_residual_data(wob_scene s, const float *sigma, int domain, float near_factor, float *delta, void *stream) {
+    return guarded([&] {
+        if (!s || !delta) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and delta are required");
+        if (domain != WOB_INTERIOR_DOMAIN && domain != WOB_EXTERIOR_DOMAIN)
+            return fail(WOB_ERR_INVALID_ARGUMENT, "domain must be 0 (interior) or 1 (exterior)");
+        DeviceGuard g(s->device);
+        cudaStream_t st = (cudaStream_t)stream;
+        CvSources cs;
+        int r = cv_sources(s, sigma, near_factor, cs, st);
+        if (r == WOB_OK) {
+            // c = domain_type_coefficient / integral_free_term(1/2) (bie_models.cuh:66-78)
+            const float c = domain == WOB_INTERIOR_DOMAIN ? 2.0f : -2.0f;
+            cudaError_t e = wobgb::launch_cv_residual(s->view<3>(), (const float4 *)cs.src.ptr, (const float *)cs.near2.ptr,
+                                                      sigma, c, delta, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) r = fail_cuda(e, "computing the residual data");
+        }
+        cs.src.release();
+        cs.near2.release();
+        return r;
+    });
+}
+
+int wob_cv_potential(wob_scene s, const float *sigma, float near_factor, const float *points, uint32_t n_points,
+                     float *out, void *stream) {
+    return guarded([&] {
+        if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+        if (n_points == 0) return (int)WOB_OK;
+        if (!points || !out) return fail(WOB_ERR_INVALID_ARGUMENT, "points and out are required");
+        DeviceGuard g(s->device);
+        cudaStream_t st = (cudaStream_t)stream;
+        CvSources cs;
+        int r = cv_sources(s, sigma, near_factor, cs, st);
+        if (r == WOB_OK) {
+            cudaError_t e = wobgb::launch_cv_potential(s->view<3>(), (const float4 *)cs.src.ptr, (const float *)cs.near2.ptr,
+                                                       sigma, points, n_points, out, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) r = fail_cuda(e, "computing the control-variate potential");
+        }
+        cs.src.release();
+        cs.near2.release();
+        return r;
+    });
+}
+
 int wob_scene_set_control_variate(wob_scene s, const float *values, uint32_t n) {
     if (!s || !values) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and values are required");
     if (n != s->host.n) return fail(WOB_ERR_INVALID_ARGUMENT, "need one value per element");

@@ -50,6 +50,17 @@ cudaError_t launch_domain_cv_2d(const SceneView<2> &s, const WalkParams &p, cons
 cudaError_t launch_domain_cv_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                 double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                 cudaStream_t stream);
+// Learned control-variate tables (k_cv_tables.cu): per-triangle sources {centroid, sigma~ area}
+// and squared near radii; the residual Neumann data delta_j of each stored triangle; the
+// single-layer potential of sigma~ and its gradient at points ([n][4]); the (centroid, normal)
+// network input of every stored element ([n][6]).
+cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float4 *src, float *near2,
+                              cudaStream_t stream);
+cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
+                               float c_coef, float *delta, cudaStream_t stream);
+cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
+                                const float *pts, uint32_t n_points, float *out, cudaStream_t stream);
+template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream);
 // Shared error message of the C ABI (capi.cu).
 void set_last_error(const char *msg);
 

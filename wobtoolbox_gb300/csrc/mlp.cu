@@ -10,6 +10,7 @@
 
 #include "device_common.cuh"
 #include "launch.hpp"
+#include "mlp_train.hpp"
 
 #include <cuda_bf16.h>
 #include <cmath>
@@ -209,6 +210,54 @@ __global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g, 
     p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
 }
 
+// ---- device-driven training loop of networks the fused step does not cover (wob_mlp_train):
+// every per-step scalar lives in device memory, so one step is a fixed sequence of launches that
+// a CUDA graph replays. sched = {lr, 1 - b1^t, 1 - b2^t, step (as bits)}: the cosine schedule
+// and Adam's bias corrections of step s (t = adam_base + s + 1).
+__global__ void train_schedule_kernel(uint32_t *step, uint32_t steps, float lr0, uint32_t adam_base, float *sched) {
+    const uint32_t s = *step;
+    sched[0] = lr0 * 0.5f * (1.0f + cospif((float)s / (float)steps));
+    const float t = (float)(adam_base + s + 1u);
+    sched[1] = 1.0f - powf(0.9f, t);
+    sched[2] = 1.0f - powf(0.999f, t);
+    sched[3] = __uint_as_float(s);
+    *step = s + 1u;
+}
+
+// Batch of the step: indices drawn uniformly from [0, n) by Philox4x32-10 on (row, step, 0,
+// "tran") with the seed as key; inputs and targets gathered into xb, tb.
+__global__ void train_gather_kernel(const float *__restrict__ in, const float *__restrict__ tg, uint32_t n,
+                                    uint32_t out_dim, uint32_t batch, uint64_t seed, const float *__restrict__ sched,
+                                    float *__restrict__ xb, float *__restrict__ tb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= batch) return;
+    const uint32_t s = __float_as_uint(sched[3]);
+    const uint4 r = philox4x32_10(make_uint4(i, s, 0u, 0x7472616eu), (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint32_t idx = (uint32_t)(((uint64_t)r.x * n) >> 32);
+#pragma unroll
+    for (int k = 0; k < kFeatIn; k++) xb[(size_t)i * kFeatIn + k] = in[(size_t)idx * kFeatIn + k];
+    for (uint32_t k = 0; k < out_dim; k++) tb[(size_t)i * out_dim + k] = tg[(size_t)idx * out_dim + k];
+}
+
+__global__ void adam_sched_kernel(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                                  float *__restrict__ v, long n, const float *__restrict__ sched, float b1, float b2,
+                                  float eps) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float lr = sched[0], bc1 = sched[1], bc2 = sched[2];
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+__global__ void train_record_loss_kernel(const float *__restrict__ loss, const float *__restrict__ sched,
+                                         float *__restrict__ hist) {
+    hist[__float_as_uint(sched[3])] = *loss;
+}
+
 }  // namespace wobgb
 
 // ------------------------------------------------------------------------------------------
@@ -236,15 +285,57 @@ struct wob_mlp_s {
     float *phi = nullptr, *Z = nullptr, *H = nullptr, *Y = nullptr, *dY = nullptr, *dA = nullptr, *dZ = nullptr,
           *loss = nullptr;
     uint64_t adam_steps = 0;
+    // training-loop state (wob_mlp_train)
+    uint32_t train_cap = 0, partial_blocks = 0;
+    float *xb = nullptr, *tb = nullptr, *sched = nullptr, *partial = nullptr, *partial_loss = nullptr;
+    uint32_t *step = nullptr;
     std::mutex mu;
 
     uint32_t n_layers() const { return hidden + 1; }
     void free_ws() {
-        for (float **p : {&phi, &Z, &H, &Y, &dY, &dA, &dZ, &loss}) {
+        for (float **p : {&phi, &Z, &H, &Y, &dY, &dA, &dZ, &loss, &xb, &tb, &sched, &partial, &partial_loss}) {
             if (*p) cudaFree(*p);
             *p = nullptr;
         }
+        if (step) cudaFree(step);
+        step = nullptr;
         cap = 0;
+        train_cap = 0;
+        partial_blocks = 0;
+    }
+    // workspace of the unfused graph-replayed step
+    cudaError_t ensure_train(uint32_t batch) {
+        cudaError_t e = ensure(batch);
+        if (e != cudaSuccess) return e;
+        if (!sched && (e = cudaMalloc(&sched, 16)) != cudaSuccess) return e;
+        if (!step && (e = cudaMalloc(&step, 4)) != cudaSuccess) return e;
+        if (batch <= train_cap) return cudaSuccess;
+        for (float **p : {&xb, &tb}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        if ((e = cudaMalloc(&xb, (size_t)batch * wobgb::kFeatIn * 4)) != cudaSuccess ||
+            (e = cudaMalloc(&tb, (size_t)batch * out_dim * 4)) != cudaSuccess)
+            return e;
+        train_cap = batch;
+        return cudaSuccess;
+    }
+    // the fused step (mlp_train.cu) covers the 4-hidden-layer, 32-frequency network
+    bool fused_ok() const { return hidden == 4 && n_freq == 32 && out_dim <= 64; }
+    cudaError_t ensure_fused(uint32_t batch) {
+        cudaError_t e;
+        if (!step && (e = cudaMalloc(&step, 4)) != cudaSuccess) return e;
+        const uint32_t blocks = wobgb::fused_train_blocks(batch);
+        if (blocks <= partial_blocks) return cudaSuccess;
+        for (float **p : {&partial, &partial_loss}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        if ((e = cudaMalloc(&partial, (size_t)blocks * n_params * 4)) != cudaSuccess ||
+            (e = cudaMalloc(&partial_loss, (size_t)blocks * 4)) != cudaSuccess)
+            return e;
+        partial_blocks = blocks;
+        return wobgb::prepare_fused_train();
     }
     cudaError_t ensure(uint32_t n) {
         if (n <= cap) return cudaSuccess;
@@ -453,6 +544,92 @@ int wob_mlp_adam_step(wob_mlp m, const float *inputs, const float *targets, uint
         m->params, m->grad, m->adam_m, m->adam_v, m->n_params, lr, b1, b2, 1e-8f, bc1, bc2);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? WOB_OK : mfail_cuda(e, "Adam step");
+}
+
+int wob_mlp_gradient_fused(wob_mlp m, const float *inputs, const float *targets, uint32_t n, float *grad, float *loss,
+                           void *stream) {
+    if (!m || !inputs || !targets || !grad || n == 0)
+        return mfail(WOB_ERR_INVALID_ARGUMENT, "mlp, inputs, targets, grad and n > 0 are required");
+    if (!m->fused_ok()) return mfail(WOB_ERR_UNSUPPORTED, "the fused step needs 4 hidden layers, 32 frequencies and out_dim <= 64");
+    std::lock_guard<std::mutex> lock(m->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = m->ensure_fused(n);
+    if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
+    if ((e = cudaMemsetAsync(m->step, 0, 4, st)) != cudaSuccess) return mfail_cuda(e, "MLP step counter");
+    wobgb::FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, n, m->n_params, 0u, 0ull, m->step,
+                            m->partial, m->partial_loss};
+    e = wobgb::launch_fused_gradient(a, grad, loss, st);
+    return e == cudaSuccess ? WOB_OK : mfail_cuda(e, "fused MLP gradient");
+}
+
+int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t n, uint32_t steps, uint32_t batch,
+                  float lr, uint64_t seed, float *loss_history, void *stream) {
+    if (!m || !inputs || !targets || n == 0 || batch == 0)
+        return mfail(WOB_ERR_INVALID_ARGUMENT, "mlp, inputs, targets, n > 0 and batch > 0 are required");
+    if (!(lr > 0.0f) || !(lr < 1e3f)) return mfail(WOB_ERR_INVALID_ARGUMENT, "lr must be positive");
+    if (steps == 0) return WOB_OK;
+    std::lock_guard<std::mutex> lock(m->mu);
+    using namespace wobgb;
+    cudaStream_t user = (cudaStream_t)stream;
+    const bool fused = m->fused_ok();
+    cudaError_t e = fused ? m->ensure_fused(batch) : m->ensure_train(batch);
+    if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
+    // The step sequence is captured once into a CUDA graph on a private stream, ordered after the
+    // caller's stream by an event, and replayed `steps` times.
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (ev) cudaEventDestroy(ev);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMemsetAsync(m->step, 0, 4, user)) != cudaSuccess || (e = cudaEventRecord(ev, user)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(cs, ev, 0)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e, "preparing the training stream");
+    }
+    const uint32_t adam_base = (uint32_t)m->adam_steps;
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e, "capturing the training step");
+    }
+    cudaError_t e_body = cudaSuccess;
+    if (fused) {
+        FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, batch, m->n_params, 1u, seed, m->step,
+                         m->partial, m->partial_loss};
+        e_body = launch_fused_train_step(a, m->params, m->adam_m, m->adam_v, steps, lr, adam_base, loss_history, cs);
+    } else {
+        train_schedule_kernel<<<1, 1, 0, cs>>>(m->step, steps, lr, adam_base, m->sched);
+        train_gather_kernel<<<(batch + 127) / 128, 128, 0, cs>>>(inputs, targets, n, m->out_dim, batch, seed, m->sched,
+                                                                 m->xb, m->tb);
+        e_body = backward_impl(m, m->xb, m->tb, batch, cs);
+        adam_sched_kernel<<<(m->n_params + 255) / 256, 256, 0, cs>>>(m->params, m->grad, m->adam_m, m->adam_v,
+                                                                     m->n_params, m->sched, 0.9f, 0.999f, 1e-8f);
+        if (loss_history) train_record_loss_kernel<<<1, 1, 0, cs>>>(m->loss, m->sched, loss_history);
+    }
+    e = cudaStreamEndCapture(cs, &graph);
+    if (e_body != cudaSuccess || e != cudaSuccess || (e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e_body != cudaSuccess ? e_body : e, "building the training graph");
+    }
+    for (uint32_t i = 0; i < steps; i++)
+        if ((e = cudaGraphLaunch(exec, cs)) != cudaSuccess) {
+            cleanup();
+            return mfail_cuda(e, "launching a training step");
+        }
+    if ((e = cudaEventRecord(ev, cs)) != cudaSuccess || (e = cudaStreamWaitEvent(user, ev, 0)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(cs)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e, "finishing the training steps");
+    }
+    m->adam_steps += steps;
+    cleanup();
+    return WOB_OK;
 }
 
 }  // extern "C"

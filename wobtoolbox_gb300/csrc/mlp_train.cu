@@ -1,0 +1,361 @@
+// Fused training step of the Fourier-feature MLP (mlp.cu's network with 4 hidden layers): one
+// kernel runs the batch gather, the forward pass and the backward pass of 64 rows per block with
+// every weight and activation in shared memory and writes the block's gradient; a second kernel
+// sums the blocks' gradients in a fixed order (so a step is deterministic) and applies Adam; a
+// third advances the step counter. wob_mlp_train replays the three as a CUDA graph.
+//
+// Network and parameter layout as in mlp.cu: phi = [sin, cos](2 pi B v) (32 frequencies of the
+// 6 inputs), 4 hidden layers 64 -> 64 with SiLU, a linear 64 -> out_dim head; FP32 parameters,
+// for each layer W [out][in] row-major then b [out]. Every product runs on the BF16 tensor cores
+// (mma.sync m16n8k16, FP32 accumulation) with operands rounded to BF16 in shared memory, as in
+// mlp.cu; pre-activations are kept as BF16 for the SiLU derivative, bias gradients are summed in
+// FP32 from the FP32 products.
+//
+// Shared-memory operands are 32-bit words holding two BF16 values adjacent along the reduction
+// index (the m16n8k16 fragment layout), rows padded to 36 words so that the 8 x 4 words of a
+// fragment load fall in 32 distinct banks. For C[m][n] = sum_k A[m][k] B[k][n] the A operand is
+// stored [m][k/2] and the B operand [n][k/2]:
+//   forward  Z = A W^T:     A = activation [row][in],   B = W   [out][in]
+//   weights  dW = dZ^T A:   A = dZ^T [out][row],        B = A^T [in][row]
+//   inputs   dA = dZ W:     A = dZ   [row][out],        B = W^T [in][out]
+#include "../../include/wob_capi.h"
+
+#include "device_common.cuh"
+#include "launch.hpp"
+#include "mlp_train.hpp"
+
+#include <cuda_bf16.h>
+
+namespace wobgb {
+
+namespace {
+
+constexpr int kTM = 64;          // rows per block
+constexpr int kW = 64;           // layer width
+constexpr int kLd = 36;          // words per shared-memory row (32 pairs + 4 padding)
+constexpr int kMat = kW * kLd;   // words per 64 x 64 operand
+constexpr int kHidden = 4;
+constexpr int kLayers = kHidden + 1;
+constexpr int kIn = 6;
+constexpr int kThreads = 128;    // 4 warps x 16 rows
+constexpr int kLayerParams = kW * kW + kW;
+
+constexpr size_t kSmemWords = (size_t)(kLayers + kHidden + 1 + kLayers + kHidden + 2) * kMat;
+constexpr size_t kSmemFloats = 2 * kLayers * kW + kTM * kIn + kTM * kW + 4;
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
+    return (uint32_t)__bfloat16_as_ushort(l) | ((uint32_t)__bfloat16_as_ushort(h) << 16);
+}
+__device__ __forceinline__ float lo_of(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float hi_of(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// acc[j][.] += sum_k A[m0 + .][k] B[k][8 j + .] for one warp's 16 rows at m0; K = 64, N = 64.
+// Fragment c[0..3] of tile j: rows m0 + gid (c0, c1) and m0 + gid + 8 (c2, c3), columns
+// 8 j + 2 tig and 8 j + 2 tig + 1.
+__device__ __forceinline__ void warp_gemm(float acc[8][4], const uint32_t *A, const uint32_t *B, int m0, int gid,
+                                          int tig) {
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+        uint32_t a[4];
+        a[0] = A[(m0 + gid) * kLd + kk * 8 + tig];
+        a[1] = A[(m0 + gid + 8) * kLd + kk * 8 + tig];
+        a[2] = A[(m0 + gid) * kLd + kk * 8 + tig + 4];
+        a[3] = A[(m0 + gid + 8) * kLd + kk * 8 + tig + 4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            uint32_t b[2];
+            b[0] = B[(j * 8 + gid) * kLd + kk * 8 + tig];
+            b[1] = B[(j * 8 + gid) * kLd + kk * 8 + tig + 4];
+            mma16816(acc[j], a, b);
+        }
+    }
+}
+
+__device__ __forceinline__ void zero_acc(float acc[8][4]) {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) acc[j][r] = 0.0f;
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+__device__ __forceinline__ float silu_d(float z) {
+    const float s = 1.0f / (1.0f + expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+// BF16 value at (row, col) of an operand kept transposed, [col][row / 2] words.
+__device__ __forceinline__ void store_t(uint32_t *M, int row, int col, float v) {
+    reinterpret_cast<__nv_bfloat16 *>(M)[col * kLd * 2 + row] = __float2bfloat16_rn(v);
+}
+
+// Column sums over the warp's 16 rows of the FP32 values in acc (fragment layout of tile j),
+// added to dst[8 j + 2 tig (+1)] in shared memory.
+__device__ __forceinline__ void add_col_sums(float acc[8][4], float *dst, int lane, int tig) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float s0 = acc[j][0] + acc[j][2], s1 = acc[j][1] + acc[j][3];
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        }
+        if (lane < 4) {
+            atomicAdd(dst + j * 8 + 2 * tig, s0);
+            atomicAdd(dst + j * 8 + 2 * tig + 1, s1);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrainArgs g) {
+    extern __shared__ uint32_t smem[];
+    uint32_t *Wf = smem;                      // layer l: [out][in]
+    uint32_t *Wb = Wf + kLayers * kMat;       // layer l >= 1: [in][out] at index l - 1
+    uint32_t *act = Wb + kHidden * kMat;      // [row][in] of the layer being evaluated
+    uint32_t *actT = act + kMat;              // layer l's input: [in][row]
+    uint32_t *Zs = actT + kLayers * kMat;     // hidden layer l's pre-activation: [row][out]
+    uint32_t *dZ = Zs + kHidden * kMat;       // [row][out]
+    uint32_t *dZT = dZ + kMat;                // [out][row]
+    float *bias = reinterpret_cast<float *>(smem + kSmemWords);  // [5][64]
+    float *dbias = bias + kLayers * kW;                          // [5][64]
+    float *xin = dbias + kLayers * kW;                           // [64][6]
+    float *tgt = xin + kTM * kIn;                                // [64][64]
+    float *red = tgt + kTM * kW;                                 // loss per warp
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
+    const int m0 = warp * 16;
+    const int out_dim = (int)g.out_dim;
+    const uint32_t step = *g.step;
+
+    // weights in both layouts (rows of the head beyond out_dim are zero), biases, bias gradients
+    for (int l = 0; l < kLayers; l++) {
+        const int fo = l == kHidden ? out_dim : kW;
+        const float *Wl = g.params + (size_t)l * kLayerParams;
+        for (int idx = tid; idx < kW * 32; idx += kThreads) {
+            const int o = idx >> 5, p = idx & 31;
+            const float w0 = o < fo ? Wl[o * kW + 2 * p] : 0.0f, w1 = o < fo ? Wl[o * kW + 2 * p + 1] : 0.0f;
+            Wf[l * kMat + o * kLd + p] = pack2(w0, w1);
+            if (l >= 1) {  // [in = o][out pair p]
+                const float v0 = 2 * p < fo ? Wl[(2 * p) * kW + o] : 0.0f;
+                const float v1 = 2 * p + 1 < fo ? Wl[(2 * p + 1) * kW + o] : 0.0f;
+                Wb[(l - 1) * kMat + o * kLd + p] = pack2(v0, v1);
+            }
+        }
+        for (int o = tid; o < kW; o += kThreads) {
+            bias[l * kW + o] = o < fo ? Wl[fo * kW + o] : 0.0f;
+            dbias[l * kW + o] = 0.0f;
+        }
+    }
+    // the block's batch rows: Philox4x32-10 on (row, step, 0, "tran") keyed by the seed
+    for (int r = tid; r < kTM; r += kThreads) {
+        const uint32_t row = blockIdx.x * kTM + r;
+        const bool ok = row < g.batch;
+        uint32_t idx = row;
+        if (ok && g.gather) {
+            const uint4 h = philox4x32_10(make_uint4(row, step, 0u, 0x7472616eu), (uint32_t)g.seed,
+                                          (uint32_t)(g.seed >> 32));
+            idx = (uint32_t)(((uint64_t)h.x * g.n) >> 32);
+        }
+        for (int k = 0; k < kIn; k++) xin[r * kIn + k] = ok ? g.inputs[(size_t)idx * kIn + k] : 0.0f;
+        for (int k = 0; k < out_dim; k++) tgt[r * kW + k] = ok ? g.targets[(size_t)idx * out_dim + k] : 0.0f;
+    }
+    if (tid < 4) red[tid] = 0.0f;
+    __syncthreads();
+    // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t
+    for (int idx = tid; idx < kTM * 32; idx += kThreads) {
+        const int r = idx >> 5, f = idx & 31;
+        float t = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kIn; k++) t = t + g.freqs[f * kIn + k] * xin[r * kIn + k];
+        float s, c;
+        sincospi_own(2.0f * t, &s, &c);
+        reinterpret_cast<__nv_bfloat16 *>(act)[r * kLd * 2 + f] = __float2bfloat16_rn(s);
+        reinterpret_cast<__nv_bfloat16 *>(act)[r * kLd * 2 + 32 + f] = __float2bfloat16_rn(c);
+        store_t(actT, r, f, s);
+        store_t(actT, r, 32 + f, c);
+    }
+    __syncthreads();
+
+    // ---- forward: a warp reads and rewrites only its own 16 rows of act
+    float acc[8][4];
+    for (int l = 0; l < kHidden; l++) {
+        zero_acc(acc);
+        warp_gemm(acc, act, Wf + l * kMat, m0, gid, tig);
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int row = m0 + gid + 8 * hh, col = j * 8 + 2 * tig;
+                const float z0 = acc[j][2 * hh] + bias[l * kW + col], z1 = acc[j][2 * hh + 1] + bias[l * kW + col + 1];
+                Zs[l * kMat + row * kLd + (col >> 1)] = pack2(z0, z1);
+                const float h0 = silu_f(z0), h1 = silu_f(z1);
+                act[row * kLd + (col >> 1)] = pack2(h0, h1);
+                store_t(actT + (l + 1) * kMat, row, col, h0);
+                store_t(actT + (l + 1) * kMat, row, col + 1, h1);
+            }
+        __syncwarp();
+    }
+    // head: y = act W^T + b; loss sum (y - t)^2 / count; acc becomes dY = 2 (y - t) / count
+    {
+        zero_acc(acc);
+        warp_gemm(acc, act, Wf + kHidden * kMat, m0, gid, tig);
+        const float count = (float)g.batch * (float)out_dim;
+        float ls = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int row = m0 + gid + 8 * hh, col = j * 8 + 2 * tig;
+                const bool rok = blockIdx.x * kTM + row < g.batch;
+                float d0 = 0.0f, d1 = 0.0f;
+                if (rok && col < out_dim) d0 = acc[j][2 * hh] + bias[kHidden * kW + col] - tgt[row * kW + col];
+                if (rok && col + 1 < out_dim)
+                    d1 = acc[j][2 * hh + 1] + bias[kHidden * kW + col + 1] - tgt[row * kW + col + 1];
+                ls += d0 * d0 + d1 * d1;
+                acc[j][2 * hh] = 2.0f * d0 / count;
+                acc[j][2 * hh + 1] = 2.0f * d1 / count;
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+        if (lane == 0) red[warp] = ls / count;
+    }
+    // ---- backward: at the top of each iteration acc holds dL/dZ_l for this warp's rows (FP32)
+    for (int l = kHidden; l >= 0; l--) {
+        add_col_sums(acc, dbias + l * kW, lane, tig);
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int row = m0 + gid + 8 * hh, col = j * 8 + 2 * tig;
+                dZ[row * kLd + (col >> 1)] = pack2(acc[j][2 * hh], acc[j][2 * hh + 1]);
+                store_t(dZT, row, col, acc[j][2 * hh]);
+                store_t(dZT, row, col + 1, acc[j][2 * hh + 1]);
+            }
+        __syncthreads();
+        const int fo = l == kHidden ? out_dim : kW;
+        // weight gradient dW[o][i] = sum_r dZ[r][o] act_l[r][i]: warp w takes o in [16 w, 16 w + 16)
+        if (m0 < fo) {
+            float wacc[8][4];
+            zero_acc(wacc);
+            warp_gemm(wacc, dZT, actT + l * kMat, m0, gid, tig);
+            float *dst = g.partial + (size_t)blockIdx.x * g.n_params + (size_t)l * kLayerParams;
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int o = m0 + gid + 8 * hh, i = j * 8 + 2 * tig;
+                    if (o < fo)
+                        *reinterpret_cast<float2 *>(dst + o * kW + i) = make_float2(wacc[j][2 * hh], wacc[j][2 * hh + 1]);
+                }
+        }
+        if (l == 0) break;
+        // input gradient dA = dZ W_l (this warp's rows), then dZ_{l-1} = dA silu'(Z_{l-1})
+        zero_acc(acc);
+        warp_gemm(acc, dZ, Wb + (l - 1) * kMat, m0, gid, tig);
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int row = m0 + gid + 8 * hh, col = j * 8 + 2 * tig;
+                const uint32_t zw = Zs[(l - 1) * kMat + row * kLd + (col >> 1)];
+                acc[j][2 * hh] *= silu_d(lo_of(zw));
+                acc[j][2 * hh + 1] *= silu_d(hi_of(zw));
+            }
+        __syncthreads();  // every warp is done reading dZ^T before it is overwritten
+    }
+    __syncthreads();
+    // the block's bias gradients and loss
+    float *dst = g.partial + (size_t)blockIdx.x * g.n_params;
+    for (int l = 0; l < kLayers; l++) {
+        const int fo = l == kHidden ? out_dim : kW;
+        for (int o = tid; o < fo; o += kThreads) dst[(size_t)l * kLayerParams + fo * kW + o] = dbias[l * kW + o];
+    }
+    if (tid == 0) g.partial_loss[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+}
+
+// Sums the blocks' gradients (in block order) and applies Adam with the cosine schedule of the
+// current step; block 0 records the step's loss.
+__global__ void mlp_reduce_adam_kernel(float *__restrict__ p, float *__restrict__ m, float *__restrict__ v,
+                                       const float *__restrict__ partial, const float *__restrict__ partial_loss,
+                                       uint32_t n_blocks, uint32_t n_params, const uint32_t *__restrict__ step,
+                                       uint32_t steps, float lr0, uint32_t adam_base, float *__restrict__ loss_hist) {
+    const uint32_t s = *step;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_params) {
+        float gsum = 0.0f;
+        for (uint32_t b = 0; b < n_blocks; b++) gsum += partial[(size_t)b * n_params + i];
+        const float lr = lr0 * 0.5f * (1.0f + cospif((float)s / (float)steps));
+        const float t = (float)(adam_base + s + 1u);
+        const float bc1 = 1.0f - powf(0.9f, t), bc2 = 1.0f - powf(0.999f, t);
+        const float mi = 0.9f * m[i] + 0.1f * gsum;
+        const float vi = 0.999f * v[i] + 0.001f * gsum * gsum;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+    }
+    if (loss_hist && blockIdx.x == 0 && threadIdx.x == 0) {
+        float l = 0.0f;
+        for (uint32_t b = 0; b < n_blocks; b++) l += partial_loss[b];
+        loss_hist[s] = l;
+    }
+}
+
+__global__ void mlp_step_advance_kernel(uint32_t *step) { *step += 1u; }
+
+__global__ void mlp_reduce_grad_kernel(const float *__restrict__ partial, const float *__restrict__ partial_loss,
+                                       uint32_t n_blocks, uint32_t n_params, float *__restrict__ grad,
+                                       float *__restrict__ loss) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_params) {
+        float gsum = 0.0f;
+        for (uint32_t b = 0; b < n_blocks; b++) gsum += partial[(size_t)b * n_params + i];
+        grad[i] = gsum;
+    }
+    if (loss && blockIdx.x == 0 && threadIdx.x == 0) {
+        float l = 0.0f;
+        for (uint32_t b = 0; b < n_blocks; b++) l += partial_loss[b];
+        *loss = l;
+    }
+}
+
+}  // namespace
+
+size_t fused_train_smem_bytes() { return kSmemWords * 4 + kSmemFloats * 4; }
+uint32_t fused_train_blocks(uint32_t batch) { return (batch + kTM - 1) / kTM; }
+
+cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, float *adam_m, float *adam_v,
+                                    uint32_t steps, float lr, uint32_t adam_base, float *loss_hist,
+                                    cudaStream_t stream) {
+    const uint32_t blocks = fused_train_blocks(a.batch);
+    mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
+    mlp_reduce_adam_kernel<<<(a.n_params + 255) / 256, 256, 0, stream>>>(params, adam_m, adam_v, a.partial,
+                                                                         a.partial_loss, blocks, a.n_params, a.step,
+                                                                         steps, lr, adam_base, loss_hist);
+    mlp_step_advance_kernel<<<1, 1, 0, stream>>>(a.step);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused_gradient(const FusedTrainArgs &a, float *grad, float *loss, cudaStream_t stream) {
+    const uint32_t blocks = fused_train_blocks(a.batch);
+    mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
+    mlp_reduce_grad_kernel<<<(a.n_params + 255) / 256, 256, 0, stream>>>(a.partial, a.partial_loss, blocks, a.n_params,
+                                                                         grad, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_fused_train() {
+    return cudaFuncSetAttribute(mlp_train_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_train_smem_bytes());
+}
+
+}  // namespace wobgb

@@ -1,0 +1,34 @@
+// Fused MLP training step (mlp_train.cu), used by wob_mlp_train for the 4-hidden-layer network.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wobgb {
+
+struct FusedTrainArgs {
+    const float *params;   // [n_params], mlp.cu's layout
+    const float *freqs;    // [32][6]
+    const float *inputs;   // [n][6] training rows
+    const float *targets;  // [n][out_dim]
+    uint32_t n, out_dim, batch, n_params;
+    uint32_t gather;       // 1: rows drawn by Philox from the n rows; 0: row r of the batch is row r
+    uint64_t seed;
+    uint32_t *step;        // device step counter (batch draws and the learning-rate schedule)
+    float *partial;        // [blocks][n_params]: each block's gradient
+    float *partial_loss;   // [blocks]
+};
+
+size_t fused_train_smem_bytes();
+uint32_t fused_train_blocks(uint32_t batch);
+cudaError_t prepare_fused_train();
+// One step: fused forward/backward, block-ordered gradient sum + Adam (cosine learning rate from
+// lr over `steps`; bias corrections at step adam_base + s + 1), step counter + 1.
+cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, float *adam_m, float *adam_v,
+                                    uint32_t steps, float lr, uint32_t adam_base, float *loss_hist,
+                                    cudaStream_t stream);
+// The fused kernel's gradient and loss of one batch, summed over blocks into grad / loss (no update).
+cudaError_t launch_fused_gradient(const FusedTrainArgs &a, float *grad, float *loss, cudaStream_t stream);
+
+}  // namespace wobgb

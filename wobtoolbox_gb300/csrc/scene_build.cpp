@@ -506,4 +506,22 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
     return "";
 }
 
+void rebuild_bv_tables(HostScene &s) {
+    const int EF = elem_record_floats(s.dim);
+    std::vector<float> bvw(s.n);
+    for (uint32_t i = 0; i < s.n; i++) {
+        const float *r = s.elems.data() + (size_t)i * EF;
+        if (s.dim == 2) {
+            bvw[i] = r[10] * (std::fabs(r[6]) + std::fabs(r[7])) / 2.0f;
+        } else {
+            const float area = s.elem_aux[(size_t)i * kElemAux3Floats + 3];
+            bvw[i] = area * (std::fabs(r[12]) + std::fabs(r[13]) + std::fabs(r[14])) / 3.0f;
+        }
+    }
+    kahan_cdf(bvw, s.bv_cdf, s.total_bv);
+    s.bv_valid = s.total_bv > 0.0f && std::isfinite(s.total_bv);
+    if (s.bv_valid) s.bv_guide = build_guide(s.bv_cdf);
+    else s.bv_guide.assign(4, 0u);
+}
+
 }  // namespace wobgb

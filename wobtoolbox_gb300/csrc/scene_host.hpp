@@ -91,6 +91,10 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
                              const float *bvals, const float *alphas, const int32_t *types,
                              HostScene &out);
 
+// Recomputes the |g| sampling weights, CDF, guide table, total and validity from the boundary
+// values in the stored element records (after the values changed).
+void rebuild_bv_tables(HostScene &s);
+
 // Guide table of a nondecreasing CDF with G = min(n, 2^22) entries of 4 words each:
 // {lo, hi, bits(cdf[lo]), bits(cdf[lo + 1])}, where lo is the first index whose CDF value reaches
 // (j - 1/2)/G and hi the lo of entry j + 2 (n - 1 for the last two). See cdf_search in

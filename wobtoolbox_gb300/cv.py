@@ -61,6 +61,14 @@ class MLP:
         check(load().wob_mlp_adam_step(self._h, _ptr(inputs), _ptr(targets), int(n), float(lr), _ptr(loss),
                                        _stream_ptr(stream)))
 
+    def train(self, inputs, targets, n: int, steps: int, batch: int, lr: float, seed: int = 0, loss_history=None,
+              stream=None) -> None:
+        """`steps` Adam steps on the device (wob_mlp_train): cosine learning-rate decay, batches drawn
+        on the device, the step replayed as one CUDA graph."""
+        from . import _ptr, _stream_ptr
+        check(load().wob_mlp_train(self._h, _ptr(inputs), _ptr(targets), int(n), int(steps), int(batch), float(lr),
+                                   int(seed), _ptr(loss_history), _stream_ptr(stream)))
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             load().wob_mlp_destroy(self._h)
@@ -143,25 +151,15 @@ def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256
         z = torch.zeros(n_train, 1, device=dev)
         x = torch.cat([d["p"], z, d["n"], z], dim=1).contiguous()
     mlp = MLP(32, 4, 1, freq_sigma, seed)
-    loss = torch.zeros(1, dtype=torch.float32, device=dev)
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(seed)
+    loss_hist = torch.zeros(steps, dtype=torch.float32, device=dev)
+    labels = labels.contiguous()
     t1 = time.perf_counter()
-    hist = []
-    for it in range(steps):
-        idx = torch.randint(0, n_train, (batch,), device=dev, generator=gen)
-        xb = x[idx].contiguous()
-        yb = labels[idx].contiguous()
-        cur_lr = lr * 0.5 * (1 + np.cos(np.pi * it / steps))
-        mlp.adam_step(xb, yb, batch, cur_lr, loss)
-        if log_every and (it % log_every == 0 or it == steps - 1):
-            torch.cuda.synchronize()
-            hist.append((it, float(loss.item())))
-            loss.zero_()
-        elif not log_every:
-            loss.zero_()
+    mlp.train(x, labels, n_train, steps, batch, lr, seed=seed, loss_history=loss_hist)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
+    lh = loss_hist.cpu().numpy()
+    every = log_every or max(1, steps // 20)
+    hist = [(int(i), float(lh[i])) for i in range(0, steps, every)] + [(steps - 1, float(lh[-1]))]
     info = dict(n_train=n_train, train_paths=train_paths, steps=steps, batch=batch, t_labels_s=t_labels,
                 t_train_s=t_train, label_noise_var=float(label_var.mean().item()), history=hist,
                 label_bounces=int(b.item()))
@@ -236,6 +234,46 @@ def element_cv_table(mlp: MLP, scene, device=None) -> np.ndarray:
     torch.cuda.synchronize()
     o = out.cpu().numpy()
     return o[:, 0].copy() if mlp.out_dim == 1 else o
+
+
+def centroid_inputs(scene, device=None):
+    """(centroid, normal) of every stored element, the network's input there: device tensor [n, 6]
+    (2D scenes padded with zeros), storage order (wob_scene_element_frames)."""
+    import torch
+    from . import _ptr
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    out = torch.empty(scene.n_elems, 6, dtype=torch.float32, device=dev)
+    check(load().wob_scene_element_frames(scene.handle, _ptr(out), None))
+    return out
+
+
+def residual_control_variate(scene, mlp: MLP, domain: int, near_factor: float = 3.0, stream=None):
+    """The residual control variate of a single-layer Neumann problem (wob_cv_residual_data):
+    sigma~ = the network at every stored triangle's centroid, constant on the triangle; returns
+    (residual scene, sigma~) where the residual scene is a copy of `scene` whose Neumann data
+    carries the offsets delta = (T sigma~ - sigma~) / c. The forward estimator on the residual
+    scene plus control_variate_potential(sigma~) estimates u."""
+    import torch
+    from . import _ptr, _stream_ptr
+    x = centroid_inputs(scene)
+    n = scene.n_elems
+    sigma = torch.zeros(n, mlp.out_dim, dtype=torch.float32, device=x.device)
+    mlp.forward(x, n, sigma, stream)
+    sigma = sigma[:, 0].contiguous()
+    delta = torch.zeros(n, dtype=torch.float32, device=x.device)
+    check(load().wob_cv_residual_data(scene.handle, _ptr(sigma), int(domain), float(near_factor), _ptr(delta),
+                                      _stream_ptr(stream)))
+    return scene.clone_with_offsets(delta, stream), sigma
+
+
+def control_variate_potential(scene, sigma, points, n_points: int, near_factor: float = 3.0, stream=None):
+    """S sigma~ and its gradient at points (wob_cv_potential): device tensor [n_points, 4]."""
+    import torch
+    from . import _ptr, _stream_ptr
+    out = torch.zeros(n_points, 4, dtype=torch.float32, device=sigma.device)
+    check(load().wob_cv_potential(scene.handle, _ptr(sigma), float(near_factor), _ptr(points), int(n_points),
+                                  _ptr(out), _stream_ptr(stream)))
+    return out
 
 
 def set_control_variate(scene, values: np.ndarray) -> None:
