@@ -352,6 +352,28 @@ int wob_solve_domain_cv(wob_scene scene, const wob_params *params, uint32_t n_po
                         double *sumsq, uint64_t *bounces, float *per_path, void *stream);
 
 /*
+ * Step bound of the scene's BVH traversals (no counterpart in the reference, whose lbvh traversal
+ * is unbounded): a line or closest-point query that visits more than max_steps nodes ends there,
+ * keeps the hits found so far and sets the scene's error word (wob_scene_poll_error; the
+ * host-buffer entry points return WOB_ERR_DEVICE_LIMIT). 0 restores the default, 5 x nodes + 16,
+ * which a correct tree never reaches; a small value lets a caller's error handling be exercised
+ * without a faulty tree.
+ */
+int wob_scene_set_traversal_limit(wob_scene scene, uint32_t max_steps);
+
+/*
+ * Measured ceiling of the uniform-sampling walk's memory access pattern (no counterpart in the
+ * reference; the roofline denominator of that walk): samples per second when every thread of a
+ * full-occupancy grid issues, with four chains in flight, what one uniform boundary sample reads
+ * -- a 16-byte guide-table entry at a random index and the 64-byte record it points to -- over
+ * tables of n_records records and n_guide entries (L2-resident at the benchmark's sizes). iters
+ * gathers per chain and thread; ms receives the timed launch's duration. Allocates and frees its
+ * own tables on the current device.
+ */
+int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters, double *samples_per_s,
+                            float *ms);
+
+/*
  * Residual control variate for the single-layer Neumann estimators (no counterpart in the
  * reference; it reuses the reference's forward walk, estimator.cuh:405-454, unchanged). The
  * control variate is a density sigma~ that is constant on each stored triangle (device array

@@ -84,6 +84,7 @@ struct wob_scene_s {
     DevBuf rhs;       // multi-RHS data [n][dim][n_rhs], storage order
     DevBuf rhs_cv;    // multi-RHS control variate [n][n_rhs], storage order
     uint32_t n_rhs = 0;
+    uint32_t traversal_limit = 0;  // 0: 5 x nodes + 16; else the override of wob_scene_set_traversal_limit
     bool has_volume = false;
     uint32_t area_G = 0, bv_G = 0;  // guide-table records
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
@@ -126,7 +127,7 @@ struct wob_scene_s {
         v.vol_n = vol_n;
         v.vol_G = vol_G;
         v.vol_res = vol_res;
-        v.traversal_limit = 5u * host.n_nodes + 16u;
+        v.traversal_limit = traversal_limit ? traversal_limit : 5u * host.n_nodes + 16u;
         v.total_area = host.total_area;
         v.total_bv = host.total_bv;
         v.vol_size = vol_size;
@@ -991,6 +992,24 @@ int cv_sources(wob_scene s, const float *sigma, float near_factor, CvSources &cs
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate sources");
 }
 }  // namespace
+
+int wob_scene_set_traversal_limit(wob_scene s, uint32_t max_steps) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    s->traversal_limit = max_steps;
+    return WOB_OK;
+}
+
+int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters, double *samples_per_s, float *ms) {
+    if (!samples_per_s || !ms || n_records == 0 || n_guide == 0 || iters == 0)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "n_records, n_guide, iters > 0 and the outputs are required");
+    if (n_records > (1u << 26) || n_guide > (1u << 26)) return fail(WOB_ERR_INVALID_ARGUMENT, "tables too large");
+    int dev = 0, sms = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return fail_cuda(e, "querying the device");
+    e = wobgb::measure_gather_peak(n_records, n_guide, iters, sms, samples_per_s, ms);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "measuring the gather ceiling");
+}
 
 int wob_scene_element_frames(wob_scene s, float *out, void *stream) {
     if (!s || !out) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and out are required");

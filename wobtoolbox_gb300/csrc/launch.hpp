@@ -61,6 +61,10 @@ cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const f
 cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
                                 const float *pts, uint32_t n_points, float *out, cudaStream_t stream);
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream);
+// Random-gather ceiling of the uniform-sampling walk (k_probe.cu): samples per second of guide +
+// 64-byte record gathers over tables of the given sizes, on the current device.
+cudaError_t measure_gather_peak(uint32_t n_rec, uint32_t n_guide, uint32_t iters, int sm_count, double *samples_per_s,
+                                float *ms);
 // Shared error message of the C ABI (capi.cu).
 void set_last_error(const char *msg);
 

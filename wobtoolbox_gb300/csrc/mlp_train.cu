@@ -254,8 +254,12 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
 #pragma unroll
                 for (int hh = 0; hh < 2; hh++) {
                     const int o = m0 + gid + 8 * hh, i = j * 8 + 2 * tig;
-                    if (o < fo)
-                        *reinterpret_cast<float2 *>(dst + o * kW + i) = make_float2(wacc[j][2 * hh], wacc[j][2 * hh + 1]);
+                    // scalar stores: a block's gradient row starts at block * n_params floats, and
+                    // n_params is odd for an odd head width, so pairs are not 8-byte aligned
+                    if (o < fo) {
+                        dst[o * kW + i] = wacc[j][2 * hh];
+                        dst[o * kW + i + 1] = wacc[j][2 * hh + 1];
+                    }
                 }
         }
         if (l == 0) break;

@@ -130,7 +130,9 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
 
     // One iteration of unknown_boundary's loop for the point yprev (reference yref) with weight wgt
     // (already halved on the last bounce): fills the tape entry, advances yprev / yref / wgt.
-    __device__ __forceinline__ void bounce(BPoint<D> &yprev, PRef &yref, float &wgt, TapeEntry &e) {
+    // last: the path's final bounce, whose transport (next sample and weight) is never used and
+    // is skipped, as in the scalar walk.
+    __device__ __forceinline__ void bounce(BPoint<D> &yprev, PRef &yref, float &wgt, TapeEntry &e, bool last) {
         e.w = wgt;
         e.a = yref;
         if constexpr (kStrat == kStratSingleLayer) {
@@ -138,6 +140,7 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
             e.k = 0.0f;
             e.b = yref;
             e.c = (yprev.type == kDirichlet) ? 2.0f * this->p.fk : this->dtc() / this->ift(yprev.angle);
+            if (last) return;
             BPoint<D> y;
             float ip;
             PRef r;
@@ -151,7 +154,8 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
             BPoint<D> ya, y;
             float ipa, ip;
             PRef ra, r;
-            sample_uniform_pair_ref<D>(this->s, this->rng, ya, ipa, ra, y, ip, r);
+            if (last) ya = sample_uniform_ref<D>(this->s, this->rng, ipa, ra);
+            else sample_uniform_pair_ref<D>(this->s, this->rng, ya, ipa, ra, y, ip, r);
             const BPoint<D> &x = yprev;
             e.b = ra;
             if (x.type == kDirichlet) {
@@ -169,6 +173,7 @@ template <int D, int kBie, int kStrat> struct MultiWalker : Walker<D, kBie, kStr
                 else e.k = this->dtc() / this->ift(x.angle) * ipa * this->K.G(ya.p, x.p);
                 e.form = kFormD;
             }
+            if (last) return;
             wgt = wgt * this->fbu(yprev, y, ip, true);
             if (this->stayed) r = yref;
             yprev = y;
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(kBlock, 5) multi_rhs_kernel(SceneView<D> s, Wa
                     w.bounces++;
                     if (m == L - 1) wgt = 0.5f * wgt;
                     TapeEntry e;
-                    w.bounce(yprev, yref, wgt, e);
+                    w.bounce(yprev, yref, wgt, e, m == L - 1);
                     tape[lane] = e;
                     alive = !(wgt == 0.0f);
                 }

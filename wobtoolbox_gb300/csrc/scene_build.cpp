@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <string>
 #include <thread>
 
 namespace wobgb {
@@ -373,6 +374,14 @@ std::string build_host_scene(int dim, uint32_t n, const float *verts, const floa
     if (alphas && !finite_all(alphas, n * D)) return "robin alphas must be finite";
     for (uint32_t i = 0; i < n; i++)
         if (types[i] < 0 || types[i] > 2) return "boundary_types must be 0 (Dirichlet), 1 (Neumann) or 2 (Robin)";
+    // Normals enter every kernel weight (dG/dn); a zero or wildly scaled normal would silently
+    // zero or scale the walk's weights, so anything far from unit length is rejected.
+    for (uint32_t i = 0; i < n; i++) {
+        double q = 0.0;
+        for (size_t k = 0; k < D; k++) q += (double)normals[i * D + k] * (double)normals[i * D + k];
+        if (!(q >= 0.25 && q <= 4.0))
+            return "normals must be unit vectors (element " + std::to_string(i) + " has |n| = " + std::to_string(std::sqrt(q)) + ")";
+    }
 
     // ---- BVH over padded element boxes
     BvhBuilder bb;

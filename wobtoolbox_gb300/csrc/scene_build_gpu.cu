@@ -42,7 +42,7 @@ __host__ __device__ inline float unord(uint32_t u) {
 
 struct Bounds {  // ordered-uint encodings
     uint32_t lo[3], hi[3], clo[3], chi[3], mag;
-    uint32_t bad;            // bit 0 non-finite vertex, 1 normal, 2 data, 3 alpha, 4 type
+    uint32_t bad;            // bit 0 non-finite vertex, 1 normal, 2 data, 3 alpha, 4 type, 5 normal length
     uint32_t all_dirichlet;  // 1 until a non-Dirichlet element is seen
 };
 
@@ -63,6 +63,9 @@ __global__ void k_validate(uint32_t n, const float *__restrict__ verts, const fl
         if (!finite_f(bvals[(size_t)i * D + k])) bad |= 4u;
         if (alphas && !finite_f(alphas[(size_t)i * D + k])) bad |= 8u;
     }
+    float q = 0.0f;
+    for (int k = 0; k < D; k++) q += normals[(size_t)i * D + k] * normals[(size_t)i * D + k];
+    if (!(q >= 0.25f && q <= 4.0f)) bad |= 32u;  // as the host build: normals far from unit length
     const int t = types[i];
     if (t < 0 || t > 2) bad |= 16u;
     if (bad) atomicOr(&b->bad, bad);
@@ -499,6 +502,7 @@ std::string build_impl(uint32_t n, const float *verts, const float *normals, con
     if (hb.bad & 4u) return "boundary values must be finite";
     if (hb.bad & 8u) return "robin alphas must be finite";
     if (hb.bad & 16u) return "boundary_types must be 0 (Dirichlet), 1 (Neumann) or 2 (Robin)";
+    if (hb.bad & 32u) return "normals must be unit vectors";
     out.all_dirichlet = hb.all_dirichlet != 0u;
     // padding of the host build: 1e-5 (extent + max |coordinate|)
     float ext = 0.0f;

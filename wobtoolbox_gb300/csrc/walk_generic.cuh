@@ -381,19 +381,26 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
         for (uint32_t m = 0; m < L; m++) {
             bounces++;
             if (m == L - 1) w = 0.5f * w;
+            // In the last bounce only the known term counts: the transport after it (the next
+            // sample and its weight) is never used, so it is skipped; the draws it would take come
+            // after every draw that matters, so no path value changes.
+            const bool last = m == L - 1;
             if (dl_dirichlet()) {
                 y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
                 contrib = contrib + w * fbk(y_prev, y, ip);
+                if (last) break;
                 w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             } else if (direct_neumann()) {
                 y = sample_boundary_value<D>(s, rng, ip);
                 contrib = contrib + w * fbk(y_prev, y, ip);
+                if (last) break;
                 y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
                 w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             } else if (strat() == kStratSingleLayer) {
                 contrib = contrib + w * fbk(y_prev, y, ip);
+                if (last) break;
                 if (p.n_resampling == 1) y = sample_uniform<D>(s, rng, ip);
                 else y = sample_ris(y_prev, ip);
                 w = w * fbu(y_prev, y, ip, true);
@@ -402,6 +409,11 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
                 // no draw between the two samples (fbk draws only for a source term): take both at once
                 BPoint<D> ya;
                 float ipa;
+                if (last) {
+                    ya = sample_uniform<D>(s, rng, ipa);
+                    contrib = contrib + w * fbk(y_prev, ya, ipa);
+                    break;
+                }
                 sample_uniform_pair<D>(s, rng, ya, ipa, y, ip);
                 contrib = contrib + w * fbk(y_prev, ya, ipa);
                 w = w * fbu(y_prev, y, ip, true);
@@ -409,6 +421,7 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
             } else {
                 y = sample_uniform<D>(s, rng, ip);
                 contrib = contrib + w * fbk(y_prev, y, ip);
+                if (last) break;
                 y = sample_uniform<D>(s, rng, ip);
                 w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
@@ -464,6 +477,7 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
             const V<D> gu = gdu(x, y, 1.0f);
 #pragma unroll
             for (int i = 0; i < D; i++) out[1 + i] = out[1 + i] + w * gu.v[i];
+            if (m == L - 1) break;  // the transport after the last bounce is never used
             y_prev = y;
             if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
             else y = sample_uniform<D>(s, rng, ip);
@@ -520,6 +534,7 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
             const V<D> gu = gdu(x, y, 1.0f);
 #pragma unroll
             for (int i = 0; i < D; i++) gres.v[i] = gres.v[i] + w * gu.v[i];
+            if (m == L - 1) break;  // the transport after the last bounce is never used
             y_prev = y;
             y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
             w = fbu(y, y_prev, ip, false) * w;
@@ -564,6 +579,7 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
             bounces++;
             if (m == L - 1) w = w * 0.5f;
             r = r + sbu(x, y, 1.0f) * w;
+            if (m == L - 1) break;  // the transport after the last bounce is never used
             y_prev = y;
             if (sl_neumann()) y = sample_line_intersection<D>(s, rng, y_prev.p, ip);
             else y = sample_uniform<D>(s, rng, ip);
