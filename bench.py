@@ -261,7 +261,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "nproc": os.cpu_count(), "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference CPU/OpenMP build unavailable (Eigen/lbvh/libigl/json submodules empty); timed the "
                 "C++ restatement of its algorithm under oracle/ on all host threads",
@@ -461,7 +462,7 @@ def run_ours(args):
             O.build()
             sample_pts = cpu_sample(sc, args.cpu_points)
             dt, b, threads = time_cpu(sc, sample_pts, args.cpu_paths)
-            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": threads, "nproc": os.cpu_count(), "kind": "port",
                                    "sample": f"{len(sample_pts)} inside slice points x {args.cpu_paths} paths x "
                                              f"{PATH_LENGTH} bounces ({dt:.1f} s)"}
         elif not args.no_cpu_baseline and args.workload == "dl2d":
@@ -473,7 +474,8 @@ def run_ours(args):
             t0 = time.perf_counter()
             _, _, b, _ = O.solve_domain(el, p, sc["points"], accel=True)
             dt = time.perf_counter() - t0
-            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            out["cpu_baseline"] = {"value": b / dt, "unit": UNIT, "cores": O.max_threads(), "nproc": os.cpu_count(),
+                                   "kind": "port",
                                    "sample": f"the full workload: {len(sc['points'])} points x {p.num_sample_paths} "
                                              f"paths x {p.path_length} bounces ({dt:.1f} s)"}
     scene.close()

@@ -27,7 +27,10 @@ def test_general_2d_matches_api(engine, cuda, tmp_path):
     r = A.run_app("general_2d", cfg)
     assert r.returncode == 0, r.stdout + r.stderr
     rows = _rmse_rows(out)
-    assert rows.shape == (3, 5) and np.all(rows[:, 0] == [512, 1024, 1536])
+    # the reference's columns (samples, time, RMSE of u and of the gradient) and two more: the
+    # iteration's bounces per second and the cumulative bounce count
+    assert rows.shape == (3, 7) and np.all(rows[:, 0] == [512, 1024, 1536])
+    assert np.all(rows[:, 5] > 0) and np.all(np.diff(rows[:, 6]) > 0)
     # cells next to the boundary dominate the RMSE (the double layer's variance grows there); it
     # falls with the sample count
     assert np.all(np.isfinite(rows[:, 2:])) and rows[-1, 2] < rows[0, 2]
@@ -76,7 +79,7 @@ def test_general_3d_matches_api(engine, cuda, tmp_path):
     r = A.run_app("general_3d", cfg)
     assert r.returncode == 0, r.stdout + r.stderr
     rows = _rmse_rows(out)
-    assert rows.shape == (2, 6) and np.all(np.isfinite(rows[:, 2:]))
+    assert rows.shape == (2, 8) and np.all(np.isfinite(rows[:, 2:]))
     _, u = A.read_field(os.path.join(out, "potential2.scalar"))
     _, ua = A.read_field(os.path.join(out, "potential_analytical.scalar"))
     _, g = A.read_field(os.path.join(out, "gradient2.vector3"), 3)
@@ -274,3 +277,25 @@ def test_simple_wob_and_wos_matches_api(engine, cuda, tmp_path, is_wos):
         ref = s[:, 0] / 256
     assert np.allclose(u[inside], ref, rtol=1e-4, atol=1e-5)
     scene.close()
+
+
+def test_general_2d_resume_is_exact(engine, cuda, tmp_path):
+    """A run stopped after 2 iterations and resumed from its checkpoint to 4 writes the same
+    fields, bit for bit, as a run of 4 iterations (the walks are indexed by their path offset)."""
+    obj = str(tmp_path / "star.obj")
+    A.write_star_obj(obj)
+    full, part = str(tmp_path / "full"), str(tmp_path / "part")
+    cfg_full, cfg_a, cfg_b = (str(tmp_path / f) for f in ("full.json", "a.json", "b.json"))
+    A.write_config(cfg_full, obj, full, grid_res=32, num_sample_paths=256, max_iterations=4, path_length=6)
+    A.write_config(cfg_a, obj, part, grid_res=32, num_sample_paths=256, max_iterations=2, path_length=6)
+    A.write_config(cfg_b, obj, part, grid_res=32, num_sample_paths=256, max_iterations=4, path_length=6, resume=True)
+    for c in (cfg_full, cfg_a, cfg_b):
+        r = A.run_app("general_2d", c)
+        assert r.returncode == 0, r.stdout + r.stderr
+    assert "resuming after 2 iterations" in r.stdout
+    for name in ("potential4.scalar", "gradient4.vector2"):
+        a = open(os.path.join(full, name), "rb").read()
+        b = open(os.path.join(part, name), "rb").read()
+        assert a == b, name
+    rows = _rmse_rows(part)
+    assert rows.shape[0] == 4 and np.all(rows[:, 0] == [256, 512, 768, 1024])

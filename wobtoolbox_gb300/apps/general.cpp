@@ -14,17 +14,27 @@
 //   unnormalised sums to compute_rmse, apps/general_3d.cu:367-368);
 // * for the Neumann shift, when the reference point (grid centre, or cell 0 outside) is not an
 //   evaluated point, the first evaluated point is used instead of propagating NaN;
-// * --setup-only stops after the analytical fields are written (no GPU needed).
+// * --setup-only stops after the analytical fields are written (no GPU needed);
+// * rmse_list.csv carries two more columns after the reference's (sample count, time, RMSE of u
+//   and of each gradient component): the iteration's bounces per second and the cumulative bounce
+//   count;
+// * after every iteration the running FP64 sums, the iteration and sample counts, the elapsed time
+//   and the next Philox path offset are written to checkpoint.bin in the output directory; with the
+//   optional key "resume": true a run continues from that file. The walks are indexed by their
+//   path offset, so a resumed run writes bit for bit the fields an uninterrupted run would.
 #include "../../include/wob_gb300.hpp"
 #include "app_io.hpp"
 
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <filesystem>
+#include <fstream>
 #include <iostream>
 #include <limits>
 #include <random>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -113,6 +123,7 @@ int main(int argc, char *argv[]) {
         prm.seed = config.contains("seed") ? (uint64_t)config["seed"].number() : 0u;
         const unsigned max_iterations =
             config.contains("max_iterations") ? (unsigned)config["max_iterations"].number() : 0u;
+        const bool resume = config.contains("resume") && config["resume"].boolean();
         const unsigned num_evaluation_points = grid_res * grid_res;
         const float max_time = (float)config["max_time"].number();
         const wob::EquationKernelType equation_kernel =
@@ -282,19 +293,63 @@ int main(int argc, char *argv[]) {
         std::vector<double> sum(m * (Dim + 1), 0.0);
 
         // the iteration loop (apps/general_2d.cu:327-367)
-        std::ofstream rmse_out(output_dir + "/rmse_list.csv");
         unsigned num_iterations = 0, total_sample_count = 0;
         double elapsed_time = 0.0;
+        const std::string ckpt_path = output_dir + "/checkpoint.bin";
+        struct CkptHeader {
+            char magic[8];
+            uint32_t dim, grid_res, num_iterations, total_sample_count;
+            uint64_t points, path_offset, seed;
+            double elapsed_time;
+        };
+        if (resume) {
+            std::ifstream in(ckpt_path, std::ios::binary);
+            if (!in) throw std::runtime_error("resume: no " + ckpt_path);
+            CkptHeader h{};
+            in.read(reinterpret_cast<char *>(&h), sizeof h);
+            if (!in || std::string(h.magic, 8) != "WOBCKPT1" || h.dim != Dim || h.grid_res != grid_res ||
+                h.points != m || h.seed != prm.seed)
+                throw std::runtime_error("resume: " + ckpt_path + " belongs to another run");
+            in.read(reinterpret_cast<char *>(sum.data()), (std::streamsize)(sum.size() * sizeof(double)));
+            if (!in) throw std::runtime_error("resume: " + ckpt_path + " is truncated");
+            num_iterations = h.num_iterations;
+            total_sample_count = h.total_sample_count;
+            prm.path_offset = h.path_offset;
+            elapsed_time = h.elapsed_time;
+            std::cout << "resuming after " << num_iterations << " iterations (" << total_sample_count << " samples)"
+                      << std::endl;
+        }
+        std::ofstream rmse_out(output_dir + "/rmse_list.csv", resume ? std::ios::app : std::ios::trunc);
+        uint64_t total_bounces = 0;
         std::vector<float> solution(num_evaluation_points);
         std::vector<Vec> gradient(num_evaluation_points);
         while (elapsed_time < max_time * 60.0 && (max_iterations == 0 || num_iterations < max_iterations)) {
             num_iterations += 1;
             total_sample_count += prm.num_sample_paths;
             const auto t0 = std::chrono::steady_clock::now();
-            scene.solve_domain(prm, points, sum);
+            const uint64_t iter_bounces = scene.solve_domain(prm, points, sum);
             const auto t1 = std::chrono::steady_clock::now();
-            elapsed_time += std::chrono::duration<double>(t1 - t0).count();
+            const double iter_time = std::chrono::duration<double>(t1 - t0).count();
+            elapsed_time += iter_time;
+            total_bounces += iter_bounces;
             prm.path_offset += prm.num_sample_paths;
+            {
+                CkptHeader h{};
+                std::memcpy(h.magic, "WOBCKPT1", 8);
+                h.dim = Dim;
+                h.grid_res = grid_res;
+                h.num_iterations = num_iterations;
+                h.total_sample_count = total_sample_count;
+                h.points = m;
+                h.path_offset = prm.path_offset;
+                h.seed = prm.seed;
+                h.elapsed_time = elapsed_time;
+                std::ofstream ck(ckpt_path + ".tmp", std::ios::binary | std::ios::trunc);
+                ck.write(reinterpret_cast<const char *>(&h), sizeof h);
+                ck.write(reinterpret_cast<const char *>(sum.data()), (std::streamsize)(sum.size() * sizeof(double)));
+                ck.close();
+                std::filesystem::rename(ckpt_path + ".tmp", ckpt_path);
+            }
 
             for (unsigned i = 0; i < num_evaluation_points; i++) {
                 solution[i] = std::numeric_limits<float>::quiet_NaN();
@@ -329,6 +384,7 @@ int main(int argc, char *argv[]) {
                 rmse_out << "," << r;
             }
             std::cout << std::flush;
+            rmse_out << "," << (iter_time > 0.0 ? (double)iter_bounces / iter_time : 0.0) << "," << total_bounces;
             rmse_out << std::endl;
             wob::utils::save_field(solution, output_dir + "/potential" + std::to_string(num_iterations) + ".scalar",
                                    grid_res);

@@ -656,7 +656,9 @@ template <int D> __device__ __forceinline__ void sample_uniform_pair(const Scene
     ipb = s.total_area;
 }
 
-template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(const SceneView<D> &s, PathRng &rng, const V<D> &x, uint32_t &m_out) {
+// The random direction of a line-intersection sample (scene.cuh:472-478, 776-784): the upper
+// half-circle in 2D, a hemisphere direction in 3D.
+template <int D> __device__ __forceinline__ V<D> line_sample_direction(PathRng &rng) {
     V<D> dir;
     if constexpr (D == 2) {
         const float theta = rng.uniform();
@@ -669,8 +671,15 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(
         dir.v[0] = dir.v[0] * r;
         dir.v[1] = dir.v[1] * r;
     }
-    uint32_t hits[kHitBuffer];
-    uint32_t m = line_query<D>(s, x, dir, hits);
+    return dir;
+}
+
+// The sample once the line's hits are known (scene.cuh:488-515, 792-830): none -> the zero point;
+// else one of the first min(m, 64) hits chosen uniformly, its point, data and Robin alpha.
+template <int D> __device__ __forceinline__ BPoint<D> line_sample_from_hits(const SceneView<D> &s, PathRng &rng,
+                                                                           const V<D> &x, const V<D> &dir,
+                                                                           const uint32_t *hits, uint32_t m,
+                                                                           uint32_t &m_out) {
     if (m == 0) {
         BPoint<D> z = bp_zero<D>();
         z.angle = 0.5f;
@@ -711,15 +720,74 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(
     return r;
 }
 
+// inv_pdf of a line-intersection sample r of m hits from x (scene.cuh:519-528, 835-845).
+template <int D> __device__ __forceinline__ float line_sample_inv_pdf(const BPoint<D> &r, const V<D> &x, uint32_t m) {
+    const V<D> rv = vsub(r.p, x);
+    const float cosv = fmax_ref(fabsf(vdot(vnormalized(rv), r.n)), kEps10);
+    if constexpr (D == 2) return (float)m * 0x1.921fb6p+1f * vnorm(rv) / cosv;
+    else return (float)m * 2.0f * 0x1.921fb6p+1f * vsqnorm(rv) / cosv;
+}
+
+template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection2(const SceneView<D> &s, PathRng &rng, const V<D> &x, uint32_t &m_out) {
+    const V<D> dir = line_sample_direction<D>(rng);
+    uint32_t hits[kHitBuffer];
+    const uint32_t m = line_query<D>(s, x, dir, hits);
+    return line_sample_from_hits<D>(s, rng, x, dir, hits, m, m_out);
+}
+
 template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection(const SceneView<D> &s, PathRng &rng, const V<D> &x, float &inv_pdf) {
     uint32_t m;
     const BPoint<D> r = sample_line_intersection2<D>(s, rng, x, m);
-    const V<D> rv = vsub(r.p, x);
-    const float cosv = fmax_ref(fabsf(vdot(vnormalized(rv), r.n)), kEps10);
-    if constexpr (D == 2) inv_pdf = (float)m * 0x1.921fb6p+1f * vnorm(rv) / cosv;
-    else inv_pdf = (float)m * 2.0f * 0x1.921fb6p+1f * vsqnorm(rv) / cosv;
+    inv_pdf = line_sample_inv_pdf<D>(r, x, m);
     return r;
 }
+
+// The 3D line query of line_query as a resumable traversal: step() pops one stack entry (a node's
+// four boxes, or a leaf's triangles) and reports when the query has finished. The entries are
+// visited in line_query's depth-first order, so the hits and their order are the same.
+struct LineTraversal3 {
+    uint32_t stack[kStackSize];
+    uint32_t hits[kHitBuffer];
+    V<3> o, d, inv;
+    int sp;
+    uint32_t count, steps;
+
+    __device__ __forceinline__ void begin(const V<3> &o_, const V<3> &d_) {
+        o = o_;
+        d = d_;
+        inv.v[0] = 1.0f / d.v[0]; inv.v[1] = 1.0f / d.v[1]; inv.v[2] = 1.0f / d.v[2];
+        sp = 0;
+        stack[sp++] = 0u;  // root node
+        count = 0;
+        steps = 0;
+    }
+    __device__ __forceinline__ bool step(const SceneView<3> &s) {
+        if (sp <= 0) return true;
+        if (++steps > s.traversal_limit) {
+            atomicOr(s.err, kErrTraversalLimit);
+            sp = 0;
+            return true;
+        }
+        const uint32_t code = stack[--sp];
+        if (code & 0x80000000u) {
+            count = leaf_hits<3>(s, code, o, d, hits, count);
+        } else {
+            uint4 ch;
+            const uint32_t mask = node_hits(s, code, o, inv, 0.0f, ch);
+            const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
+            if (sp + 4 > (int)kStackSize) {
+                atomicOr(s.err, kErrStackOverflow);
+                sp = 0;
+                return true;
+            }
+#pragma unroll
+            for (int k = 3; k >= 0; k--)
+                if ((mask >> k) & 1u)
+                    if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
+        }
+        return sp <= 0;
+    }
+};
 
 template <int D> __device__ __forceinline__ BPoint<D> sample_boundary_value(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
     const float u1 = rng.uniform();

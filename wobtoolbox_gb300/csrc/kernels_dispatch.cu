@@ -82,7 +82,7 @@ cudaError_t launch_domain_3d(const SceneView<3> &s, const WalkParams &p, const f
     if (p.n_volume == 0 && st == kStratSingleLayer)
         return launch_domain_variant<3, kSingleLayer, kStratSingleLayer, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
     if (p.n_volume == 0 && st == kStratFwdSlNeumann)
-        return launch_domain_variant<3, kSingleLayer, kStratFwdSlNeumann, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+        return launch_fwd_wavefront_3d(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
     return launch_domain_variant<3, -1, kStratRuntime, true>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
 }
 

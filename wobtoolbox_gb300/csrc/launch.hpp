@@ -86,6 +86,10 @@ inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {
     return ppt;
 }
 
+// Forward single-layer Neumann walk in 3D as a per-lane state machine (k_fwd_wavefront.cu).
+cudaError_t launch_fwd_wavefront_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                                    double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                    cudaStream_t stream);
 // Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                              double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
