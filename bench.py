@@ -667,7 +667,9 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
                 break
         return curve, t_hit, int(b_.item())
 
-    # warm-up of the walk kernel and of the training graph (not timed)
+    # one-time calibration and warm-up (not timed): the forward walk's kernel shape is autotuned
+    # (it serves the plain and the residual walks alike), then the training graph is warmed up
+    tuned = scene.autotune_domain(dataclasses.replace(base, num_sample_paths=plain_paths), d_pts, n_pts)
     tmp = torch.zeros(n_pts, 4, dtype=torch.float64, device=dev)
     scene.solve_domain(dataclasses.replace(base, num_sample_paths=32), d_pts, n_pts, tmp)
     warm, _ = cv.train_density_cv(scene, base, n_train=8192, train_paths=16, steps=20, batch=8192, lr=2e-3, seed=99)
@@ -697,6 +699,7 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
         "paths_per_point": {"plain": plain_curve[-1][2], "cv": cv_curve[-1][2]},
         "final_rmse": {"plain": plain_curve[-1][1], "cv": cv_curve[-1][1]},
         "triangles": int(len(F)), "points": n_pts, "plain_bounces_per_s": rate,
+        "forward_walk_autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
         "train_loss_first_last": [info["history"][0][1], info["history"][-1][1]],
         "plain_curve": plain_curve[::max(1, len(plain_curve) // 8)], "cv_curve": cv_curve,
         "clock": "wall time on a synchronised device; RMSE evaluation excluded; CV time includes its setup",

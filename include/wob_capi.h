@@ -171,13 +171,17 @@ int wob_solve_domain_host(wob_scene scene, const wob_params *params, const float
 
 /*
  * Autotuner (no counterpart in the reference, whose launch shape is fixed by thrust::for_each):
- * the specialised walk kernels are compiled for several occupancy targets; this times each on
- * the first points (device pointer, about 2^21 paths) with the given parameters and makes the
- * fastest the one used for that kernel variant from then on (process-wide). chosen = index of
- * the chosen configuration (-1: these parameters use no tunable kernel), ms_per_config[k] = time
- * of configuration k (room for 8), n_configs = number of configurations. Allocates a temporary
- * output buffer and synchronises `stream`.
+ * the specialised walk kernels are compiled for several occupancy targets (minimum resident
+ * blocks per SM 1, 5, 6, 8) and run with a cap on the paths one lane takes per warp unit (the
+ * launcher's choice up to 8, or 4, 2, 1) -- WOB_TUNE_CONFIGS configurations, index = occupancy +
+ * 4 x cap. This times each on the first points (device pointer, about 2^21 paths) with the given
+ * parameters and makes the fastest the one used for that kernel variant from then on
+ * (process-wide). chosen = index of the chosen configuration (-1: these parameters use no
+ * tunable kernel), ms_per_config[k] = time of configuration k (room for WOB_TUNE_CONFIGS),
+ * n_configs = number of configurations. Allocates a temporary output buffer and synchronises
+ * `stream`.
  */
+#define WOB_TUNE_CONFIGS 16
 int wob_autotune_domain(wob_scene scene, const wob_params *params, const float *points,
                         uint32_t n_points, int32_t *chosen, float *ms_per_config, int32_t *n_configs,
                         void *stream);
@@ -352,14 +356,16 @@ int wob_solve_domain_cv(wob_scene scene, const wob_params *params, uint32_t n_po
                         double *sumsq, uint64_t *bounces, float *per_path, void *stream);
 
 /*
- * Step bound of the scene's BVH traversals (no counterpart in the reference, whose lbvh traversal
- * is unbounded): a line or closest-point query that visits more than max_steps nodes ends there,
- * keeps the hits found so far and sets the scene's error word (wob_scene_poll_error; the
- * host-buffer entry points return WOB_ERR_DEVICE_LIMIT). 0 restores the default, 5 x nodes + 16,
- * which a correct tree never reaches; a small value lets a caller's error handling be exercised
- * without a faulty tree.
+ * Step bounds of the scene's device loops (no counterpart in the reference, whose lbvh traversal
+ * and walk-on-spheres loop are unbounded). A line or closest-point query that visits more than
+ * max_traversal_steps nodes ends there, keeps the hits found so far and sets the scene's error
+ * word; a walk-on-spheres path stops after max_wos_jumps jumps with the value at its closest point
+ * and sets the error word (wob_scene_poll_error; the host-buffer entry points return
+ * WOB_ERR_DEVICE_LIMIT). 0 restores a default: 5 x nodes + 16 steps, which a correct tree never
+ * reaches, and 4096 jumps (larger values are refused). Lower values let a caller's error handling
+ * be exercised without a faulty scene.
  */
-int wob_scene_set_traversal_limit(wob_scene scene, uint32_t max_steps);
+int wob_scene_set_step_limits(wob_scene scene, uint32_t max_traversal_steps, uint32_t max_wos_jumps);
 
 /*
  * Measured ceiling of the uniform-sampling walk's memory access pattern (no counterpart in the
@@ -403,6 +409,12 @@ int wob_scene_clone(wob_scene scene, wob_scene *out);
 int wob_scene_add_boundary_offsets(wob_scene scene, const float *delta, uint32_t n_elems, int delta_on_device,
                                    void *stream);
 int wob_scene_element_frames(wob_scene scene, float *out, void *stream);
+/* n boundary points uniform by area (the walk's uniform boundary sample, Philox stream 2 of point
+ * index i with `seed`): device arrays p, normals [n][dim], interior_angle, boundary_value, type,
+ * robin_alpha (may be NULL) [n] -- the training points of the control variate's labels. */
+int wob_scene_sample_boundary(wob_scene scene, uint32_t n, uint64_t seed, float *p, float *normals,
+                              float *interior_angle, float *boundary_value, int32_t *boundary_type,
+                              float *robin_alpha, void *stream);
 
 /*
  * Fourier-feature MLP trained with the engine's own CUDA kernels: (x, n) in R^6 ->

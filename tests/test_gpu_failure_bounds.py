@@ -1,10 +1,10 @@
 """The device-side failure bounds, made to run out without any fault.
 
-- Walk on spheres stops a walk after 4096 jumps (the reference's loop has no bound): with eps far
-  below what FP32 coordinates can resolve, every walk reaches the bound; the kernel returns, the
-  estimates stay finite and the scene's error word carries the step-limit bit.
+- Walk on spheres stops a walk after 4096 jumps (the reference's loop has no bound); lowering the
+  bound with wob_scene_set_step_limits makes the walks reach it: the kernel returns, the estimates
+  stay finite and the scene's error word carries the step-limit bit.
 - BVH traversals stop after a step bound (5 x nodes + 16 by default); lowering it with
-  wob_scene_set_traversal_limit makes the line queries of a forward walk run out: the solve
+  wob_scene_set_step_limits makes the line queries of a forward walk run out: the solve
   returns, the error word carries the traversal bit, the host-buffer entry point returns
   WOB_ERR_DEVICE_LIMIT, and restoring the default gives the unbounded results again.
 - Elements of zero area inside a valid scene carry no sampling weight and meet no line: walks on
@@ -33,13 +33,21 @@ def test_wos_step_limit_is_reported(engine, cuda):
     pts = sc["points"][:4]
     s = torch.zeros(len(pts), dtype=torch.float64, device="cuda")
     q = torch.zeros(1, dtype=torch.int64, device="cuda")
-    scene.solve_wos(engine.EstimatorParams(num_sample_paths=8, eps=1e-30, seed=3), torch.from_numpy(pts).cuda(),
-                    len(pts), s, None, q)
+    p = engine.EstimatorParams(num_sample_paths=8, eps=1e-6, seed=3)
+    engine.check(engine.load().wob_scene_set_step_limits(scene.handle, 0, 3))
+    scene.solve_wos(p, torch.from_numpy(pts).cuda(), len(pts), s, None, q)
     torch.cuda.synchronize()
     assert scene.poll_error() & ERR_WOS_STEP_LIMIT
     assert np.all(np.isfinite(s.cpu().numpy()))
-    assert int(q.item()) <= len(pts) * 8 * 4096
+    assert int(q.item()) <= len(pts) * 8 * 3
     assert scene.poll_error() == 0  # polling clears the word
+    with pytest.raises(engine.WobError):
+        engine.check(engine.load().wob_scene_set_step_limits(scene.handle, 0, 5000))
+    engine.check(engine.load().wob_scene_set_step_limits(scene.handle, 0, 0))
+    s.zero_()
+    scene.solve_wos(p, torch.from_numpy(pts).cuda(), len(pts), s, None, q)
+    torch.cuda.synchronize()
+    assert scene.poll_error() == 0
     scene.close()
 
 
@@ -56,7 +64,7 @@ def test_traversal_limit_is_reported_and_reset(engine, cuda):
     scene.solve_domain(p, d, len(pts), ref)
     torch.cuda.synchronize()
     assert scene.poll_error() == 0
-    engine.check(lib.wob_scene_set_traversal_limit(scene.handle, 2))
+    engine.check(lib.wob_scene_set_step_limits(scene.handle, 2, 0))
     s = torch.zeros_like(ref)
     scene.solve_domain(p, d, len(pts), s)
     torch.cuda.synchronize()
@@ -69,7 +77,7 @@ def test_traversal_limit_is_reported_and_reset(engine, cuda):
                                    h_s.ctypes.data, None, C.byref(b))
     assert st == WOB_ERR_DEVICE_LIMIT and "bound" in lib.wob_last_error().decode()
     scene.poll_error()
-    engine.check(lib.wob_scene_set_traversal_limit(scene.handle, 0))
+    engine.check(lib.wob_scene_set_step_limits(scene.handle, 0, 0))
     s2 = torch.zeros_like(ref)
     scene.solve_domain(p, d, len(pts), s2)
     torch.cuda.synchronize()

@@ -214,14 +214,18 @@ def test_invalid_arguments_raise(engine, cuda):
     scene.close()
 
 
-@pytest.mark.parametrize("case", ["uniform3d", "li2d"])
+@pytest.mark.parametrize("case", ["uniform3d", "li2d", "fwd3d"])
 def test_every_tuned_configuration_is_bit_identical(engine, oracle, cuda, case):
-    """The occupancy configurations the autotuner chooses among give the same paths."""
+    """The configurations the autotuner chooses among (occupancy, paths-per-lane cap and, for the 3D
+    forward walk, the lockstep kernel or the per-lane state machine) give the same paths."""
     import ctypes as C
     lib = engine.load()
     if case == "uniform3d":
         sc = S.scene3d(2, False)
         p = _params(engine, 2, 0, 0, 2, path_length=6, num_sample_paths=64)
+    elif case == "fwd3d":
+        sc = S.scene3d(1, True, subdiv=3)
+        p = _params(engine, 0, 1, 1, 1, path_length=4, num_sample_paths=96)
     else:
         sc = S.scene2d(0, False)
         p = _params(engine, 1, 0, 0, 0, path_length=6, num_sample_paths=64)

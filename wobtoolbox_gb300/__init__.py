@@ -292,7 +292,7 @@ class SceneHost:
         p = params.to_c()
         chosen = C.c_int32(-1)
         n = C.c_int32(0)
-        ms = (C.c_float * 8)()
+        ms = (C.c_float * 64)()
         check(load().wob_autotune_domain(self._h, C.byref(p), _ptr(points), int(n_points), C.byref(chosen), ms,
                                          C.byref(n), _stream_ptr(stream)))
         return int(chosen.value), [float(ms[i]) for i in range(n.value)]

@@ -84,7 +84,8 @@ struct wob_scene_s {
     DevBuf rhs;       // multi-RHS data [n][dim][n_rhs], storage order
     DevBuf rhs_cv;    // multi-RHS control variate [n][n_rhs], storage order
     uint32_t n_rhs = 0;
-    uint32_t traversal_limit = 0;  // 0: 5 x nodes + 16; else the override of wob_scene_set_traversal_limit
+    uint32_t traversal_limit = 0;  // 0: 5 x nodes + 16; else the override of wob_scene_set_step_limits
+    uint32_t wos_limit = 0;        // 0: kWosMaxSteps; else the override of wob_scene_set_step_limits
     bool has_volume = false;
     uint32_t area_G = 0, bv_G = 0;  // guide-table records
     uint32_t vol_res = 0, vol_n = 0, vol_G = 0;
@@ -128,6 +129,7 @@ struct wob_scene_s {
         v.vol_G = vol_G;
         v.vol_res = vol_res;
         v.traversal_limit = traversal_limit ? traversal_limit : 5u * host.n_nodes + 16u;
+        v.wos_step_limit = wos_limit ? wos_limit : wobgb::kWosMaxSteps;
         v.total_area = host.total_area;
         v.total_bv = host.total_bv;
         v.vol_size = vol_size;
@@ -207,6 +209,7 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     w.path_offset = p->path_offset;
     w.point_offset = p->point_offset;
     w.ppt = 1;
+    w.ppt_cap = 0;
     w.mode = 0;
     w.n_pot = 0;
     w.m_ker = 0;
@@ -993,9 +996,11 @@ int cv_sources(wob_scene s, const float *sigma, float near_factor, CvSources &cs
 }
 }  // namespace
 
-int wob_scene_set_traversal_limit(wob_scene s, uint32_t max_steps) {
+int wob_scene_set_step_limits(wob_scene s, uint32_t max_traversal_steps, uint32_t max_wos_jumps) {
     if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
-    s->traversal_limit = max_steps;
+    if (max_wos_jumps > wobgb::kWosMaxSteps) return fail(WOB_ERR_INVALID_ARGUMENT, "max_wos_jumps above the 4096 bound");
+    s->traversal_limit = max_traversal_steps;
+    s->wos_limit = max_wos_jumps;
     return WOB_OK;
 }
 
@@ -1009,6 +1014,21 @@ int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters
         return fail_cuda(e, "querying the device");
     e = wobgb::measure_gather_peak(n_records, n_guide, iters, sms, samples_per_s, ms);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "measuring the gather ceiling");
+}
+
+int wob_scene_sample_boundary(wob_scene s, uint32_t n, uint64_t seed, float *p, float *normals, float *interior_angle,
+                              float *boundary_value, int32_t *boundary_type, float *robin_alpha, void *stream) {
+    if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (n == 0) return WOB_OK;
+    if (!p || !normals || !interior_angle || !boundary_value || !boundary_type)
+        return fail(WOB_ERR_INVALID_ARGUMENT, "p, normals, interior_angle, boundary_value and boundary_type are required");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = s->host.dim == 2 ? wobgb::launch_sample_boundary<2>(s->view<2>(), n, seed, p, normals, interior_angle,
+                                                                        boundary_value, boundary_type, robin_alpha, st)
+                                     : wobgb::launch_sample_boundary<3>(s->view<3>(), n, seed, p, normals, interior_angle,
+                                                                        boundary_value, boundary_type, robin_alpha, st);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the boundary sampler");
 }
 
 int wob_scene_element_frames(wob_scene s, float *out, void *stream) {

@@ -195,6 +195,7 @@ template <int D> struct SceneView {
     uint32_t alpha_const;  // D==3: every vertex alpha is alpha_value (elem_aux not read for alphas)
     float alpha_value;
     uint32_t vol_n, vol_G, vol_res, traversal_limit;
+    uint32_t wos_step_limit;  // jumps of a walk-on-spheres path (kWosMaxSteps unless overridden)
     float total_area, total_bv, vol_size;
 };
 
@@ -785,6 +786,41 @@ struct LineTraversal3 {
                 if ((mask >> k) & 1u)
                     if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
         }
+        return sp <= 0;
+    }
+    // One batch of line_query's 3D loop: pop (and test) nodes until 8 leaves are held or the
+    // stack is empty, then test the held leaves in pop order. Same hits, same order.
+    __device__ __forceinline__ bool step_batch(const SceneView<3> &s) {
+        constexpr int kLeafBatch = 8;
+        uint32_t leaves[kLeafBatch];
+        int nl = 0;
+        bool stop = false;
+        while (sp > 0 && nl < kLeafBatch) {
+            if (++steps > s.traversal_limit) {
+                atomicOr(s.err, kErrTraversalLimit);
+                stop = true;
+                break;
+            }
+            const uint32_t code = stack[--sp];
+            if (code & 0x80000000u) {
+                leaves[nl++] = code;
+                continue;
+            }
+            uint4 ch;
+            const uint32_t mask = node_hits(s, code, o, inv, 0.0f, ch);
+            const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
+            if (sp + 4 > (int)kStackSize) {
+                atomicOr(s.err, kErrStackOverflow);
+                stop = true;
+                break;
+            }
+#pragma unroll
+            for (int k = 3; k >= 0; k--)
+                if ((mask >> k) & 1u)
+                    if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
+        }
+        for (int l = 0; l < nl; l++) count = leaf_hits<3>(s, leaves[l], o, d, hits, count);
+        if (stop) sp = 0;
         return sp <= 0;
     }
 };

@@ -25,7 +25,9 @@ constexpr int kFwdBlock = 128;
 
 enum : int { kLaneIdle = 0, kLaneNewPath = 1, kLaneQuery = 2 };
 
-template <bool kPerPath, int kMinB>
+// kBatch: a loop iteration advances a lane by one batch of its traversal (nodes until 8 leaves are
+// held, then those leaves: LineTraversal3::step_batch) instead of one stack entry.
+template <bool kPerPath, bool kBatch, int kMinB>
 __global__ void __launch_bounds__(kFwdBlock, kMinB) fwd_wavefront_kernel(SceneView<3> s, WalkParams p,
                                                                         const float *__restrict__ pts,
                                                                         uint32_t n_points, double *__restrict__ sum,
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(kFwdBlock, kMinB) fwd_wavefront_kernel(SceneVi
                 m = 0;
                 start_bounce = true;
             } else if (phase == kLaneQuery) {
-                if (tr.step(s)) {
+                if (kBatch ? tr.step_batch(s) : tr.step(s)) {
                     uint32_t mh;
                     const BPoint<3> yn = line_sample_from_hits<3>(s, w.rng, y_prev.p, tr.d, tr.hits, tr.count, mh);
                     const float ip = line_sample_inv_pdf<3>(yn, y_prev.p, mh);
@@ -143,20 +145,32 @@ __global__ void __launch_bounds__(kFwdBlock, kMinB) fwd_wavefront_kernel(SceneVi
 
 }  // namespace
 
-cudaError_t launch_fwd_wavefront_3d(const SceneView<3> &s, const WalkParams &p_in, const float *pts, uint32_t n_points,
-                                    double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
-                                    cudaStream_t stream) {
-    WalkParams p = p_in;
-    p.ppt = choose_ppt(n_points, p.n_paths);
-    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
+template <bool kBatch, int kMinB>
+static cudaError_t launch_mode(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                               double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                               uint64_t units, cudaStream_t stream) {
     if (per_path) {
-        auto k = fwd_wavefront_kernel<true, 4>;
+        auto k = fwd_wavefront_kernel<true, kBatch, kMinB>;
         k<<<persistent_grid(k, units), kFwdBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, per_path);
     } else {
-        auto k = fwd_wavefront_kernel<false, 4>;
+        auto k = fwd_wavefront_kernel<false, kBatch, kMinB>;
         k<<<persistent_grid(k, units), kFwdBlock, 0, stream>>>(s, p, pts, n_points, sum, sumsq, bounces, nullptr);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_fwd_wavefront_3d(const SceneView<3> &s, const WalkParams &p_in, const float *pts, uint32_t n_points,
+                                    double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
+                                    int mode, cudaStream_t stream) {
+    WalkParams p = p_in;
+    p.ppt = choose_ppt(n_points, p.n_paths);
+    if (p.ppt_cap && p.ppt > p.ppt_cap) p.ppt = p.ppt_cap;
+    const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
+    switch (mode) {
+    case 0: return launch_mode<false, 4>(s, p, pts, n_points, sum, sumsq, bounces, per_path, units, stream);
+    case 1: return launch_mode<true, 4>(s, p, pts, n_points, sum, sumsq, bounces, per_path, units, stream);
+    default: return launch_mode<true, 1>(s, p, pts, n_points, sum, sumsq, bounces, per_path, units, stream);
+    }
 }
 
 }  // namespace wobgb

@@ -10,7 +10,7 @@
 //
 // Work decomposition as the walk kernels (a warp runs the paths of one point, FP64 sums per point),
 // with path regeneration inside a warp (see wos_kernel).
-// A walk stops after kWosMaxSteps jumps at the latest (taking the value at its current closest
+// A walk stops after kWosMaxSteps jumps (or the scene's lower test override) at the latest (taking the value at its current closest
 // point); such walks are counted in the scene's error word (kErrWosStepLimit).
 #include "kernels.cuh"
 #include "wos.hpp"
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kBlock) wos_kernel(SceneView<2> s, WalkParams 
                 if (R < p.eps || c.elem == 0xFFFFFFFFu) {
                     out = c.elem == 0xFFFFFFFFu ? 0.0f : closest_value(s, c);
                     done = true;
-                } else if (step + 1 >= kWosMaxSteps) {
+                } else if (step + 1 >= s.wos_step_limit) {
                     atomicOr(s.err, kErrWosStepLimit);
                     out = closest_value(s, c);
                     done = true;

@@ -273,6 +273,7 @@ cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p_in,
                                   cudaStream_t stream) {
     WalkParams p = p_in;
     p.ppt = choose_ppt(n_points, p.n_paths);
+    if (p.ppt_cap && p.ppt > p.ppt_cap) p.ppt = p.ppt_cap;
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
     if (per_path) {
         auto k = domain_kernel<D, kBie, kStrat, kVol, true, kMinB>;

@@ -5,16 +5,25 @@
 #include "walk_generic.cuh"
 
 #include <atomic>
+#include <cstdio>
 
 namespace wobgb {
 
 // ---- autotuned variants: 0 = 3D direct uniform, 1 = 2D double-layer line intersection,
-// 2 = 3D direct Neumann; configurations = minimum resident blocks {1 (no limit), 5, 6, 8}.
+// 2 = 3D direct Neumann, 3 = 3D forward single-layer Neumann; configuration c = kernel shape
+// (c % 4: for variants 0-2 the minimum resident blocks {1 (no limit), 5, 6, 8}; for variant 3 the
+// lockstep kernel at >= 5 blocks/SM or the per-lane state machine k_fwd_wavefront.cu in its three
+// modes) and paths-per-lane cap (c / 4: {launcher's choice (up to 8), 4, 2, 1}).
 namespace {
-std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}};
-const int kMinBOf[kTuneConfigs] = {1, 5, 6, 8};
-const char *kConfigNames[kTuneConfigs] = {"128 threads, no register cap", "128 threads, >=5 blocks/SM",
-                                          "128 threads, >=6 blocks/SM", "128 threads, >=8 blocks/SM"};
+std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}, {0}};
+const char *kFwdNames[kTuneOccupancies] = {"lockstep walk, >=5 blocks/SM", "state machine, one entry per step",
+                                           "state machine, one leaf batch per step",
+                                           "state machine, leaf batches, no register cap"};
+const int kMinBOf[kTuneOccupancies] = {1, 5, 6, 8};
+const uint32_t kPptCapOf[kTunePptCaps] = {0u, 4u, 2u, 1u};
+const char *kOccNames[kTuneOccupancies] = {"no register cap", ">=5 blocks/SM", ">=6 blocks/SM", ">=8 blocks/SM"};
+const char *kPptNames[kTunePptCaps] = {"paths/lane <= 8", "paths/lane <= 4", "paths/lane <= 2", "paths/lane = 1"};
+char g_names[kTuneConfigs][64];
 }  // namespace
 
 int tunable_domain_variant(int dim, const WalkParams &p) {
@@ -23,6 +32,7 @@ int tunable_domain_variant(int dim, const WalkParams &p) {
     if (dim == 3 && st == kStratUniform && p.bie == kDirect) return 0;
     if (dim == 2 && st == kStratLineIntersection) return 1;
     if (dim == 3 && st == kStratDirectNeumann) return 2;
+    if (dim == 3 && st == kStratFwdSlNeumann) return 3;
     return -1;
 }
 int domain_config(int variant) { return (variant >= 0 && variant < kNumTunable) ? g_config[variant].load() : 0; }
@@ -31,13 +41,26 @@ void set_domain_config(int variant, int config) {
 }
 const char *domain_config_name(int variant, int config) {
     (void)variant;
-    return (config >= 0 && config < kTuneConfigs) ? kConfigNames[config] : "";
+    if (config < 0 || config >= kTuneConfigs) return "";
+    static char fwd_names[kTuneConfigs][80];
+    if (variant == 3) {
+        if (!fwd_names[config][0])
+            snprintf(fwd_names[config], sizeof fwd_names[config], "128 threads, %s, %s",
+                     kFwdNames[config % kTuneOccupancies], kPptNames[config / kTuneOccupancies]);
+        return fwd_names[config];
+    }
+    if (!g_names[config][0])
+        snprintf(g_names[config], sizeof g_names[config], "128 threads, %s, %s", kOccNames[config % kTuneOccupancies],
+                 kPptNames[config / kTuneOccupancies]);
+    return g_names[config];
 }
 
 template <int D, int kBie, int kStrat>
-static cudaError_t launch_cfg(int config, const SceneView<D> &s, const WalkParams &p, const float *pts, uint32_t n,
+static cudaError_t launch_cfg(int config, const SceneView<D> &s, const WalkParams &p_in, const float *pts, uint32_t n,
                               double *sum, double *sumsq, unsigned long long *b, float *pp, cudaStream_t st) {
-    switch (kMinBOf[config]) {
+    WalkParams p = p_in;
+    p.ppt_cap = kPptCapOf[config / kTuneOccupancies];
+    switch (kMinBOf[config % kTuneOccupancies]) {
     case 5: return launch_domain_variant<D, kBie, kStrat, false, 5>(s, p, pts, n, sum, sumsq, b, pp, st);
     case 6: return launch_domain_variant<D, kBie, kStrat, false, 6>(s, p, pts, n, sum, sumsq, b, pp, st);
     case 8: return launch_domain_variant<D, kBie, kStrat, false, 8>(s, p, pts, n, sum, sumsq, b, pp, st);
@@ -55,6 +78,15 @@ cudaError_t launch_domain_config(int dim, int variant, int config, const void *s
         return launch_cfg<2, kDoubleLayer, kStratLineIntersection>(config, *(const SceneView<2> *)scene_view, p, pts, n, sum, sumsq, b, pp, st);
     if (variant == 2 && dim == 3)
         return launch_cfg<3, kDirect, kStratDirectNeumann>(config, *(const SceneView<3> *)scene_view, p, pts, n, sum, sumsq, b, pp, st);
+    if (variant == 3 && dim == 3) {
+        WalkParams q = p;
+        q.ppt_cap = kPptCapOf[config / kTuneOccupancies];
+        const SceneView<3> &v = *(const SceneView<3> *)scene_view;
+        const int shape = config % kTuneOccupancies;
+        if (shape == 0)
+            return launch_domain_variant<3, kSingleLayer, kStratFwdSlNeumann, false, 5>(v, q, pts, n, sum, sumsq, b, pp, st);
+        return launch_fwd_wavefront_3d(v, q, pts, n, sum, sumsq, b, pp, shape - 1, st);
+    }
     return cudaErrorInvalidValue;
 }
 
@@ -81,8 +113,7 @@ cudaError_t launch_domain_3d(const SceneView<3> &s, const WalkParams &p, const f
     const int st = strategy_of(p.bie, p.estimator, p.problem);
     if (p.n_volume == 0 && st == kStratSingleLayer)
         return launch_domain_variant<3, kSingleLayer, kStratSingleLayer, false, 5>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
-    if (p.n_volume == 0 && st == kStratFwdSlNeumann)
-        return launch_fwd_wavefront_3d(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
+
     return launch_domain_variant<3, -1, kStratRuntime, true>(s, p, pts, n_points, sum, sumsq, bounces, per_path, stream);
 }
 

@@ -33,8 +33,11 @@ cudaError_t launch_line_query_impl(const SceneView<D> &s, const float *origins, 
 // Autotuned variants: the hot specialisations are compiled for several occupancy targets.
 // tunable_domain_variant() names the tunable variant a solve would use (-1: none);
 // set_domain_config() / domain_config() select the compiled configuration used from then on.
-constexpr int kNumTunable = 3;
-constexpr int kTuneConfigs = 4;
+// A configuration is (minimum resident blocks per SM, cap on paths per lane of a warp unit).
+constexpr int kNumTunable = 4;
+constexpr int kTuneOccupancies = 4;
+constexpr int kTunePptCaps = 4;
+constexpr int kTuneConfigs = kTuneOccupancies * kTunePptCaps;
 int tunable_domain_variant(int dim, const WalkParams &p);
 int domain_config(int variant);
 void set_domain_config(int variant, int config);
@@ -65,6 +68,10 @@ template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float 
 // 64-byte record gathers over tables of the given sizes, on the current device.
 cudaError_t measure_gather_peak(uint32_t n_rec, uint32_t n_guide, uint32_t iters, int sm_count, double *samples_per_s,
                                 float *ms);
+// Boundary points uniform by area (k_sample.cu): position, normal, angle, data, type, alpha.
+template <int D>
+cudaError_t launch_sample_boundary(const SceneView<D> &s, uint32_t n, uint64_t seed, float *p, float *nrm,
+                                   float *angle, float *bv, int32_t *type, float *alpha, cudaStream_t stream);
 // Shared error message of the C ABI (capi.cu).
 void set_last_error(const char *msg);
 
@@ -86,10 +93,12 @@ inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {
     return ppt;
 }
 
-// Forward single-layer Neumann walk in 3D as a per-lane state machine (k_fwd_wavefront.cu).
+// Forward single-layer Neumann walk in 3D as a per-lane state machine (k_fwd_wavefront.cu):
+// mode 0 one traversal entry per loop iteration (>= 4 blocks/SM), 1 one leaf batch per iteration
+// (>= 4 blocks/SM), 2 one leaf batch per iteration (no register cap).
 cudaError_t launch_fwd_wavefront_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                     double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
-                                    cudaStream_t stream);
+                                    int mode, cudaStream_t stream);
 // Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                              double *sum, double *sumsq, unsigned long long *bounces, float *per_path,

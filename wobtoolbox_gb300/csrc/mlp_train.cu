@@ -9,7 +9,8 @@
 // for each layer W [out][in] row-major then b [out]. Every product runs on the BF16 tensor cores
 // (mma.sync m16n8k16, FP32 accumulation) with operands rounded to BF16 in shared memory, as in
 // mlp.cu; pre-activations are kept as BF16 for the SiLU derivative, bias gradients are summed in
-// FP32 from the FP32 products.
+// FP32 from the FP32 products. No atomics: every sum has a fixed order, so training is
+// deterministic.
 //
 // Shared-memory operands are 32-bit words holding two BF16 values adjacent along the reduction
 // index (the m16n8k16 fragment layout), rows padded to 36 words so that the 8 x 4 words of a
@@ -41,7 +42,8 @@ constexpr int kThreads = 128;    // 4 warps x 16 rows
 constexpr int kLayerParams = kW * kW + kW;
 
 constexpr size_t kSmemWords = (size_t)(kLayers + kHidden + 1 + kLayers + kHidden + 2) * kMat;
-constexpr size_t kSmemFloats = 2 * kLayers * kW + kTM * kIn + kTM * kW + 4;
+constexpr int kWarps = kThreads / 32;
+constexpr size_t kSmemFloats = kLayers * kW + kLayers * kWarps * kW + kTM * kIn + kTM * kW + 4;
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
@@ -99,8 +101,9 @@ __device__ __forceinline__ void store_t(uint32_t *M, int row, int col, float v) 
 }
 
 // Column sums over the warp's 16 rows of the FP32 values in acc (fragment layout of tile j),
-// added to dst[8 j + 2 tig (+1)] in shared memory.
-__device__ __forceinline__ void add_col_sums(float acc[8][4], float *dst, int lane, int tig) {
+// stored to the warp's own row dst[8 j + 2 tig (+1)] in shared memory (the rows of the block's
+// warps are added in warp order later, so the sum does not depend on scheduling).
+__device__ __forceinline__ void store_col_sums(float acc[8][4], float *dst, int lane, int tig) {
 #pragma unroll
     for (int j = 0; j < 8; j++) {
         float s0 = acc[j][0] + acc[j][2], s1 = acc[j][1] + acc[j][3];
@@ -110,8 +113,8 @@ __device__ __forceinline__ void add_col_sums(float acc[8][4], float *dst, int la
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
         }
         if (lane < 4) {
-            atomicAdd(dst + j * 8 + 2 * tig, s0);
-            atomicAdd(dst + j * 8 + 2 * tig + 1, s1);
+            dst[j * 8 + 2 * tig] = s0;
+            dst[j * 8 + 2 * tig + 1] = s1;
         }
     }
 }
@@ -126,8 +129,8 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     uint32_t *dZ = Zs + kHidden * kMat;       // [row][out]
     uint32_t *dZT = dZ + kMat;                // [out][row]
     float *bias = reinterpret_cast<float *>(smem + kSmemWords);  // [5][64]
-    float *dbias = bias + kLayers * kW;                          // [5][64]
-    float *xin = dbias + kLayers * kW;                           // [64][6]
+    float *dbias = bias + kLayers * kW;                          // [5][4 warps][64]
+    float *xin = dbias + kLayers * kWarps * kW;                  // [64][6]
     float *tgt = xin + kTM * kIn;                                // [64][64]
     float *red = tgt + kTM * kW;                                 // loss per warp
 
@@ -150,10 +153,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
                 Wb[(l - 1) * kMat + o * kLd + p] = pack2(v0, v1);
             }
         }
-        for (int o = tid; o < kW; o += kThreads) {
-            bias[l * kW + o] = o < fo ? Wl[fo * kW + o] : 0.0f;
-            dbias[l * kW + o] = 0.0f;
-        }
+        for (int o = tid; o < kW; o += kThreads) bias[l * kW + o] = o < fo ? Wl[fo * kW + o] : 0.0f;
     }
     // the block's batch rows: Philox4x32-10 on (row, step, 0, "tran") keyed by the seed
     for (int r = tid; r < kTM; r += kThreads) {
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     }
     // ---- backward: at the top of each iteration acc holds dL/dZ_l for this warp's rows (FP32)
     for (int l = kHidden; l >= 0; l--) {
-        add_col_sums(acc, dbias + l * kW, lane, tig);
+        store_col_sums(acc, dbias + (l * kWarps + warp) * kW, lane, tig);
 #pragma unroll
         for (int j = 0; j < 8; j++)
 #pragma unroll
@@ -282,7 +282,11 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     float *dst = g.partial + (size_t)blockIdx.x * g.n_params;
     for (int l = 0; l < kLayers; l++) {
         const int fo = l == kHidden ? out_dim : kW;
-        for (int o = tid; o < fo; o += kThreads) dst[(size_t)l * kLayerParams + fo * kW + o] = dbias[l * kW + o];
+        for (int o = tid; o < fo; o += kThreads) {
+            float b = dbias[(l * kWarps) * kW + o];
+            for (int q = 1; q < kWarps; q++) b += dbias[(l * kWarps + q) * kW + o];
+            dst[(size_t)l * kLayerParams + fo * kW + o] = b;
+        }
     }
     if (tid == 0) g.partial_loss[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
 }

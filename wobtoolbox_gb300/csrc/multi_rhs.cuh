@@ -283,7 +283,9 @@ __global__ void __launch_bounds__(kBlock, 5) multi_rhs_kernel(SceneView<D> s, Wa
                     w.bounces++;
                     if (m == L - 1) wgt = 0.5f * wgt;
                     TapeEntry e;
-                    w.bounce(yprev, yref, wgt, e, m == L - 1);
+                    // with a control variate the potential samples are drawn after the walk from the
+                    // same stream, so the last transport's draws must still be taken
+                    w.bounce(yprev, yref, wgt, e, !kCV && m == L - 1);
                     tape[lane] = e;
                     alive = !(wgt == 0.0f);
                 }

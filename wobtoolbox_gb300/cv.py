@@ -129,9 +129,14 @@ def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256
 
     import torch
     dev = device or torch.device("cuda", torch.cuda.current_device())
-    v, nrm, bv, ty, _ = scene.stored_arrays()
-    bp = sample_boundary_points(v, nrm, bv, ty, n_train, seed)
-    d = {k: torch.from_numpy(np.ascontiguousarray(bp[k])).to(dev) for k in ("p", "n", "angle", "bv", "type")}
+    D = scene.dim
+    d = {"p": torch.empty(n_train, D, device=dev), "n": torch.empty(n_train, D, device=dev),
+         "angle": torch.empty(n_train, device=dev), "bv": torch.empty(n_train, device=dev),
+         "type": torch.empty(n_train, dtype=torch.int32, device=dev)}
+    # training points uniform by area, drawn on the device (wob_scene_sample_boundary)
+    check(load().wob_scene_sample_boundary(scene.handle, n_train, int(seed), d["p"].data_ptr(), d["n"].data_ptr(),
+                                           d["angle"].data_ptr(), d["bv"].data_ptr(), d["type"].data_ptr(), None,
+                                           None))
     s = torch.zeros(n_train, dtype=torch.float64, device=dev)
     q = torch.zeros_like(s)
     b = torch.zeros(1, dtype=torch.int64, device=dev)
