@@ -606,8 +606,8 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
     Both estimators run progressive iterations (plain_paths / cv_paths new paths per point each) and
     the RMSE of the running estimate is taken after each; times are wall-clock on a synchronised
     device, excluding only the RMSE evaluation. The control variate's clock starts before its
-    training labels: labels (65,536 boundary points x 256-path walk estimates of the density),
-    2000 device Adam steps of the 32-frequency 4 x 64 SiLU network, the network at every
+    training labels: labels (65,536 boundary points x 256-path walk estimates of the density,
+    clamped to the 0.999 quantile of their magnitude), 2000 device Adam steps of the 32-frequency 4 x 64 SiLU network, the network at every
     triangle's centroid, the residual Neumann data, the residual scene, the control variate's
     potential at the points, then the residual walks. Returns a dict."""
     import torch
@@ -701,6 +701,7 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
         "triangles": int(len(F)), "points": n_pts, "plain_bounces_per_s": rate,
         "forward_walk_autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
         "train_loss_first_last": [info["history"][0][1], info["history"][-1][1]],
+        "label_clip": {"quantile": info["clip_quantile"], "threshold": info["clip_threshold"]},
         "plain_curve": plain_curve[::max(1, len(plain_curve) // 8)], "cv_curve": cv_curve,
         "clock": "wall time on a synchronised device; RMSE evaluation excluded; CV time includes its setup",
     }

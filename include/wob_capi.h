@@ -415,6 +415,11 @@ int wob_scene_element_frames(wob_scene scene, float *out, void *stream);
 int wob_scene_sample_boundary(wob_scene scene, uint32_t n, uint64_t seed, float *p, float *normals,
                               float *interior_angle, float *boundary_value, int32_t *boundary_type,
                               float *robin_alpha, void *stream);
+/* Clamps n device floats in place to [-t, t], where t is the ceil(quantile * n)-th smallest |v|
+ * (exact: a radix select on the device), and writes t to *threshold (device, may be NULL). The
+ * control variate's labels go through it before training: a mean-squared fit would otherwise
+ * chase the few heavy-tailed walk estimates. quantile in (0, 1]. Stream-ordered, no host sync. */
+int wob_clip_magnitude_quantile(float *values, uint32_t n, float quantile, float *threshold, void *stream);
 
 /*
  * Fourier-feature MLP trained with the engine's own CUDA kernels: (x, n) in R^6 ->

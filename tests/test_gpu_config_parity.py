@@ -7,7 +7,9 @@ Three hot-path code paths appear only at these sizes, and each gets a bit-identi
   then take their alphas from the scene constant instead of the second record array; every
   occupancy build the autotuner chooses among is run;
 - the 3D exterior Neumann workload (forward single layer, line-intersection sampling, 4 bounces)
-  on the 327,680-triangle icosphere: deep BVH traversals with leaves postponed in batches;
+  on the 327,680-triangle icosphere: deep BVH traversals with leaves postponed in batches, in the
+  lockstep kernel and in the split-phase wavefront (every trace shape, chunks smaller than the
+  launch so that several chunks run);
 - a 2D comb whose lines meet far more than 64 segments: the hit buffer overflows and the sample is
   drawn among the first 64 hits with m clamped to 64, as scene.cuh:497 and :801 do.
 
@@ -124,7 +126,66 @@ def test_exterior_neumann_327680_triangles(engine, oracle, cuda):
     assert len(pts) == 32
     params = engine.EstimatorParams(bie_model=0, domain=1, estimator=1, problem=1, path_length=4,
                                     num_sample_paths=32, seed=0)
-    _run_and_compare(engine, oracle, cuda, scene, params, pts, accel=True)
+    lib = engine.load()
+    v = C.c_int32(-1)
+    engine.check(lib.wob_tunable_variant(scene.handle, C.byref(params.to_c()), C.byref(v)))
+    old = C.c_int32(0)
+    engine.check(lib.wob_get_domain_config(v.value, C.byref(old)))
+    ref = None
+    try:
+        # 0: the lockstep kernel; 1-3: the wavefront's trace shapes; 13: shape 1 with the
+        # smallest chunk setting
+        for cfg in (0, 1, 2, 3, 13):
+            engine.check(lib.wob_set_domain_config(v.value, cfg))
+            got = _run_and_compare(engine, oracle, cuda, scene, params, pts, accel=True)
+            assert ref is None or np.array_equal(got, ref)
+            ref = got
+    finally:
+        lib.wob_set_domain_config(v.value, old.value)
+    scene.close()
+
+
+def test_forward_wavefront_chunks_equal_lockstep(engine, cuda):
+    """The wavefront over many chunks (2^19 paths each: 16,384 points x 64 paths = 2 chunks)
+    gives every path the lockstep kernel's value, with per-point sums equal up to order."""
+    import dataclasses
+    torch = cuda
+    V, F, _ = W.displaced_icosphere(5, 0.15, 4, 1)
+    verts, normals = W.mesh_elements(V, F)
+    g = (0.2 + normals[:, None, :2].sum(-1) * np.ones((1, 3))).astype(np.float32)
+    scene = engine.SceneHost(verts, normals, g, np.ones(len(F), np.int32))
+    pts = W.slice_points_z0(200, 4.0)
+    pts = np.ascontiguousarray(pts[np.linalg.norm(pts, axis=1) > 1.6][:16384])
+    assert len(pts) == 16384
+    d = torch.from_numpy(pts).cuda()
+    params = engine.EstimatorParams(bie_model=0, domain=1, estimator=1, problem=1, path_length=5,
+                                    num_sample_paths=64, seed=9, path_offset=128)
+    lib = engine.load()
+    v = C.c_int32(-1)
+    engine.check(lib.wob_tunable_variant(scene.handle, C.byref(params.to_c()), C.byref(v)))
+    old = C.c_int32(0)
+    engine.check(lib.wob_get_domain_config(v.value, C.byref(old)))
+    outs = []
+    try:
+        for cfg in (0, 13):
+            engine.check(lib.wob_set_domain_config(v.value, cfg))
+            vals = torch.zeros(len(pts), 64, 4, device="cuda")
+            scene.debug_domain_paths(params, d, len(pts), vals)
+            s = torch.zeros(len(pts), 4, dtype=torch.float64, device="cuda")
+            q = torch.zeros_like(s)
+            b = torch.zeros(1, dtype=torch.int64, device="cuda")
+            scene.solve_domain(dataclasses.replace(params), d, len(pts), s, q, b)
+            torch.cuda.synchronize()
+            assert scene.poll_error() == 0
+            outs.append((vals.cpu().numpy(), s.cpu().numpy(), q.cpu().numpy(), int(b.item())))
+    finally:
+        lib.wob_set_domain_config(v.value, old.value)
+    (va, sa, qa, ba), (vb, sb, qb, bb) = outs
+    assert np.array_equal(va, vb)
+    scale = np.abs(va.astype(np.float64)).sum(1)
+    assert np.all(np.abs(sa - sb) <= 1e-12 * scale + 1e-300)
+    assert np.all(np.abs(qa - qb) <= 1e-12 * (va.astype(np.float64) ** 2).sum(1) + 1e-300)
+    assert ba == bb == len(pts) * 64 * 5
     scene.close()
 
 

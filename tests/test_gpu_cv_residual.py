@@ -1,5 +1,7 @@
 """The residual control variate and the fused training step on the GPU.
 
+- the label clip (wob_clip_magnitude_quantile) against numpy's order statistic, on heavy-tailed
+  values with ties, zeros and a quantile of 1;
 - the fused training step's gradient (wob_mlp_gradient_fused) against torch float64 autograd and
   against the unfused kernels, for a scalar and a 64-wide head, with a batch that is not a
   multiple of the 64-row tile; device training (wob_mlp_train) is deterministic and lowers the loss;
@@ -94,6 +96,25 @@ def test_device_training_is_deterministic_and_learns(engine, cuda):
         params.append(mlp.params()[0])
         mlp.close()
     assert np.array_equal(params[0], params[1])
+
+
+@pytest.mark.parametrize("n,q", [(1, 0.5), (1000, 0.999), (65536, 0.999), (100003, 0.9), (5000, 1.0)])
+def test_clip_magnitude_quantile_matches_numpy(engine, cuda, n, q):
+    torch = cuda
+    rng = np.random.default_rng(n)
+    v = (rng.standard_t(1.5, n) * 0.1).astype(np.float32)
+    v[: n // 10] = np.round(v[: n // 10], 2)  # ties
+    v[n // 10: n // 10 + n // 20] = 0.0
+    d = torch.from_numpy(v).cuda()
+    t = torch.zeros(1, device="cuda")
+    engine.check(engine.load().wob_clip_magnitude_quantile(d.data_ptr(), n, q, t.data_ptr(), None))
+    torch.cuda.synchronize()
+    k = min(max(int(np.ceil(np.float64(np.float32(q)) * n)), 1), n)
+    ref_t = np.sort(np.abs(v))[k - 1]
+    assert float(t.item()) == ref_t
+    assert np.array_equal(d.cpu().numpy(), np.clip(v, -ref_t, ref_t))
+    with pytest.raises(engine.WobError):
+        engine.check(engine.load().wob_clip_magnitude_quantile(d.data_ptr(), n, 0.0, None, None))
 
 
 def _ext_neumann_scene(engine):

@@ -217,7 +217,7 @@ def test_invalid_arguments_raise(engine, cuda):
 @pytest.mark.parametrize("case", ["uniform3d", "li2d", "fwd3d"])
 def test_every_tuned_configuration_is_bit_identical(engine, oracle, cuda, case):
     """The configurations the autotuner chooses among (occupancy, paths-per-lane cap and, for the 3D
-    forward walk, the lockstep kernel or the per-lane state machine) give the same paths."""
+    forward walk, the lockstep kernel or the split-phase wavefront) give the same paths."""
     import ctypes as C
     lib = engine.load()
     if case == "uniform3d":

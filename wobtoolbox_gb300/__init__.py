@@ -219,7 +219,8 @@ class SceneHost:
     def clone_with_offsets(self, delta, stream=None) -> "SceneHost":
         """An independent copy of this scene whose stored element j has delta[j] added to each of
         its vertex boundary values (delta: device tensor or host array, [n_elems], storage order),
-        with the |g| sampling tables rebuilt (wob_scene_clone + wob_scene_add_boundary_offsets)."""
+        with the |g| sampling tables rebuilt (wob_scene_clone + wob_scene_add_boundary_offsets).
+        The clone's host copy of the element arrays is formed only when first asked for."""
         lib = load()
         h = C.c_void_p()
         check(lib.wob_scene_clone(self._h, C.byref(h)))
@@ -227,17 +228,33 @@ class SceneHost:
         obj._h, obj.dim, obj.n_elems, obj.n_rhs = h, self.dim, self.n_elems, 0
         obj.element_order = self.element_order.copy()
         on_dev = hasattr(delta, "is_cuda") and delta.is_cuda
-        d_host = (delta.detach().cpu().numpy() if on_dev else np.asarray(delta)).astype(np.float32).reshape(-1)
         if on_dev:
             check(lib.wob_scene_add_boundary_offsets(h, _ptr(delta), self.n_elems, 1, _stream_ptr(stream)))
+            kept = delta.detach().reshape(-1).float().clone()  # a later change to delta leaves the clone's view
         else:
-            d_c = np.ascontiguousarray(d_host)
-            check(lib.wob_scene_add_boundary_offsets(h, d_c.ctypes.data, self.n_elems, 0, _stream_ptr(stream)))
-        v, nrm, bv, ty, al = self._host
-        bv2 = bv.copy()
-        bv2[self.element_order] = bv[self.element_order] + d_host[:, None]  # the same float32 adds
-        obj._host = (v, nrm, bv2, ty, al)
+            kept = np.ascontiguousarray(np.asarray(delta, dtype=np.float32).reshape(-1))
+            check(lib.wob_scene_add_boundary_offsets(h, kept.ctypes.data, self.n_elems, 0, _stream_ptr(stream)))
+        parent = self._host
+
+        def host_arrays():
+            d_host = kept.cpu().numpy() if on_dev else kept
+            v, nrm, bv, ty, al = parent
+            bv2 = bv.copy()
+            bv2[obj.element_order] = bv[obj.element_order] + d_host[:, None]  # the same float32 adds
+            return (v, nrm, bv2, ty, al)
+
+        obj._host_fn = host_arrays
         return obj
+
+    @property
+    def _host(self):
+        if self.__dict__.get("_host_arrays") is None:
+            self._host_arrays = self._host_fn()
+        return self._host_arrays
+
+    @_host.setter
+    def _host(self, value):
+        self._host_arrays = value
 
     def info(self) -> dict:
         inf = _capi.wob_scene_info()

@@ -31,7 +31,7 @@ EXPORTED = [
     "wob_autotune_domain", "wob_tunable_variant", "wob_set_domain_config", "wob_get_domain_config",
     "wob_batch_create", "wob_batch_solve", "wob_batch_destroy", "wob_solve_unknown_boundary",
     "wob_scene_set_control_variate", "wob_solve_domain_cv", "wob_cv_residual_data", "wob_cv_potential",
-    "wob_scene_clone", "wob_scene_add_boundary_offsets", "wob_scene_element_frames", "wob_scene_sample_boundary", "wob_measure_gather_peak", "wob_scene_set_step_limits", "wob_mlp_create", "wob_mlp_destroy",
+    "wob_scene_clone", "wob_scene_add_boundary_offsets", "wob_scene_element_frames", "wob_scene_sample_boundary", "wob_clip_magnitude_quantile", "wob_measure_gather_peak", "wob_scene_set_step_limits", "wob_mlp_create", "wob_mlp_destroy",
     "wob_mlp_num_params", "wob_mlp_get_params", "wob_mlp_set_params", "wob_mlp_forward", "wob_mlp_gradient",
     "wob_mlp_adam_step", "wob_mlp_train", "wob_mlp_gradient_fused", "wob_scene_set_rhs", "wob_solve_domain_multi",
     "wob_solve_unknown_boundary_multi",
@@ -112,6 +112,7 @@ def load() -> C.CDLL:
         "wob_scene_add_boundary_offsets": (C.c_int, [vp, vp, u32, C.c_int, vp]),
         "wob_scene_element_frames": (C.c_int, [vp, vp, vp]),
         "wob_scene_sample_boundary": (C.c_int, [vp, u32, u64, vp, vp, vp, vp, vp, vp, vp]),
+        "wob_clip_magnitude_quantile": (C.c_int, [vp, u32, f32, vp, vp]),
         "wob_measure_gather_peak": (C.c_int, [u32, u32, u32, P(C.c_double), P(f32)]),
         "wob_scene_set_step_limits": (C.c_int, [vp, u32, u32]),
         "wob_solve_domain_cv": (C.c_int, [vp, P(wob_params), u32, u32, vp, u32, vp, vp, vp, vp, vp]),

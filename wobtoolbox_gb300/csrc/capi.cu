@@ -210,6 +210,7 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     w.point_offset = p->point_offset;
     w.ppt = 1;
     w.ppt_cap = 0;
+    w.no_alloc = 0;
     w.mode = 0;
     w.n_pot = 0;
     w.m_ker = 0;
@@ -656,6 +657,7 @@ static int solve_domain_host_noalloc_impl(wob_scene s, const wob_params *params,
     wobgb::WalkParams w;
     int st = check_params(s, params, w);
     if (st != WOB_OK) return st;
+    w.no_alloc = 1;  // kernels whose launchers allocate (the forward wavefront) are not chosen
     if (n_points == 0) return WOB_OK;
     if (!points || !sum) return fail(WOB_ERR_INVALID_ARGUMENT, "points and sum are required");
     const int D = s->host.dim;
@@ -1029,6 +1031,14 @@ int wob_scene_sample_boundary(wob_scene s, uint32_t n, uint64_t seed, float *p, 
                                      : wobgb::launch_sample_boundary<3>(s->view<3>(), n, seed, p, normals, interior_angle,
                                                                         boundary_value, boundary_type, robin_alpha, st);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the boundary sampler");
+}
+
+int wob_clip_magnitude_quantile(float *values, uint32_t n, float quantile, float *threshold, void *stream) {
+    if (n == 0) return WOB_OK;
+    if (!values) return fail(WOB_ERR_INVALID_ARGUMENT, "values is NULL");
+    if (!(quantile > 0.0f && quantile <= 1.0f)) return fail(WOB_ERR_INVALID_ARGUMENT, "quantile must be in (0, 1]");
+    cudaError_t e = wobgb::launch_clip_quantile(values, n, quantile, threshold, (cudaStream_t)stream);
+    return e == cudaSuccess ? WOB_OK : fail_cuda(e, "clipping the values");
 }
 
 int wob_scene_element_frames(wob_scene s, float *out, void *stream) {

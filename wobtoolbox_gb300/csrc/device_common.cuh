@@ -15,6 +15,9 @@ namespace wobgb {
 constexpr float kEps10 = 10.0f * 1.1920928955078125e-7f;  // 10 FLT_EPSILON (scene.cuh:418, 531)
 constexpr uint32_t kHitBuffer = 64;                         // hit buffer of scene.cuh:481
 constexpr uint32_t kStackSize = 64;
+constexpr int kWalkBlock = 128;   // threads per block of every kernel that runs 3D line queries
+constexpr int kSharedStack = 24;  // entries of a thread's 3D traversal stack held in shared memory
+constexpr int kLeafBatch = 8;     // leaves a 3D line query holds before testing them
 constexpr uint32_t kChildEmptyD = 0xFFFFFFFFu;
 
 // Device error word bits (see ErrorWord in capi.cu).
@@ -52,6 +55,20 @@ struct PathRng {
     __device__ __forceinline__ PathRng(uint64_t seed, uint32_t stream, uint32_t point, uint64_t path)
         : k0((uint32_t)seed), k1((uint32_t)(seed >> 32) + stream), c1((uint32_t)path),
           c2((uint32_t)(path >> 32)), c3(point), block(0), buf(make_uint4(0, 0, 0, 0)), used(4) {}
+    // Uniforms drawn so far, and the inverse: the stream positioned after d draws (a path whose
+    // state is kept in memory between kernels resumes exactly).
+    __device__ __forceinline__ uint32_t drawn() const { return used == 4 ? block * 4u : (block - 1u) * 4u + (uint32_t)used; }
+    __device__ __forceinline__ void seek(uint32_t d) {
+        const uint32_t b = d >> 2, r = d & 3u;
+        if (r == 0) {
+            block = b;
+            used = 4;
+        } else {
+            buf = philox4x32_10(make_uint4(b, c1, c2, c3), k0, k1);
+            block = b + 1u;
+            used = (int)r;
+        }
+    }
     __device__ __forceinline__ float uniform() {
         if (used == 4) {
             buf = philox4x32_10(make_uint4(block, c1, c2, c3), k0, k1);
@@ -371,7 +388,40 @@ __device__ __forceinline__ uint32_t node_hits(const SceneView<2> &s, uint32_t no
     return mask;
 }
 
-__device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t node, const V<3> &o, const V<3> &inv, float, uint4 &child) {
+// The infinite line o + t d in the form the 3D box test uses: per axis the reciprocal direction r
+// (|d| clamped to at least 1e-20, so r is finite) and -o r. A slab bound is then one FMA,
+// t = fma(b, r, -o r), and no product is infinite or NaN for finite coordinates below 1e18.
+struct LineSlab3 {
+    float r[3], nor[3];
+};
+__device__ __forceinline__ LineSlab3 line_slab3(const V<3> &o, const V<3> &d) {
+    LineSlab3 L;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float di = fabsf(d.v[i]) > 1e-20f ? d.v[i] : copysignf(1e-20f, d.v[i]);
+        L.r[i] = 1.0f / di;
+        L.nor[i] = -(o.v[i] * L.r[i]);
+    }
+    return L;
+}
+
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Slab test of the line against the 4 children's boxes. The slab bounds carry an absolute error
+// of about one float ulp of |o| along the line (the rounding of o r and of the FMA), while the
+// boxes are padded by 1e-5 (extent + max |coordinate|): a line that meets an element of a child
+// crosses that child's padded box over a length of at least twice the pad, so the test never
+// rejects it, and the hits (decided by the exact element test alone) do not depend on it.
+__device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t node, const LineSlab3 &L, uint4 &child) {
     const float4 *p = s.nodes + 8 * node;
     const F8 r0 = ldg8(p), r1 = ldg8(p + 2), r2 = ldg8(p + 4);
     const float4 lx = r0.a, ly = r0.b, lz = r1.a;
@@ -383,11 +433,11 @@ __device__ __forceinline__ uint32_t node_hits(const SceneView<3> &s, uint32_t no
     uint32_t mask = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const float tx1 = (lxs[k] - o.v[0]) * inv.v[0], tx2 = (hxs[k] - o.v[0]) * inv.v[0];
-        const float ty1 = (lys[k] - o.v[1]) * inv.v[1], ty2 = (hys[k] - o.v[1]) * inv.v[1];
-        const float tz1 = (lzs[k] - o.v[2]) * inv.v[2], tz2 = (hzs[k] - o.v[2]) * inv.v[2];
-        const float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
-        const float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+        const float tx1 = __fmaf_rn(lxs[k], L.r[0], L.nor[0]), tx2 = __fmaf_rn(hxs[k], L.r[0], L.nor[0]);
+        const float ty1 = __fmaf_rn(lys[k], L.r[1], L.nor[1]), ty2 = __fmaf_rn(hys[k], L.r[1], L.nor[1]);
+        const float tz1 = __fmaf_rn(lzs[k], L.r[2], L.nor[2]), tz2 = __fmaf_rn(hzs[k], L.r[2], L.nor[2]);
+        const float tn = fmax3f(fminf(tx1, tx2), fminf(ty1, ty2), fminf(tz1, tz2));
+        const float tf = fmin3f(fmaxf(tx1, tx2), fmaxf(ty1, ty2), fmaxf(tz1, tz2));
         if (tn <= tf) mask |= 1u << k;
     }
     return mask;
@@ -492,64 +542,101 @@ __device__ __forceinline__ uint32_t leaf_hits(const SceneView<D> &s, uint32_t co
     return count;
 }
 
-template <int D>
-__device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D> &o, const V<D> &d, uint32_t *hits) {
-    if constexpr (D == 2) {
-        uint32_t n_grid;
-        if (s.lg_K != 0u && line_grid_query(s, o, d, hits, n_grid)) return n_grid;
+// The 3D line query. Depth-first over the 4-wide BVH, children in order, so the leaves (and the
+// hits) come in storage order:
+// - the first child a node's test keeps is visited next straight from a register; only its
+//   later siblings are pushed (in reverse order), so descending costs no stack traffic;
+// - the stack's first kSharedStack entries live in shared memory, one 4-byte column per thread
+//   (entry-major: lanes at different depths still touch distinct banks), deeper entries in a
+//   local array; the held leaves likewise;
+// - leaves are postponed: a lane takes nodes until it holds kLeafBatch leaves or has nothing
+//   left, then tests the held leaves in the order it met them, so the lanes of a warp run node
+//   tests together and triangle tests together instead of alternating between them.
+// Every kernel that calls it runs kWalkBlock threads per block.
+__device__ __forceinline__ uint32_t *stack_column() {
+    __shared__ uint32_t s_stack[kSharedStack * kWalkBlock];
+    return s_stack + threadIdx.x;
+}
+__device__ __forceinline__ uint32_t *leaf_column() {
+    __shared__ uint32_t s_leaf[kLeafBatch * kWalkBlock];
+    return s_leaf + threadIdx.x;
+}
+
+__device__ __forceinline__ uint32_t line_query3(const SceneView<3> &s, const V<3> &o, const V<3> &d, uint32_t *hits) {
+    uint32_t *const my_stack = stack_column();
+    uint32_t *const my_leaf = leaf_column();
+    uint32_t spill[kStackSize - kSharedStack];
+    const LineSlab3 L = line_slab3(o, d);
+    int sp = 0;
+    uint32_t code = 0u;  // root node
+    bool live = true;
+    uint32_t steps = 0, count = 0;
+    while (live) {
+        int nl = 0;
+        while (nl < kLeafBatch) {
+            if (++steps > s.traversal_limit) {
+                atomicOr(s.err, kErrTraversalLimit);
+                live = false;
+                break;
+            }
+            if (code & 0x80000000u) {
+                my_leaf[nl * kWalkBlock] = code;
+                nl++;
+            } else {
+                uint4 ch;
+                uint32_t keep = node_hits(s, code, L, ch);
+                const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (cs[k] == kChildEmptyD) keep &= ~(1u << k);
+                if (keep) {
+                    if (sp + 3 > (int)kStackSize) {
+                        atomicOr(s.err, kErrStackOverflow);
+                        live = false;
+                        break;
+                    }
+                    const uint32_t first = (uint32_t)(__ffs(keep) - 1);
+#pragma unroll
+                    for (int k = 3; k >= 1; k--)
+                        if ((uint32_t)k > first && ((keep >> k) & 1u)) {
+                            if (sp < kSharedStack) my_stack[sp * kWalkBlock] = cs[k];
+                            else spill[sp - kSharedStack] = cs[k];
+                            sp++;
+                        }
+                    code = cs[first];
+                    continue;
+                }
+            }
+            if (sp == 0) {
+                live = false;
+                break;
+            }
+            sp--;
+            code = sp < kSharedStack ? my_stack[sp * kWalkBlock] : spill[sp - kSharedStack];
+        }
+        for (int l = 0; l < nl; l++) count = leaf_hits<3>(s, my_leaf[l * kWalkBlock], o, d, hits, count);
     }
+    return count;
+}
+
+// The 2D line query: the line grid, else depth-first over the 4-wide BVH.
+__device__ __forceinline__ uint32_t line_query2(const SceneView<2> &s, const V<2> &o, const V<2> &d, uint32_t *hits) {
+    uint32_t n_grid;
+    if (s.lg_K != 0u && line_grid_query(s, o, d, hits, n_grid)) return n_grid;
     uint32_t stack[kStackSize];
     int sp = 0;
     stack[sp++] = 0u;  // root node
     uint32_t count = 0;
-    V<D> aux;
-    float c0 = 0.0f;
-    if constexpr (D == 2) {
-        aux = d;
-        c0 = d.v[0] * o.v[1] - d.v[1] * o.v[0];
-    } else {
-        aux.v[0] = 1.0f / d.v[0]; aux.v[1] = 1.0f / d.v[1]; aux.v[2] = 1.0f / d.v[2];
-    }
+    const float c0 = d.v[0] * o.v[1] - d.v[1] * o.v[0];
     uint32_t steps = 0;
-    if constexpr (D == 3) {
-        // Leaves are postponed: a lane pops nodes (testing them) until it holds kLeafBatch leaves
-        // or its stack is empty, then tests the held leaves in the order they were popped, so the
-        // lanes of a warp run node tests together and triangle tests together instead of
-        // alternating between them; the hits and their order are those of the plain depth-first
-        // loop.
-        constexpr int kLeafBatch = 8;
-        uint32_t leaves[kLeafBatch];
-        bool stop = false;
-        while (sp > 0 && !stop) {
-            int nl = 0;
-            while (sp > 0 && nl < kLeafBatch) {
-                if (++steps > s.traversal_limit) { atomicOr(s.err, kErrTraversalLimit); stop = true; break; }
-                const uint32_t code = stack[--sp];
-                if (code & 0x80000000u) {
-                    leaves[nl++] = code;
-                    continue;
-                }
-                uint4 ch;
-                const uint32_t mask = node_hits(s, code, o, aux, c0, ch);
-                const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
-                if (sp + 4 > (int)kStackSize) { atomicOr(s.err, kErrStackOverflow); stop = true; break; }
-#pragma unroll
-                for (int k = 3; k >= 0; k--)
-                    if ((mask >> k) & 1u)
-                        if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
-            }
-            for (int l = 0; l < nl; l++) count = leaf_hits<D>(s, leaves[l], o, d, hits, count);
-        }
-        return count;
-    }
     while (sp > 0) {
         if (++steps > s.traversal_limit) { atomicOr(s.err, kErrTraversalLimit); break; }
         const uint32_t code = stack[--sp];
         if (code & 0x80000000u) {
-            count = leaf_hits<D>(s, code, o, d, hits, count);
+            count = leaf_hits<2>(s, code, o, d, hits, count);
         } else {
             uint4 ch;
-            const uint32_t mask = node_hits(s, code, o, aux, c0, ch);
+            const uint32_t mask = node_hits(s, code, o, d, c0, ch);
             const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
             if (sp + 4 > (int)kStackSize) { atomicOr(s.err, kErrStackOverflow); break; }
 #pragma unroll
@@ -559,6 +646,12 @@ __device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D>
         }
     }
     return count;
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t line_query(const SceneView<D> &s, const V<D> &o, const V<D> &d, uint32_t *hits) {
+    if constexpr (D == 3) return line_query3(s, o, d, hits);
+    else return line_query2(s, o, d, hits);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -676,22 +769,25 @@ template <int D> __device__ __forceinline__ V<D> line_sample_direction(PathRng &
 }
 
 // The sample once the line's hits are known (scene.cuh:488-515, 792-830): none -> the zero point;
-// else one of the first min(m, 64) hits chosen uniformly, its point, data and Robin alpha.
-template <int D> __device__ __forceinline__ BPoint<D> line_sample_from_hits(const SceneView<D> &s, PathRng &rng,
-                                                                           const V<D> &x, const V<D> &dir,
-                                                                           const uint32_t *hits, uint32_t m,
-                                                                           uint32_t &m_out) {
-    if (m == 0) {
-        BPoint<D> z = bp_zero<D>();
-        z.angle = 0.5f;
-        m_out = 0;
-        return z;
-    }
+// else one of the first min(m, 64) hits chosen uniformly, its point, data and Robin alpha. Split in
+// two for kernels that choose the hit where the query ran and form the point elsewhere:
+// line_hit_choice takes the choice's draw (only when there is a hit) and returns the element,
+// line_hit_point forms the sample on it.
+__device__ __forceinline__ uint32_t line_hit_choice(PathRng &rng, const uint32_t *hits, uint32_t &m) {
+    if (m == 0) return 0u;
     m = m < kHitBuffer ? m : kHitBuffer;
     const float u = rng.uniform();
     uint32_t k = (uint32_t)((float)m * u);
     k = (m - 1) < k ? (m - 1) : k;
-    const uint32_t ei = hits[k];
+    return hits[k];
+}
+template <int D> __device__ __forceinline__ BPoint<D> line_hit_point(const SceneView<D> &s, uint32_t ei, uint32_t m,
+                                                                    const V<D> &x, const V<D> &dir) {
+    if (m == 0) {
+        BPoint<D> z = bp_zero<D>();
+        z.angle = 0.5f;
+        return z;
+    }
     const Elem<D> e = load_elem<D>(s, ei);
     float t = 0.0f;
     isect_elem<D>(s, ei, x, dir, t);
@@ -717,8 +813,15 @@ template <int D> __device__ __forceinline__ BPoint<D> line_sample_from_hits(cons
         r.bv = L0 * e.bv[0] + L1 * e.bv[1] + L2 * e.bv[2];
         r.alpha = L0 * e.alpha[0] + L1 * e.alpha[1] + L2 * e.alpha[2];
     }
-    m_out = m;
     return r;
+}
+template <int D> __device__ __forceinline__ BPoint<D> line_sample_from_hits(const SceneView<D> &s, PathRng &rng,
+                                                                           const V<D> &x, const V<D> &dir,
+                                                                           const uint32_t *hits, uint32_t m,
+                                                                           uint32_t &m_out) {
+    const uint32_t ei = line_hit_choice(rng, hits, m);
+    m_out = m;
+    return line_hit_point<D>(s, ei, m, x, dir);
 }
 
 // inv_pdf of a line-intersection sample r of m hits from x (scene.cuh:519-528, 835-845).
@@ -742,88 +845,6 @@ template <int D> __device__ __forceinline__ BPoint<D> sample_line_intersection(c
     inv_pdf = line_sample_inv_pdf<D>(r, x, m);
     return r;
 }
-
-// The 3D line query of line_query as a resumable traversal: step() pops one stack entry (a node's
-// four boxes, or a leaf's triangles) and reports when the query has finished. The entries are
-// visited in line_query's depth-first order, so the hits and their order are the same.
-struct LineTraversal3 {
-    uint32_t stack[kStackSize];
-    uint32_t hits[kHitBuffer];
-    V<3> o, d, inv;
-    int sp;
-    uint32_t count, steps;
-
-    __device__ __forceinline__ void begin(const V<3> &o_, const V<3> &d_) {
-        o = o_;
-        d = d_;
-        inv.v[0] = 1.0f / d.v[0]; inv.v[1] = 1.0f / d.v[1]; inv.v[2] = 1.0f / d.v[2];
-        sp = 0;
-        stack[sp++] = 0u;  // root node
-        count = 0;
-        steps = 0;
-    }
-    __device__ __forceinline__ bool step(const SceneView<3> &s) {
-        if (sp <= 0) return true;
-        if (++steps > s.traversal_limit) {
-            atomicOr(s.err, kErrTraversalLimit);
-            sp = 0;
-            return true;
-        }
-        const uint32_t code = stack[--sp];
-        if (code & 0x80000000u) {
-            count = leaf_hits<3>(s, code, o, d, hits, count);
-        } else {
-            uint4 ch;
-            const uint32_t mask = node_hits(s, code, o, inv, 0.0f, ch);
-            const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
-            if (sp + 4 > (int)kStackSize) {
-                atomicOr(s.err, kErrStackOverflow);
-                sp = 0;
-                return true;
-            }
-#pragma unroll
-            for (int k = 3; k >= 0; k--)
-                if ((mask >> k) & 1u)
-                    if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
-        }
-        return sp <= 0;
-    }
-    // One batch of line_query's 3D loop: pop (and test) nodes until 8 leaves are held or the
-    // stack is empty, then test the held leaves in pop order. Same hits, same order.
-    __device__ __forceinline__ bool step_batch(const SceneView<3> &s) {
-        constexpr int kLeafBatch = 8;
-        uint32_t leaves[kLeafBatch];
-        int nl = 0;
-        bool stop = false;
-        while (sp > 0 && nl < kLeafBatch) {
-            if (++steps > s.traversal_limit) {
-                atomicOr(s.err, kErrTraversalLimit);
-                stop = true;
-                break;
-            }
-            const uint32_t code = stack[--sp];
-            if (code & 0x80000000u) {
-                leaves[nl++] = code;
-                continue;
-            }
-            uint4 ch;
-            const uint32_t mask = node_hits(s, code, o, inv, 0.0f, ch);
-            const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
-            if (sp + 4 > (int)kStackSize) {
-                atomicOr(s.err, kErrStackOverflow);
-                stop = true;
-                break;
-            }
-#pragma unroll
-            for (int k = 3; k >= 0; k--)
-                if ((mask >> k) & 1u)
-                    if (cs[k] != kChildEmptyD) stack[sp++] = cs[k];
-        }
-        for (int l = 0; l < nl; l++) count = leaf_hits<3>(s, leaves[l], o, d, hits, count);
-        if (stop) sp = 0;
-        return sp <= 0;
-    }
-};
 
 template <int D> __device__ __forceinline__ BPoint<D> sample_boundary_value(const SceneView<D> &s, PathRng &rng, float &inv_pdf) {
     const float u1 = rng.uniform();

@@ -21,8 +21,9 @@
 // triangle's own term in the residual data is zero: n_j is normal to triangle j, so dG/dn_x
 // vanishes on it.
 //
-// Work decomposition: one thread per target, 256 targets per block; the sources stream through
-// shared memory in tiles of 256 {centroid, sigma~ A, near radius^2}, read as broadcasts. Far pairs
+// Work decomposition: two targets per thread (one where two would leave SMs idle), 256 threads per
+// block; the sources stream through shared memory in tiles of 256 {centroid, sigma~ A, near
+// radius^2}, read as broadcasts. Far pairs
 // cost one rsqrt and a dozen FMAs; a warp in which any lane has a near pair takes the closed form
 // for those lanes (the targets of a warp and the sources of a tile are both consecutive in BVH
 // storage order, so near pairs come in spatial clusters). FP32 partial sums per tile, FP64 across
@@ -137,8 +138,10 @@ __global__ void cv_sources_kernel(SceneView<3> s, const float *__restrict__ sigm
 }
 
 // kMode 0: residual data at the stored triangles' centroids; kMode 1: potential and gradient at
-// points (out: [n][4] = u, du/dx, du/dy, du/dz).
-template <int kMode>
+// points (out: [n][4] = u, du/dx, du/dy, du/dz). Each thread takes kTgt targets (a block covers
+// kTgt x 256), so every source read from shared memory serves kTgt pairs; one target per thread
+// where two would leave SMs without a block.
+template <int kMode, int kTgt>
 __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const float4 *__restrict__ src,
                                                           const float *__restrict__ near2,
                                                           const float *__restrict__ sigma,
@@ -146,22 +149,27 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
                                                           float c_coef, float *__restrict__ out) {
     __shared__ float4 s_src[kCvBlock];
     __shared__ float s_n2[kCvBlock];
-    const uint32_t tgt = blockIdx.x * kCvBlock + threadIdx.x;
-    const bool active = tgt < n_targets;
-    float xd[3] = {0.0f, 0.0f, 0.0f};
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-    if (active) {
-        if (kMode == 0) {
-            const TriVerts t = load_tri(s, tgt);
-            centroid_of(t, xd);
-            const float4 q2 = __ldg(s.elems + 4 * tgt + 2);
-            nx = q2.y; ny = q2.z; nz = q2.w;
-        } else {
-            for (int k = 0; k < 3; k++) xd[k] = pts[(size_t)tgt * 3 + k];
+    uint32_t tgt[kTgt];
+    bool active[kTgt];
+    float xd[kTgt][3], nn[kTgt][3];
+    for (int t = 0; t < kTgt; t++) {
+        tgt[t] = blockIdx.x * (kCvBlock * kTgt) + t * kCvBlock + threadIdx.x;
+        active[t] = tgt[t] < n_targets;
+        for (int k = 0; k < 3; k++) xd[t][k] = nn[t][k] = 0.0f;
+        if (active[t]) {
+            if (kMode == 0) {
+                const TriVerts tv = load_tri(s, tgt[t]);
+                centroid_of(tv, xd[t]);
+                const float4 q2 = __ldg(s.elems + 4 * tgt[t] + 2);
+                nn[t][0] = q2.y; nn[t][1] = q2.z; nn[t][2] = q2.w;
+            } else {
+                for (int k = 0; k < 3; k++) xd[t][k] = pts[(size_t)tgt[t] * 3 + k];
+            }
         }
     }
-    const float x = xd[0], y = xd[1], z = xd[2];
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    double acc[kTgt][4];
+    for (int t = 0; t < kTgt; t++)
+        for (int c = 0; c < 4; c++) acc[t][c] = 0.0;
     const uint32_t n_src = s.n_elems;
     for (uint32_t t0 = 0; t0 < n_src; t0 += kCvBlock) {
         __syncthreads();
@@ -172,55 +180,71 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
         }
         __syncthreads();
         const uint32_t cnt = min((uint32_t)kCvBlock, n_src - t0);
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+        float a[kTgt][4];
+#pragma unroll
+        for (int t = 0; t < kTgt; t++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) a[t][c] = 0.0f;
         for (uint32_t k = 0; k < cnt; k++) {
             const float4 q = s_src[k];
-            const float dx = x - q.x, dy = y - q.y, dz = z - q.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const bool near = r2 < s_n2[k];
-            if (!near) {
-                const float rinv = rsqrtf(r2);
-                const float r3 = rinv * rinv * rinv;
-                if (kMode == 0) {
-                    a0 += q.w * (dx * nx + dy * ny + dz * nz) * r3;
-                } else {
-                    a0 += q.w * rinv;
-                    const float wr3 = q.w * r3;
-                    a1 -= wr3 * dx;
-                    a2 -= wr3 * dy;
-                    a3 -= wr3 * dz;
+            const float n2 = s_n2[k];
+            bool near[kTgt];
+            bool any_near = false;
+#pragma unroll
+            for (int t = 0; t < kTgt; t++) {
+                const float dx = xd[t][0] - q.x, dy = xd[t][1] - q.y, dz = xd[t][2] - q.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                near[t] = r2 < n2;
+                any_near |= near[t] && active[t];
+                if (!near[t]) {
+                    const float rinv = rsqrtf(r2);
+                    const float r3 = rinv * rinv * rinv;
+                    if (kMode == 0) {
+                        a[t][0] += q.w * (dx * nn[t][0] + dy * nn[t][1] + dz * nn[t][2]) * r3;
+                    } else {
+                        a[t][0] += q.w * rinv;
+                        const float wr3 = q.w * r3;
+                        a[t][1] -= wr3 * dx;
+                        a[t][2] -= wr3 * dy;
+                        a[t][3] -= wr3 * dz;
+                    }
                 }
             }
-            if (__any_sync(0xffffffffu, near && active)) {
+            if (__any_sync(0xffffffffu, any_near)) {
                 const uint32_t i = t0 + k;
-                if (near && active && !(kMode == 0 && i == tgt)) {
-                    const TriVerts tri = load_tri(s, i);
-                    float P, G[3];
-                    triangle_potential(xd, tri, P, G);
-                    const float sg = __ldg(sigma + i);
-                    if (kMode == 0) {
-                        a0 -= sg * (G[0] * nx + G[1] * ny + G[2] * nz);
-                    } else {
-                        a0 += sg * P;
-                        a1 += sg * G[0];
-                        a2 += sg * G[1];
-                        a3 += sg * G[2];
+#pragma unroll
+                for (int t = 0; t < kTgt; t++) {
+                    if (near[t] && active[t] && !(kMode == 0 && i == tgt[t])) {
+                        const TriVerts tri = load_tri(s, i);
+                        float P, G[3];
+                        triangle_potential(xd[t], tri, P, G);
+                        const float sg = __ldg(sigma + i);
+                        if (kMode == 0) {
+                            a[t][0] -= sg * (G[0] * nn[t][0] + G[1] * nn[t][1] + G[2] * nn[t][2]);
+                        } else {
+                            a[t][0] += sg * P;
+                            a[t][1] += sg * G[0];
+                            a[t][2] += sg * G[1];
+                            a[t][3] += sg * G[2];
+                        }
                     }
                 }
             }
         }
-        acc[0] += a0;
-        acc[1] += a1;
-        acc[2] += a2;
-        acc[3] += a3;
+#pragma unroll
+        for (int t = 0; t < kTgt; t++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[t][c] += a[t][c];
     }
-    if (!active) return;
-    if (kMode == 0) {
-        const double c = (double)c_coef;
-        const double Tsig = c * kInv4Pi * acc[0];
-        out[tgt] = (float)((Tsig - (double)__ldg(sigma + tgt)) / c);
-    } else {
-        for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * acc[k]);
+    for (int t = 0; t < kTgt; t++) {
+        if (!active[t]) continue;
+        if (kMode == 0) {
+            const double c = (double)c_coef;
+            const double Tsig = c * kInv4Pi * acc[t][0];
+            out[tgt[t]] = (float)((Tsig - (double)__ldg(sigma + tgt[t])) / c);
+        } else {
+            for (int k = 0; k < 4; k++) out[(size_t)tgt[t] * 4 + k] = (float)(kInv4Pi * acc[t][k]);
+        }
     }
 }
 
@@ -245,6 +269,21 @@ __global__ void element_frames_kernel(SceneView<D> s, float *__restrict__ out) {
     }
 }
 
+template <int kMode>
+void launch_sum(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma, const float *pts,
+                uint32_t n, float c_coef, float *out, cudaStream_t stream) {
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t two = (n + 2 * kCvBlock - 1) / (2 * kCvBlock);
+    if (two >= 2u * (uint32_t)sms) {
+        cv_sum_kernel<kMode, 2><<<two, kCvBlock, 0, stream>>>(s, src, near2, sigma, pts, n, c_coef, out);
+    } else {
+        cv_sum_kernel<kMode, 1><<<(n + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, pts, n,
+                                                                                       c_coef, out);
+    }
+}
+
 }  // namespace
 
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream) {
@@ -262,16 +301,14 @@ cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float n
 
 cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
                                float c_coef, float *delta, cudaStream_t stream) {
-    cv_sum_kernel<0><<<(s.n_elems + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, nullptr,
-                                                                                      s.n_elems, c_coef, delta);
+    launch_sum<0>(s, src, near2, sigma, nullptr, s.n_elems, c_coef, delta, stream);
     return cudaGetLastError();
 }
 
 cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
                                 const float *pts, uint32_t n_points, float *out, cudaStream_t stream) {
     if (n_points == 0) return cudaSuccess;
-    cv_sum_kernel<1><<<(n_points + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, pts,
-                                                                                     n_points, 0.0f, out);
+    launch_sum<1>(s, src, near2, sigma, pts, n_points, 0.0f, out, stream);
     return cudaGetLastError();
 }
 

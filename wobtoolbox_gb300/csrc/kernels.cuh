@@ -13,7 +13,7 @@
 
 namespace wobgb {
 
-constexpr int kBlock = 128;
+constexpr int kBlock = kWalkBlock;  // the 3D line query keeps its stack in shared memory columns of this block
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

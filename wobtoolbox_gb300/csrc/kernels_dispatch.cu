@@ -12,13 +12,16 @@ namespace wobgb {
 // ---- autotuned variants: 0 = 3D direct uniform, 1 = 2D double-layer line intersection,
 // 2 = 3D direct Neumann, 3 = 3D forward single-layer Neumann; configuration c = kernel shape
 // (c % 4: for variants 0-2 the minimum resident blocks {1 (no limit), 5, 6, 8}; for variant 3 the
-// lockstep kernel at >= 5 blocks/SM or the per-lane state machine k_fwd_wavefront.cu in its three
-// modes) and paths-per-lane cap (c / 4: {launcher's choice (up to 8), 4, 2, 1}).
+// lockstep kernel at >= 5 blocks/SM or the split-phase wavefront k_fwd_wave.cu in its three trace
+// shapes) and c / 4: paths-per-lane cap {launcher's choice (up to 8), 4, 2, 1} for the lockstep
+// kernels, paths per wavefront chunk {2^22, 2^21, 2^20, 2^19} for the wavefront.
 namespace {
-std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}, {0}};
-const char *kFwdNames[kTuneOccupancies] = {"lockstep walk, >=5 blocks/SM", "state machine, one entry per step",
-                                           "state machine, one leaf batch per step",
-                                           "state machine, leaf batches, no register cap"};
+// defaults: the 3D forward walk starts on the wavefront (trace at >= 6 blocks/SM, 2^22-path chunks)
+std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}, {2}};
+const char *kFwdNames[kTuneOccupancies] = {"lockstep walk, >=5 blocks/SM", "wavefront, trace >=8 blocks/SM",
+                                           "wavefront, trace >=6 blocks/SM",
+                                           "wavefront, trace >=8 blocks/SM, 4-leaf batches"};
+const uint32_t kWaveSlotsOf[kTunePptCaps] = {1u << 22, 1u << 21, 1u << 20, 1u << 19};
 const int kMinBOf[kTuneOccupancies] = {1, 5, 6, 8};
 const uint32_t kPptCapOf[kTunePptCaps] = {0u, 4u, 2u, 1u};
 const char *kOccNames[kTuneOccupancies] = {"no register cap", ">=5 blocks/SM", ">=6 blocks/SM", ">=8 blocks/SM"};
@@ -44,9 +47,14 @@ const char *domain_config_name(int variant, int config) {
     if (config < 0 || config >= kTuneConfigs) return "";
     static char fwd_names[kTuneConfigs][80];
     if (variant == 3) {
-        if (!fwd_names[config][0])
-            snprintf(fwd_names[config], sizeof fwd_names[config], "128 threads, %s, %s",
-                     kFwdNames[config % kTuneOccupancies], kPptNames[config / kTuneOccupancies]);
+        if (!fwd_names[config][0]) {
+            if (config % kTuneOccupancies == 0)
+                snprintf(fwd_names[config], sizeof fwd_names[config], "128 threads, %s, %s", kFwdNames[0],
+                         kPptNames[config / kTuneOccupancies]);
+            else
+                snprintf(fwd_names[config], sizeof fwd_names[config], "128 threads, %s, %u paths per chunk",
+                         kFwdNames[config % kTuneOccupancies], kWaveSlotsOf[config / kTuneOccupancies]);
+        }
         return fwd_names[config];
     }
     if (!g_names[config][0])
@@ -83,9 +91,9 @@ cudaError_t launch_domain_config(int dim, int variant, int config, const void *s
         q.ppt_cap = kPptCapOf[config / kTuneOccupancies];
         const SceneView<3> &v = *(const SceneView<3> *)scene_view;
         const int shape = config % kTuneOccupancies;
-        if (shape == 0)
+        if (shape == 0 || p.no_alloc)
             return launch_domain_variant<3, kSingleLayer, kStratFwdSlNeumann, false, 5>(v, q, pts, n, sum, sumsq, b, pp, st);
-        return launch_fwd_wavefront_3d(v, q, pts, n, sum, sumsq, b, pp, shape - 1, st);
+        return launch_fwd_wave_3d(v, p, pts, n, sum, sumsq, b, pp, shape, kWaveSlotsOf[config / kTuneOccupancies], st);
     }
     return cudaErrorInvalidValue;
 }

@@ -72,6 +72,9 @@ cudaError_t measure_gather_peak(uint32_t n_rec, uint32_t n_guide, uint32_t iters
 template <int D>
 cudaError_t launch_sample_boundary(const SceneView<D> &s, uint32_t n, uint64_t seed, float *p, float *nrm,
                                    float *angle, float *bv, int32_t *type, float *alpha, cudaStream_t stream);
+// Clamps device values to [-t, t], t = the ceil(q n)-th smallest |v| (k_sample.cu); t also to
+// *threshold when it is not null.
+cudaError_t launch_clip_quantile(float *values, uint32_t n, float quantile, float *threshold, cudaStream_t stream);
 // Shared error message of the C ABI (capi.cu).
 void set_last_error(const char *msg);
 
@@ -93,12 +96,13 @@ inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {
     return ppt;
 }
 
-// Forward single-layer Neumann walk in 3D as a per-lane state machine (k_fwd_wavefront.cu):
-// mode 0 one traversal entry per loop iteration (>= 4 blocks/SM), 1 one leaf batch per iteration
-// (>= 4 blocks/SM), 2 one leaf batch per iteration (no register cap).
-cudaError_t launch_fwd_wavefront_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
-                                    double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
-                                    int mode, cudaStream_t stream);
+// Forward single-layer Neumann walk in 3D as a split-phase wavefront (k_fwd_wave.cu): shape 1
+// traces at >= 8 blocks/SM with 8-leaf batches, 2 at >= 6 blocks/SM, 3 at >= 8 blocks/SM with
+// 4-leaf batches; paths advance in chunks of at most max_slots paths (whole points). Allocates its
+// path state stream-ordered (cudaMallocAsync).
+cudaError_t launch_fwd_wave_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
+                               double *sum, double *sumsq, unsigned long long *bounces, float *per_path, int shape,
+                               uint32_t max_slots, cudaStream_t stream);
 // Dispatchers (kernels_dispatch.cu): pick the specialised variant for the parameters.
 cudaError_t launch_domain_2d(const SceneView<2> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                              double *sum, double *sumsq, unsigned long long *bounces, float *per_path,

@@ -20,6 +20,7 @@ struct WalkParams {
     uint32_t point_offset;
     uint32_t ppt;   // paths per lane in one warp unit (set by the launcher, >= 1)
     uint32_t ppt_cap;  // 0: the launcher's choice; else at most this many (an autotuned setting)
+    uint32_t no_alloc;  // 1: only kernels that allocate nothing (the allocation-free entry point)
     uint32_t mode;  // boundary kernel: 0 = boundary estimate, 1 = unknown boundary density
     uint32_t n_pot, m_ker;  // control-variate estimator: samples of <G_x, sigma~> and of K sigma~
 };

@@ -122,9 +122,12 @@ def sample_boundary_points(verts: np.ndarray, normals: np.ndarray, bvals: np.nda
 
 def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256, steps: int = 2000,
                      batch: int = 8192, lr: float = 2e-3, freq_sigma: float = 1.0, seed: int = 0, device=None,
-                     log_every: int = 0):
+                     log_every: int = 0, clip_quantile: float | None = 0.999):
     """Steps 1-3 of the module docstring. `params` are backward single-layer parameters of the
-    problem (the density the forward estimator transports). Returns (mlp, info)."""
+    problem (the density the forward estimator transports). The labels are clamped to the
+    clip_quantile quantile of their magnitude (wob_clip_magnitude_quantile; None: unclipped) --
+    the walk's density estimates are heavy-tailed, and the fit only has to be close, not unbiased,
+    for the control variate to stay unbiased. Returns (mlp, info)."""
     import dataclasses
 
     import torch
@@ -149,8 +152,12 @@ def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256
                                             n_train, s.data_ptr(), q.data_ptr(), b.data_ptr(), None))
     torch.cuda.synchronize()
     t_labels = time.perf_counter() - t0
-    labels = (s / train_paths).float()
+    labels = (s / train_paths).float().contiguous()
     label_var = (q / train_paths - (s / train_paths) ** 2).clamp(min=0) / train_paths
+    clip_t = torch.zeros(1, dtype=torch.float32, device=dev)
+    if clip_quantile is not None:
+        check(load().wob_clip_magnitude_quantile(labels.data_ptr(), n_train, float(clip_quantile), clip_t.data_ptr(),
+                                                 None))
     x = torch.cat([d["p"], d["n"]], dim=1).contiguous()
     if scene.dim == 2:  # (x, y, 0, nx, ny, 0)
         z = torch.zeros(n_train, 1, device=dev)
@@ -167,7 +174,8 @@ def train_density_cv(scene, params, n_train: int = 65536, train_paths: int = 256
     hist = [(int(i), float(lh[i])) for i in range(0, steps, every)] + [(steps - 1, float(lh[-1]))]
     info = dict(n_train=n_train, train_paths=train_paths, steps=steps, batch=batch, t_labels_s=t_labels,
                 t_train_s=t_train, label_noise_var=float(label_var.mean().item()), history=hist,
-                label_bounces=int(b.item()))
+                label_bounces=int(b.item()), clip_quantile=clip_quantile,
+                clip_threshold=float(clip_t.item()) if clip_quantile is not None else None)
     return mlp, info
 
 
