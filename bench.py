@@ -595,7 +595,7 @@ def run_batch(args):
 
 
 def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, plain_budget=20.0, cv_budget=5.0,
-                    train_steps=2000, near_factor=3.0, seed=SEED):
+                    train_steps=2000, near_factor=3.0, theta=0.3, seed=SEED):
     """Time to RMSE `target` against the analytic solution, plain forward WoB vs the learned
     residual control variate, on the exterior Neumann workload: displaced icosphere (0.15 sum
     c_lm Y_lm, l <= 4) subdivided `subdiv` times (7: 327,680 triangles), Neumann data of
@@ -681,9 +681,9 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
     mlp, info = cv.train_density_cv(scene, base, n_train=65536, train_paths=256, steps=train_steps, batch=8192,
                                     lr=2e-3, freq_sigma=1.0, seed=seed)
     t1 = clock()
-    rscene, sigma = cv.residual_control_variate(scene, mlp, wob.ExteriorDomain, near_factor=near_factor)
+    rscene, sigma = cv.residual_control_variate(scene, mlp, wob.ExteriorDomain, near_factor=near_factor, theta=theta)
     t2 = clock()
-    pot = cv.control_variate_potential(scene, sigma, d_pts, n_pts, near_factor=near_factor)
+    pot = cv.control_variate_potential(scene, sigma, d_pts, n_pts, near_factor=near_factor, theta=theta)
     u_cv = pot[:, 0].double().cpu().numpy()
     t3 = clock()
     setup = t3 - t0
@@ -702,6 +702,7 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
         "forward_walk_autotune": {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
         "train_loss_first_last": [info["history"][0][1], info["history"][-1][1]],
         "label_clip": {"quantile": info["clip_quantile"], "threshold": info["clip_threshold"]},
+        "cv_tables": {"near_factor": near_factor, "cluster_theta": theta},
         "plain_curve": plain_curve[::max(1, len(plain_curve) // 8)], "cv_curve": cv_curve,
         "clock": "wall time on a synchronised device; RMSE evaluation excluded; CV time includes its setup",
     }
@@ -720,7 +721,8 @@ def run_cv(args):
     wob.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     res = cv_time_to_rmse(dev, subdiv=args.cv_subdiv, plain_paths=args.cv_paths, plain_budget=args.cv_budget,
-                          cv_budget=args.cv_budget, near_factor=args.cv_near)
+                          cv_budget=args.cv_budget, near_factor=args.cv_near,
+                          theta=args.cv_theta)
     out = {
         "metric": "time to RMSE 1e-3 vs analytic, plain vs learned-CV WoB (3D exterior Neumann)",
         "value": res["plain_over_cv"], "unit": "x (plain time / CV time including its setup)", "n_gpus": world,
@@ -1197,6 +1199,8 @@ def main():
     ap.add_argument("--cv-paths", type=int, default=256, help="plain paths per point per iteration of --workload cv3d")
     ap.add_argument("--cv-budget", type=float, default=20.0, help="seconds per estimator of --workload cv3d")
     ap.add_argument("--cv-near", type=float, default=3.0, help="near-field factor of the control-variate tables")
+    ap.add_argument("--cv-theta", type=float, default=0.3,
+                    help="cluster acceptance of the control-variate tables' far field (0: every triangle)")
     ap.add_argument("--no-time-to-rmse", action="store_true",
                     help="skip the plain vs learned-CV time-to-RMSE leg of the default workload")
     ap.add_argument("--mrhs-subdiv", type=int, default=8, help="icosphere subdivision of --workload mrhs3d")

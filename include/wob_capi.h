@@ -391,7 +391,11 @@ int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters
  * wob_cv_residual_data: delta_j at the centroid of every stored triangle (device [n_elems]).
  * wob_cv_potential: S sigma~ and its gradient at points (device [n][3] in, [n][4] out: u, grad u).
  * Both sum over all triangles: the centroid rule beyond near_factor times a triangle's longest
- * edge, the closed form of a uniformly charged triangle (Wilton et al. 1984) nearer. 3D scenes.
+ * edge, the closed form of a uniformly charged triangle (Wilton et al. 1984) nearer. With
+ * theta > 0 the far field of a cluster of 32 consecutive stored triangles is its quadrupole
+ * expansion wherever the cluster's radius is below theta times its distance from every target of
+ * a warp (and beyond the triangles' near radii); theta = 0 sums every triangle. theta = 0.3 adds
+ * about 2e-4 (relative to the largest value) to the centroid rule's own error. 3D scenes.
  * wob_scene_clone: an independent copy of a scene (geometry, records, tables, volume cache).
  * wob_scene_add_boundary_offsets: adds delta_j to the vertex values of stored element j (delta on
  * the device when delta_on_device != 0, else on the host) and rebuilds the |g| sampling tables;
@@ -401,9 +405,9 @@ int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters
  * wob_scene_element_frames: (centroid, normal) of every stored element, the network's input there:
  * device [n_elems][6] (2D scenes: (x, y, 0, nx, ny, 0)).
  */
-int wob_cv_residual_data(wob_scene scene, const float *sigma, int domain, float near_factor, float *delta,
-                         void *stream);
-int wob_cv_potential(wob_scene scene, const float *sigma, float near_factor, const float *points,
+int wob_cv_residual_data(wob_scene scene, const float *sigma, int domain, float near_factor, float theta,
+                         float *delta, void *stream);
+int wob_cv_potential(wob_scene scene, const float *sigma, float near_factor, float theta, const float *points,
                      uint32_t n_points, float *out, void *stream);
 int wob_scene_clone(wob_scene scene, wob_scene *out);
 int wob_scene_add_boundary_offsets(wob_scene scene, const float *delta, uint32_t n_elems, int delta_on_device,

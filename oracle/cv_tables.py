@@ -21,6 +21,13 @@ s+ = (b - rho).s, t = (a - rho).m, R0^2 = t^2 + h^2, R- = |x - a|, R+ = |x - b|,
 The engine's kernels (csrc/k_cv_tables.cu) evaluate these for triangles near the target and the
 one-point (centroid) rule A_T / |x - c_T| far away; residual_data and potential below evaluate the
 same split in float64 for the tests, and with near_factor large the closed forms everywhere.
+
+With theta > 0 the kernels also take whole clusters (32 consecutive stored triangles) by the
+quadrupole expansion of their centroid sources about the cluster's mean centroid z, wherever the
+cluster is farther than max(rho / theta, rho + eta) (rho: its radius about z, eta: its largest
+near radius) plus omega from the centre W of the 32 consecutive targets of a warp (omega: their
+radius about W), the triangles in storage order and the evaluation points in Morton order
+(_morton_order). _cluster_far restates that decision and _cluster_field the expansion.
 """
 from __future__ import annotations
 
@@ -98,7 +105,85 @@ def _tri_arrays(verts):
     return a, b, c, cen, area, h2
 
 
-def residual_data(verts, normals, sigma, c_coef: float, near_factor: float, chunk: int = 256):
+def _clusters(cen, w, near2, theta, size=32):
+    """Per cluster: centre z, far radius, M0, M1, M2 (float64)."""
+    nc = (len(cen) + size - 1) // size
+    z = np.zeros((nc, 3)); r_far = np.full(nc, np.inf); M0 = np.zeros(nc); M1 = np.zeros((nc, 3))
+    M2 = np.zeros((nc, 3, 3))
+    for k in range(nc):
+        sl = slice(k * size, min(len(cen), (k + 1) * size))
+        z[k] = cen[sl].mean(0)
+        d = cen[sl] - z[k]
+        rho = np.sqrt((d ** 2).sum(1)).max()
+        eta = np.sqrt(near2[sl].max())
+        if theta > 0:
+            r_far[k] = max(rho / theta, rho + eta)
+        M0[k] = w[sl].sum()
+        M1[k] = (w[sl, None] * d).sum(0)
+        M2[k] = np.einsum("i,ij,ik->jk", w[sl], d, d)
+    return z, r_far, M0, M1, M2
+
+
+def _cluster_far(x_group, z, r_far):
+    W = x_group.mean(0)
+    om = np.sqrt(((x_group - W) ** 2).sum(1)).max()
+    return ((W - z) ** 2).sum(1) > (r_far + om) ** 2
+
+
+def _cluster_field(x, z, M0, M1, M2):
+    """sum over the given clusters of the quadrupole expansion of sum w / |x - c| and its gradient,
+    for points x [m, 3]: returns phi [m], grad [m, 3]."""
+    R = x[:, None, :] - z[None, :, :]
+    R2 = (R ** 2).sum(-1)
+    Rn = np.sqrt(R2)
+    RM1 = (R * M1[None]).sum(-1)
+    M2R = np.einsum("kij,mkj->mki", M2, R)
+    RM2R = (R * M2R).sum(-1)
+    t = np.trace(M2, axis1=1, axis2=2)[None, :]
+    Q = 3 * RM2R - R2 * t
+    phi = (M0[None] / Rn + RM1 / Rn ** 3 + Q / (2 * Rn ** 5)).sum(1)
+    a = -M0[None] / Rn ** 3 - 3 * RM1 / Rn ** 5 - t / Rn ** 5 - 2.5 * Q / Rn ** 7
+    g = (a[..., None] * R + M1[None] / Rn[..., None] ** 3 + 3 * M2R / Rn[..., None] ** 5).sum(1)
+    return phi, g
+
+
+def _morton_order(points):
+    """The engine's Morton order of evaluation points: 10 bits a coordinate of (p - lo) / (hi - lo)
+    in float32 over the points' bounds, codes interleaved x, y, z from the low bit, ties by index."""
+    p = np.asarray(points, np.float32)
+    lo, hi = p.min(0), p.max(0)
+    code = np.zeros(len(p), np.uint64)
+    for k in range(3):
+        if hi[k] > lo[k]:
+            t = (p[:, k] - lo[k]) / np.float32(hi[k] - lo[k])
+        else:
+            t = np.zeros(len(p), np.float32)
+        q = np.minimum(np.maximum(t * np.float32(1024.0), np.float32(0.0)), np.float32(1023.0)).astype(np.uint64)
+        for b in range(10):
+            code |= ((q >> np.uint64(b)) & np.uint64(1)) << np.uint64(3 * b + k)
+    return np.lexsort((np.arange(len(p)), code))
+
+
+def _cluster_split(tx, cen, w, near2, theta, size=32, order=None):
+    """Per target: the far clusters' expansion (phi, grad) and the mask [targets, sources] of the
+    sources still summed pair by pair, for targets tx in warps of 32 consecutive ones."""
+    z, r_far, M0, M1, M2 = _clusters(cen, w, near2, theta, size)
+    phi = np.zeros(len(tx)); g = np.zeros((len(tx), 3))
+    pair = np.ones((len(tx), len(cen)), bool)
+    order = np.arange(len(tx)) if order is None else order
+    for g0 in range(0, len(tx), 32):
+        grp = order[g0:g0 + 32]
+        far = _cluster_far(tx[grp], z, r_far)
+        if far.any():
+            ph, gr = _cluster_field(tx[grp], z[far], M0[far], M1[far], M2[far])
+            phi[grp] += ph
+            g[grp] += gr
+            for k in np.nonzero(far)[0]:
+                pair[np.ix_(grp, np.arange(k * size, min(len(cen), (k + 1) * size)))] = False
+    return phi, g, pair
+
+
+def residual_data(verts, normals, sigma, c_coef: float, near_factor: float, chunk: int = 256, theta: float = 0.0):
     """delta_j = ((T sigma~)(c_j) - sigma~_j) / c for every triangle j of the stored arrays, with the
     kernel's split: closed form for pairs with |c_j - c_i|^2 < near_factor^2 h_i^2 (h_i the longest
     edge of i), centroid rule otherwise, the triangle's own term zero (k_cv_tables.cu)."""
@@ -107,14 +192,19 @@ def residual_data(verts, normals, sigma, c_coef: float, near_factor: float, chun
     sig = np.asarray(sigma, np.float64)
     near2 = near_factor ** 2 * h2
     out = np.zeros(len(cen))
+    if theta > 0:
+        _, cg, pair = _cluster_split(cen, cen, area * sig, near2, theta)
+    else:
+        cg, pair = np.zeros((len(cen), 3)), None
     for j0 in range(0, len(cen), chunk):
         j1 = min(len(cen), j0 + chunk)
         d = cen[j0:j1, None, :] - cen[None, :, :]
         r2 = (d ** 2).sum(-1)
-        near = r2 < near2[None, :]
+        take = np.ones(r2.shape, bool) if pair is None else pair[j0:j1]
+        near = (r2 < near2[None, :]) & take
         with np.errstate(divide="ignore", invalid="ignore"):
-            far = np.where(near, 0.0, (d * n[j0:j1, None, :]).sum(-1) / r2 ** 1.5 * (area * sig)[None, :])
-        acc = far.sum(1)
+            far = np.where(near | ~take, 0.0, (d * n[j0:j1, None, :]).sum(-1) / r2 ** 1.5 * (area * sig)[None, :])
+        acc = far.sum(1) - (cg[j0:j1] * n[j0:j1]).sum(1)
         jj, ii = np.nonzero(near)
         jj = jj + j0
         keep = jj != ii
@@ -126,23 +216,28 @@ def residual_data(verts, normals, sigma, c_coef: float, near_factor: float, chun
     return out
 
 
-def potential(verts, sigma, points, near_factor: float, chunk: int = 128):
+def potential(verts, sigma, points, near_factor: float, chunk: int = 128, theta: float = 0.0):
     """u~(x) = (1/4 pi) sum_i sigma~_i P_i(x) and its gradient at points ([n, 4]), same split."""
     a, b, c, cen, area, h2 = _tri_arrays(verts)
     sig = np.asarray(sigma, np.float64)
     x = np.asarray(points, np.float64)
     near2 = near_factor ** 2 * h2
     out = np.zeros((len(x), 4))
+    if theta > 0:
+        cphi, cg, pair = _cluster_split(x, cen, area * sig, near2, theta, order=_morton_order(points))
+    else:
+        cphi, cg, pair = np.zeros(len(x)), np.zeros((len(x), 3)), None
     for p0 in range(0, len(x), chunk):
         p1 = min(len(x), p0 + chunk)
         d = x[p0:p1, None, :] - cen[None, :, :]
         r2 = (d ** 2).sum(-1)
-        near = r2 < near2[None, :]
+        take = np.ones(r2.shape, bool) if pair is None else pair[p0:p1]
+        near = (r2 < near2[None, :]) & take
         w = (area * sig)[None, :]
         with np.errstate(divide="ignore", invalid="ignore"):
-            u = np.where(near, 0.0, w / np.sqrt(r2))
-            gr = np.where(near[..., None], 0.0, -w[..., None] * d / r2[..., None] ** 1.5)
-        acc = np.concatenate([u.sum(1)[:, None], gr.sum(1)], 1)
+            u = np.where(near | ~take, 0.0, w / np.sqrt(r2))
+            gr = np.where((near | ~take)[..., None], 0.0, -w[..., None] * d / r2[..., None] ** 1.5)
+        acc = np.concatenate([(u.sum(1) + cphi[p0:p1])[:, None], gr.sum(1) + cg[p0:p1]], 1)
         pj, ii = np.nonzero(near)
         P, G = triangle_potential(x[p0 + pj], a[ii], b[ii], c[ii])
         np.add.at(acc, pj, np.concatenate([(sig[ii] * P)[:, None], sig[ii][:, None] * G], 1))

@@ -31,3 +31,41 @@ def test_split_tends_to_closed_form():
     errs = [np.abs(T.residual_data(verts, normals, sig, -2.0, k) - exact).max() for k in (1.0, 2.0, 4.0)]
     assert errs[0] > errs[1] > errs[2]
     assert errs[2] < 2e-2 * np.abs(exact).max()
+
+
+def _median_order(cen, ids=None):
+    """Storage order of a median-split hierarchy (spatially compact runs, as the BVH's leaf order)."""
+    if ids is None:
+        ids = np.arange(len(cen))
+    if len(ids) <= 4:
+        return list(ids)
+    c = cen[ids]
+    ax = int(np.argmax(c.max(0) - c.min(0)))
+    o = np.argsort(c[:, ax], kind="stable")
+    mid = len(ids) // 2
+    return _median_order(cen, ids[o[:mid]]) + _median_order(cen, ids[o[mid:]])
+
+
+def test_cluster_expansion_close_to_pairwise():
+    """theta = 0.3: clusters of 32 taken by their quadrupole expansion change the residual data
+    and the potential by well under the pairwise split's own error; theta = 0 is the pairwise sum."""
+    from wobtoolbox_gb300 import workloads as W
+    V, F, _ = W.displaced_icosphere(4, 0.15, 4, 0)
+    verts, normals = W.mesh_elements(V, F)
+    cen = verts.astype(np.float64).mean(1)
+    order = np.array(_median_order(cen))
+    v, n = verts[order], normals[order]
+    c = v.astype(np.float64).mean(1)
+    sig = 0.05 + 0.02 * np.sin(3 * c[:, 0]) * np.cos(2 * c[:, 1]) + 0.01 * c[:, 2]
+    ref = T.residual_data(v, n, sig, -2.0, 3.0)
+    assert np.array_equal(T.residual_data(v, n, sig, -2.0, 3.0, theta=0.0), ref)
+    got = T.residual_data(v, n, sig, -2.0, 3.0, theta=0.3)
+    assert np.abs(got - ref).max() < 2e-4 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
+    assert not np.array_equal(got, ref)  # clusters were taken
+    rng = np.random.default_rng(0)
+    d = rng.standard_normal((64, 3))
+    pts = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(1.5, 3.0, (64, 1))
+    pr = T.potential(v, sig, pts, 3.0)
+    pg = T.potential(v, sig, pts, 3.0, theta=0.3)
+    scale = np.abs(pr).max(0)
+    assert np.all(np.abs(pg - pr) <= 2e-4 * scale), (np.abs(pg - pr) / scale).max()

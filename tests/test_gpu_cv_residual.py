@@ -122,12 +122,15 @@ def _ext_neumann_scene(engine):
     return case, engine.SceneHost(case["verts"], case["normals"], case["bvals"], case["types"])
 
 
-def test_cv_tables_match_float64(engine, cuda):
+@pytest.mark.parametrize("theta", [0.0, 0.3])
+def test_cv_tables_match_float64(engine, cuda, theta):
+    """Pairwise (theta 0) and with clusters taken by their expansion (theta 0.3, the same cluster
+    decisions restated in float64); the 5,120-triangle scene has 160 clusters."""
     from oracle import cv_tables as T
     from wobtoolbox_gb300 import cv
     from wobtoolbox_gb300 import workloads as W
     torch = cuda
-    V, F, _ = W.displaced_icosphere(3, 0.15, 4, 0)
+    V, F, _ = W.displaced_icosphere(4, 0.15, 4, 0)
     verts, normals = W.mesh_elements(V, F)
     g = np.ones((len(F), 3), np.float32)
     scene = engine.SceneHost(verts, normals, g, np.ones(len(F), np.int32))
@@ -139,12 +142,15 @@ def test_cv_tables_match_float64(engine, cuda):
     assert np.abs(frames[:, :3] - cen).max() < 1e-6 and np.array_equal(frames[:, 3:], n)
     for domain, c in ((1, -2.0), (0, 2.0)):
         delta = torch.zeros(len(F), device="cuda")
-        engine.check(engine.load().wob_cv_residual_data(scene.handle, d_sig.data_ptr(), domain, 3.0,
+        engine.check(engine.load().wob_cv_residual_data(scene.handle, d_sig.data_ptr(), domain, 3.0, theta,
                                                         delta.data_ptr(), None))
         torch.cuda.synchronize()
-        ref = T.residual_data(v, n, sig, c, 3.0)
+        ref = T.residual_data(v, n, sig, c, 3.0, theta=theta)
         got = delta.cpu().numpy()
         assert np.abs(got - ref).max() < 2e-4 * np.abs(ref).max(), np.abs(got - ref).max()
+        if theta > 0:  # and close to the pairwise sum
+            dense = T.residual_data(v, n, sig, c, 3.0)
+            assert np.abs(got - dense).max() < 4e-4 * np.abs(dense).max()
     # potential at points far from and close to the surface (down to 1e-3 of the radius)
     rng = np.random.default_rng(3)
     dirs = rng.standard_normal((200, 3))
@@ -152,10 +158,11 @@ def test_cv_tables_match_float64(engine, cuda):
     k = rng.integers(0, len(F), 100)
     near_pts = cen[k] + n[k].astype(np.float64) * rng.uniform(1e-3, 0.05, (100, 1))
     pts = np.concatenate([dirs[:100] * 2.0, near_pts]).astype(np.float32)
-    out = cv.control_variate_potential(scene, d_sig, torch.from_numpy(pts).cuda(), len(pts), near_factor=3.0)
+    out = cv.control_variate_potential(scene, d_sig, torch.from_numpy(pts).cuda(), len(pts), near_factor=3.0,
+                                       theta=theta)
     torch.cuda.synchronize()
     got = out.cpu().numpy()
-    ref = T.potential(v, sig, pts, 3.0)
+    ref = T.potential(v, sig, pts, 3.0, theta=theta)
     scale = np.abs(ref).max(0)
     assert np.all(np.abs(got - ref) <= 2e-4 * scale + 1e-7), np.abs(got - ref).max(0)
     # the split against the closed form at every pair (the far-field rule's error)

@@ -106,8 +106,8 @@ def load() -> C.CDLL:
         "wob_batch_destroy": (C.c_int, [vp]),
         "wob_solve_unknown_boundary": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp]),
         "wob_scene_set_control_variate": (C.c_int, [vp, vp, u32]),
-        "wob_cv_residual_data": (C.c_int, [vp, vp, C.c_int, f32, vp, vp]),
-        "wob_cv_potential": (C.c_int, [vp, vp, f32, vp, u32, vp, vp]),
+        "wob_cv_residual_data": (C.c_int, [vp, vp, C.c_int, f32, f32, vp, vp]),
+        "wob_cv_potential": (C.c_int, [vp, vp, f32, f32, vp, u32, vp, vp]),
         "wob_scene_clone": (C.c_int, [vp, P(vp)]),
         "wob_scene_add_boundary_offsets": (C.c_int, [vp, vp, u32, C.c_int, vp]),
         "wob_scene_element_frames": (C.c_int, [vp, vp, vp]),

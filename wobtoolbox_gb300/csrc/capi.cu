@@ -979,21 +979,26 @@ int scene_add_boundary_offsets_impl(wob_scene s, const float *delta, uint32_t n,
     return WOB_OK;
 }
 
-// Triangle sources of sigma~ in a scratch allocation freed on return.
+// Triangle sources and clusters of sigma~ in a scratch allocation freed on return.
 struct CvSources {
-    DevBuf src, near2;
+    DevBuf src, near2, clusters;
 };
-int cv_sources(wob_scene s, const float *sigma, float near_factor, CvSources &cs, cudaStream_t st) {
+int cv_sources(wob_scene s, const float *sigma, float near_factor, float theta, CvSources &cs, cudaStream_t st) {
     if (s->host.dim != 3) return fail(WOB_ERR_UNSUPPORTED, "the control-variate tables are implemented for 3D scenes");
     if (!sigma) return fail(WOB_ERR_INVALID_ARGUMENT, "sigma is required");
     if (!(near_factor >= 0.0f) || !(near_factor < 1e6f)) return fail(WOB_ERR_INVALID_ARGUMENT, "near_factor must be in [0, 1e6)");
+    if (!(theta >= 0.0f) || !(theta < 1.0f)) return fail(WOB_ERR_INVALID_ARGUMENT, "theta must be in [0, 1)");
     const size_t n = s->host.n;
+    const size_t n_cl = (n + 31) / 32;
     cudaError_t e;
-    if ((e = cudaMalloc(&cs.src.ptr, n * 16)) != cudaSuccess || (e = cudaMalloc(&cs.near2.ptr, n * 4)) != cudaSuccess)
+    if ((e = cudaMalloc(&cs.src.ptr, n * 16)) != cudaSuccess || (e = cudaMalloc(&cs.near2.ptr, n * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&cs.clusters.ptr, n_cl * 64)) != cudaSuccess)
         return fail_cuda(e, "allocating the control-variate sources");
     cs.src.bytes = n * 16;
     cs.near2.bytes = n * 4;
-    e = wobgb::launch_cv_sources(s->view<3>(), sigma, near_factor, (float4 *)cs.src.ptr, (float *)cs.near2.ptr, st);
+    cs.clusters.bytes = n_cl * 64;
+    e = wobgb::launch_cv_sources(s->view<3>(), sigma, near_factor, theta, (float4 *)cs.src.ptr, (float *)cs.near2.ptr,
+                                 (float4 *)cs.clusters.ptr, st);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate sources");
 }
 }  // namespace
@@ -1058,7 +1063,8 @@ int wob_scene_add_boundary_offsets(wob_scene scene, const float *delta, uint32_t
     return guarded([&] { return scene_add_boundary_offsets_impl(scene, delta, n_elems, delta_on_device, stream); });
 }
 
-int wob_cv_residual_data(wob_scene s, const float *sigma, int domain, float near_factor, float *delta, void *stream) {
+int wob_cv_residual_data(wob_scene s, const float *sigma, int domain, float near_factor, float theta, float *delta,
+                         void *stream) {
     return guarded([&] {
         if (!s || !delta) return fail(WOB_ERR_INVALID_ARGUMENT, "scene and delta are required");
         if (domain != WOB_INTERIOR_DOMAIN && domain != WOB_EXTERIOR_DOMAIN)
@@ -1066,23 +1072,24 @@ int wob_cv_residual_data(wob_scene s, const float *sigma, int domain, float near
         DeviceGuard g(s->device);
         cudaStream_t st = (cudaStream_t)stream;
         CvSources cs;
-        int r = cv_sources(s, sigma, near_factor, cs, st);
+        int r = cv_sources(s, sigma, near_factor, theta, cs, st);
         if (r == WOB_OK) {
             // c = domain_type_coefficient / integral_free_term(1/2) (bie_models.cuh:66-78)
             const float c = domain == WOB_INTERIOR_DOMAIN ? 2.0f : -2.0f;
             cudaError_t e = wobgb::launch_cv_residual(s->view<3>(), (const float4 *)cs.src.ptr, (const float *)cs.near2.ptr,
-                                                      sigma, c, delta, st);
+                                                      (const float4 *)cs.clusters.ptr, sigma, c, delta, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) r = fail_cuda(e, "computing the residual data");
         }
         cs.src.release();
         cs.near2.release();
+        cs.clusters.release();
         return r;
     });
 }
 
-int wob_cv_potential(wob_scene s, const float *sigma, float near_factor, const float *points, uint32_t n_points,
-                     float *out, void *stream) {
+int wob_cv_potential(wob_scene s, const float *sigma, float near_factor, float theta, const float *points,
+                     uint32_t n_points, float *out, void *stream) {
     return guarded([&] {
         if (!s) return fail(WOB_ERR_INVALID_ARGUMENT, "scene is NULL");
         if (n_points == 0) return (int)WOB_OK;
@@ -1090,15 +1097,24 @@ int wob_cv_potential(wob_scene s, const float *sigma, float near_factor, const f
         DeviceGuard g(s->device);
         cudaStream_t st = (cudaStream_t)stream;
         CvSources cs;
-        int r = cv_sources(s, sigma, near_factor, cs, st);
+        DevBuf order;
+        int r = cv_sources(s, sigma, near_factor, theta, cs, st);
         if (r == WOB_OK) {
-            cudaError_t e = wobgb::launch_cv_potential(s->view<3>(), (const float4 *)cs.src.ptr, (const float *)cs.near2.ptr,
-                                                       sigma, points, n_points, out, st);
+            const size_t words = wobgb::cv_point_order_words(n_points);
+            cudaError_t e = cudaMalloc(&order.ptr, words * 4);
+            if (e == cudaSuccess) {
+                order.bytes = words * 4;
+                e = wobgb::launch_cv_potential(s->view<3>(), (const float4 *)cs.src.ptr, (const float *)cs.near2.ptr,
+                                               (const float4 *)cs.clusters.ptr, sigma, points, n_points,
+                                               (uint32_t *)order.ptr, out, st);
+            }
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) r = fail_cuda(e, "computing the control-variate potential");
         }
         cs.src.release();
         cs.near2.release();
+        cs.clusters.release();
+        order.release();
         return r;
     });
 }

@@ -21,13 +21,20 @@
 // triangle's own term in the residual data is zero: n_j is normal to triangle j, so dG/dn_x
 // vanishes on it.
 //
-// Work decomposition: two targets per thread (one where two would leave SMs idle), 256 threads per
-// block; the sources stream through shared memory in tiles of 256 {centroid, sigma~ A, near
-// radius^2}, read as broadcasts. Far pairs
-// cost one rsqrt and a dozen FMAs; a warp in which any lane has a near pair takes the closed form
-// for those lanes (the targets of a warp and the sources of a tile are both consecutive in BVH
-// storage order, so near pairs come in spatial clusters). FP32 partial sums per tile, FP64 across
-// tiles. This unit is compiled with FMA contraction (it is not part of the bit-exact walk).
+// Far field by clusters (a two-level treecode): the stored triangles are cut into clusters of 32
+// consecutive ones (BVH storage order keeps them spatially compact), each with its centre z (mean
+// centroid), radius rho, largest near radius eta and the moments of its centroid sources about z
+// up to the quadrupole (M0 = sum w, M1 = sum w d, M2 = sum w d d^T, w = sigma~ A, d = c - z).
+// A warp takes 32 consecutive targets and the bounding sphere (W, omega) of their positions; a
+// cluster with |W - z| > max(rho / theta, rho + eta) + omega is far from every target of the warp
+// and enters through its quadrupole expansion of sum w / |x - c| (one evaluation instead of 32,
+// error of order (rho / |x - z|)^3 of the cluster's share); any other cluster is taken triangle by
+// triangle as above. theta = 0 takes every triangle (the dense sum). The decision is uniform
+// across the warp, so lanes never diverge between the two.
+//
+// Work decomposition: one warp per 32 targets, 8 warps a block, every warp walks the cluster table
+// in order (records read as broadcasts). FP32 partial sums over 32 clusters, FP64 across them.
+// This unit is compiled with FMA contraction (it is not part of the bit-exact walk).
 #include "device_common.cuh"
 #include "launch.hpp"
 
@@ -137,114 +144,238 @@ __global__ void cv_sources_kernel(SceneView<3> s, const float *__restrict__ sigm
     near2[i] = near_factor * near_factor * h2;
 }
 
+constexpr int kClusterSize = 32;
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Morton order of evaluation points: bounds (order-preserving integer atomics), 30-bit codes (10
+// bits a coordinate), a bitonic sort of {code, index} keys padded to a power of two.
+__device__ __forceinline__ uint32_t ordered_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered_bits(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ uint32_t spread_bits10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__global__ void bounds_init_kernel(uint32_t *bb) {
+    if (threadIdx.x < 6) bb[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
+}
+__global__ void pts_bounds_kernel(const float *__restrict__ pts, uint32_t n, uint32_t *__restrict__ bb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 3; k++) {
+        const uint32_t o = ordered_bits(pts[(size_t)i * 3 + k]);
+        atomicMin(bb + k, o);
+        atomicMax(bb + 3 + k, o);
+    }
+}
+__global__ void pts_morton_kernel(const float *__restrict__ pts, uint32_t n, uint32_t n2, const uint32_t *__restrict__ bb,
+                                  uint64_t *__restrict__ key) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n2) return;
+    if (i >= n) {
+        key[i] = ~0ull;
+        return;
+    }
+    uint32_t code = 0;
+    for (int k = 0; k < 3; k++) {
+        const float lo = from_ordered_bits(bb[k]), hi = from_ordered_bits(bb[3 + k]);
+        const float t = hi > lo ? (pts[(size_t)i * 3 + k] - lo) / (hi - lo) : 0.0f;
+        const uint32_t q = (uint32_t)fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+        code |= spread_bits10(q) << k;
+    }
+    key[i] = ((uint64_t)code << 32) | i;
+}
+__global__ void bitonic_kernel(uint32_t n2, uint32_t j, uint32_t k, uint64_t *__restrict__ key) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n2) return;
+    const uint32_t l = i ^ j;
+    if (l <= i) return;
+    const uint64_t a = key[i], b = key[l];
+    if (((i & k) == 0) == (a > b)) {
+        key[i] = b;
+        key[l] = a;
+    }
+}
+
+// One warp per cluster: the record {z, r_far}, {M0, M1}, {M2xx, M2yy, M2zz, M2xy}, {M2xz, M2yz,
+// trace M2, 0}; r_far = max(rho / theta, rho + eta), infinite for theta = 0.
+__global__ void cv_cluster_kernel(uint32_t n, const float4 *__restrict__ src, const float *__restrict__ near2,
+                                  float theta, float4 *__restrict__ cl) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_cl = (n + kClusterSize - 1) / kClusterSize;
+    if (k >= n_cl) return;
+    const uint32_t i = k * kClusterSize + lane;
+    const bool valid = i < n;
+    const float4 q = valid ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float e2 = valid ? __ldg(near2 + i) : 0.0f;
+    const float cnt = (float)__popc(__ballot_sync(0xffffffffu, valid));
+    const float zx = warp_sum_f(q.x) / cnt, zy = warp_sum_f(q.y) / cnt, zz = warp_sum_f(q.z) / cnt;
+    const float dx = valid ? q.x - zx : 0.0f, dy = valid ? q.y - zy : 0.0f, dz = valid ? q.z - zz : 0.0f;
+    const float rho = sqrtf(warp_max_f(dx * dx + dy * dy + dz * dz));
+    const float eta = sqrtf(warp_max_f(e2));
+    const float w = q.w;
+    const float m0 = warp_sum_f(w);
+    const float m1x = warp_sum_f(w * dx), m1y = warp_sum_f(w * dy), m1z = warp_sum_f(w * dz);
+    const float mxx = warp_sum_f(w * dx * dx), myy = warp_sum_f(w * dy * dy), mzz = warp_sum_f(w * dz * dz);
+    const float mxy = warp_sum_f(w * dx * dy), mxz = warp_sum_f(w * dx * dz), myz = warp_sum_f(w * dy * dz);
+    if (lane == 0) {
+        const float r_far = theta > 0.0f ? fmaxf(rho / theta, rho + eta) : __int_as_float(0x7f800000);
+        cl[4 * k + 0] = make_float4(zx, zy, zz, r_far);
+        cl[4 * k + 1] = make_float4(m0, m1x, m1y, m1z);
+        cl[4 * k + 2] = make_float4(mxx, myy, mzz, mxy);
+        cl[4 * k + 3] = make_float4(mxz, myz, mxx + myy + mzz, 0.0f);
+    }
+}
+
+// sum w / |x - c| over a cluster by its quadrupole expansion about z (R = x - z):
+//   phi = M0 / R + (R . M1) / R^3 + (3 R.M2.R - R^2 tr M2) / (2 R^5),
+// and its gradient term by term.
+__device__ __forceinline__ void cluster_field(const float x[3], const float4 &q0, const float4 &q1, const float4 &q2,
+                                             const float4 &q3, float &phi, float g[3]) {
+    const float R[3] = {x[0] - q0.x, x[1] - q0.y, x[2] - q0.z};
+    const float R2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+    const float ri = rsqrtf(R2);
+    const float ri2 = ri * ri, ri3 = ri * ri2, ri5 = ri3 * ri2;
+    const float RM1 = R[0] * q1.y + R[1] * q1.z + R[2] * q1.w;
+    const float M2R[3] = {q2.x * R[0] + q2.w * R[1] + q3.x * R[2], q2.w * R[0] + q2.y * R[1] + q3.y * R[2],
+                          q3.x * R[0] + q3.y * R[1] + q2.z * R[2]};
+    const float RM2R = R[0] * M2R[0] + R[1] * M2R[1] + R[2] * M2R[2];
+    const float Q = 3.0f * RM2R - R2 * q3.z;
+    phi = q1.x * ri + RM1 * ri3 + 0.5f * Q * ri5;
+    const float a = -q1.x * ri3 - 3.0f * RM1 * ri5 - q3.z * ri5 - 2.5f * Q * ri5 * ri2;
+    const float m1[3] = {q1.y, q1.z, q1.w};
+#pragma unroll
+    for (int k = 0; k < 3; k++) g[k] = a * R[k] + m1[k] * ri3 + 3.0f * M2R[k] * ri5;
+}
+
 // kMode 0: residual data at the stored triangles' centroids; kMode 1: potential and gradient at
-// points (out: [n][4] = u, du/dx, du/dy, du/dz). Each thread takes kTgt targets (a block covers
-// kTgt x 256), so every source read from shared memory serves kTgt pairs; one target per thread
-// where two would leave SMs without a block.
-template <int kMode, int kTgt>
+// points (out: [n][4] = u, du/dx, du/dy, du/dz).
+template <int kMode>
 __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const float4 *__restrict__ src,
                                                           const float *__restrict__ near2,
                                                           const float *__restrict__ sigma,
-                                                          const float *__restrict__ pts, uint32_t n_targets,
+                                                          const float4 *__restrict__ cl, const float *__restrict__ pts,
+                                                          const uint64_t *__restrict__ order, uint32_t n_targets,
                                                           float c_coef, float *__restrict__ out) {
-    __shared__ float4 s_src[kCvBlock];
-    __shared__ float s_n2[kCvBlock];
-    uint32_t tgt[kTgt];
-    bool active[kTgt];
-    float xd[kTgt][3], nn[kTgt][3];
-    for (int t = 0; t < kTgt; t++) {
-        tgt[t] = blockIdx.x * (kCvBlock * kTgt) + t * kCvBlock + threadIdx.x;
-        active[t] = tgt[t] < n_targets;
-        for (int k = 0; k < 3; k++) xd[t][k] = nn[t][k] = 0.0f;
-        if (active[t]) {
-            if (kMode == 0) {
-                const TriVerts tv = load_tri(s, tgt[t]);
-                centroid_of(tv, xd[t]);
-                const float4 q2 = __ldg(s.elems + 4 * tgt[t] + 2);
-                nn[t][0] = q2.y; nn[t][1] = q2.z; nn[t][2] = q2.w;
-            } else {
-                for (int k = 0; k < 3; k++) xd[t][k] = pts[(size_t)tgt[t] * 3 + k];
-            }
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = slot < n_targets;
+    // points are taken in Morton order (order: sorted {code, index} keys), so that the 32 targets
+    // of a warp are close together; triangles are already (BVH storage order)
+    const uint32_t tgt = (kMode == 1 && active) ? (uint32_t)__ldg(order + slot) : slot;
+    const uint32_t act = __ballot_sync(0xffffffffu, active);
+    if (!act) return;
+    float xd[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
+    if (active) {
+        if (kMode == 0) {
+            const TriVerts tv = load_tri(s, tgt);
+            centroid_of(tv, xd);
+            const float4 q2 = __ldg(s.elems + 4 * tgt + 2);
+            nn[0] = q2.y; nn[1] = q2.z; nn[2] = q2.w;
+        } else {
+            for (int k = 0; k < 3; k++) xd[k] = pts[(size_t)tgt * 3 + k];
         }
     }
-    double acc[kTgt][4];
-    for (int t = 0; t < kTgt; t++)
-        for (int c = 0; c < 4; c++) acc[t][c] = 0.0;
+    // the bounding sphere of the warp's targets
+    const float cnt = (float)__popc(act);
+    const float Wx = warp_sum_f(xd[0]) / cnt, Wy = warp_sum_f(xd[1]) / cnt, Wz = warp_sum_f(xd[2]) / cnt;
+    const float ox = xd[0] - Wx, oy = xd[1] - Wy, oz = xd[2] - Wz;
+    const float om = sqrtf(warp_max_f(active ? ox * ox + oy * oy + oz * oz : 0.0f));
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const uint32_t n_src = s.n_elems;
-    for (uint32_t t0 = 0; t0 < n_src; t0 += kCvBlock) {
-        __syncthreads();
-        const uint32_t li = t0 + threadIdx.x;
-        if (li < n_src) {
-            s_src[threadIdx.x] = __ldg(src + li);
-            s_n2[threadIdx.x] = __ldg(near2 + li);
-        }
-        __syncthreads();
-        const uint32_t cnt = min((uint32_t)kCvBlock, n_src - t0);
-        float a[kTgt][4];
-#pragma unroll
-        for (int t = 0; t < kTgt; t++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) a[t][c] = 0.0f;
-        for (uint32_t k = 0; k < cnt; k++) {
-            const float4 q = s_src[k];
-            const float n2 = s_n2[k];
-            bool near[kTgt];
-            bool any_near = false;
-#pragma unroll
-            for (int t = 0; t < kTgt; t++) {
-                const float dx = xd[t][0] - q.x, dy = xd[t][1] - q.y, dz = xd[t][2] - q.z;
+    const uint32_t n_cl = (n_src + kClusterSize - 1) / kClusterSize;
+    for (uint32_t k = 0; k < n_cl; k++) {
+        const float4 q0 = __ldg(cl + 4 * k);
+        const float Dx = Wx - q0.x, Dy = Wy - q0.y, Dz = Wz - q0.z;
+        const float thr = q0.w + om;
+        if (Dx * Dx + Dy * Dy + Dz * Dz > thr * thr) {
+            // far from every target of the warp: the cluster's expansion
+            const float4 q1 = __ldg(cl + 4 * k + 1), q2 = __ldg(cl + 4 * k + 2), q3 = __ldg(cl + 4 * k + 3);
+            float phi, g[3];
+            cluster_field(xd, q0, q1, q2, q3, phi, g);
+            if (kMode == 0) {
+                a[0] -= g[0] * nn[0] + g[1] * nn[1] + g[2] * nn[2];
+            } else {
+                a[0] += phi;
+                a[1] += g[0];
+                a[2] += g[1];
+                a[3] += g[2];
+            }
+        } else {
+            const uint32_t i0 = k * kClusterSize, i1 = min(n_src, i0 + kClusterSize);
+            for (uint32_t i = i0; i < i1; i++) {
+                const float4 q = __ldg(src + i);
+                const float n2 = __ldg(near2 + i);
+                const float dx = xd[0] - q.x, dy = xd[1] - q.y, dz = xd[2] - q.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                near[t] = r2 < n2;
-                any_near |= near[t] && active[t];
-                if (!near[t]) {
+                const bool near = r2 < n2;
+                if (!near) {
                     const float rinv = rsqrtf(r2);
                     const float r3 = rinv * rinv * rinv;
                     if (kMode == 0) {
-                        a[t][0] += q.w * (dx * nn[t][0] + dy * nn[t][1] + dz * nn[t][2]) * r3;
+                        a[0] += q.w * (dx * nn[0] + dy * nn[1] + dz * nn[2]) * r3;
                     } else {
-                        a[t][0] += q.w * rinv;
+                        a[0] += q.w * rinv;
                         const float wr3 = q.w * r3;
-                        a[t][1] -= wr3 * dx;
-                        a[t][2] -= wr3 * dy;
-                        a[t][3] -= wr3 * dz;
+                        a[1] -= wr3 * dx;
+                        a[2] -= wr3 * dy;
+                        a[3] -= wr3 * dz;
                     }
                 }
-            }
-            if (__any_sync(0xffffffffu, any_near)) {
-                const uint32_t i = t0 + k;
-#pragma unroll
-                for (int t = 0; t < kTgt; t++) {
-                    if (near[t] && active[t] && !(kMode == 0 && i == tgt[t])) {
+                if (__any_sync(0xffffffffu, near && active)) {
+                    if (near && active && !(kMode == 0 && i == tgt)) {
                         const TriVerts tri = load_tri(s, i);
                         float P, G[3];
-                        triangle_potential(xd[t], tri, P, G);
+                        triangle_potential(xd, tri, P, G);
                         const float sg = __ldg(sigma + i);
                         if (kMode == 0) {
-                            a[t][0] -= sg * (G[0] * nn[t][0] + G[1] * nn[t][1] + G[2] * nn[t][2]);
+                            a[0] -= sg * (G[0] * nn[0] + G[1] * nn[1] + G[2] * nn[2]);
                         } else {
-                            a[t][0] += sg * P;
-                            a[t][1] += sg * G[0];
-                            a[t][2] += sg * G[1];
-                            a[t][3] += sg * G[2];
+                            a[0] += sg * P;
+                            a[1] += sg * G[0];
+                            a[2] += sg * G[1];
+                            a[3] += sg * G[2];
                         }
                     }
                 }
             }
         }
+        if ((k & 31u) == 31u) {
 #pragma unroll
-        for (int t = 0; t < kTgt; t++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) acc[t][c] += a[t][c];
-    }
-    for (int t = 0; t < kTgt; t++) {
-        if (!active[t]) continue;
-        if (kMode == 0) {
-            const double c = (double)c_coef;
-            const double Tsig = c * kInv4Pi * acc[t][0];
-            out[tgt[t]] = (float)((Tsig - (double)__ldg(sigma + tgt[t])) / c);
-        } else {
-            for (int k = 0; k < 4; k++) out[(size_t)tgt[t] * 4 + k] = (float)(kInv4Pi * acc[t][k]);
+            for (int c = 0; c < 4; c++) {
+                acc[c] += a[c];
+                a[c] = 0.0f;
+            }
         }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[c] += a[c];
+    if (!active) return;
+    if (kMode == 0) {
+        const double c = (double)c_coef;
+        const double Tsig = c * kInv4Pi * acc[0];
+        out[tgt] = (float)((Tsig - (double)__ldg(sigma + tgt)) / c);
+    } else {
+        for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * acc[k]);
     }
 }
 
@@ -269,21 +400,6 @@ __global__ void element_frames_kernel(SceneView<D> s, float *__restrict__ out) {
     }
 }
 
-template <int kMode>
-void launch_sum(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma, const float *pts,
-                uint32_t n, float c_coef, float *out, cudaStream_t stream) {
-    int sms = 152;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t two = (n + 2 * kCvBlock - 1) / (2 * kCvBlock);
-    if (two >= 2u * (uint32_t)sms) {
-        cv_sum_kernel<kMode, 2><<<two, kCvBlock, 0, stream>>>(s, src, near2, sigma, pts, n, c_coef, out);
-    } else {
-        cv_sum_kernel<kMode, 1><<<(n + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, pts, n,
-                                                                                       c_coef, out);
-    }
-}
-
 }  // namespace
 
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream) {
@@ -293,22 +409,43 @@ template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float 
 template cudaError_t launch_element_frames<2>(const SceneView<2> &, float *, cudaStream_t);
 template cudaError_t launch_element_frames<3>(const SceneView<3> &, float *, cudaStream_t);
 
-cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float4 *src, float *near2,
-                              cudaStream_t stream) {
+cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float theta, float4 *src,
+                              float *near2, float4 *clusters, cudaStream_t stream) {
     cv_sources_kernel<<<(s.n_elems + 255) / 256, 256, 0, stream>>>(s, sigma, near_factor, src, near2);
+    const uint32_t n_cl = (s.n_elems + kClusterSize - 1) / kClusterSize;
+    cv_cluster_kernel<<<(n_cl * 32 + 255) / 256, 256, 0, stream>>>(s.n_elems, src, near2, theta, clusters);
     return cudaGetLastError();
 }
 
-cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
-                               float c_coef, float *delta, cudaStream_t stream) {
-    launch_sum<0>(s, src, near2, sigma, nullptr, s.n_elems, c_coef, delta, stream);
+cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
+                               const float *sigma, float c_coef, float *delta, cudaStream_t stream) {
+    cv_sum_kernel<0><<<(s.n_elems + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters,
+                                                                                     nullptr, nullptr, s.n_elems, c_coef,
+                                                                                     delta);
     return cudaGetLastError();
 }
 
-cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
-                                const float *pts, uint32_t n_points, float *out, cudaStream_t stream) {
+uint32_t cv_point_order_words(uint32_t n_points) {
+    uint32_t n2 = 1;
+    while (n2 < n_points) n2 <<= 1;
+    return 2 * n2 + 8;  // n2 keys of 8 bytes, then the 6 bound words
+}
+
+cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
+                                const float *sigma, const float *pts, uint32_t n_points, uint32_t *scratch,
+                                float *out, cudaStream_t stream) {
     if (n_points == 0) return cudaSuccess;
-    launch_sum<1>(s, src, near2, sigma, pts, n_points, 0.0f, out, stream);
+    uint32_t n2 = 1;
+    while (n2 < n_points) n2 <<= 1;
+    uint64_t *key = (uint64_t *)scratch;
+    uint32_t *bb = scratch + 2 * (size_t)n2;
+    bounds_init_kernel<<<1, 32, 0, stream>>>(bb);
+    pts_bounds_kernel<<<(n_points + 255) / 256, 256, 0, stream>>>(pts, n_points, bb);
+    pts_morton_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(pts, n_points, n2, bb, key);
+    for (uint32_t k = 2; k <= n2; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(n2, j, k, key);
+    cv_sum_kernel<1><<<(n_points + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, pts,
+                                                                                    key, n_points, 0.0f, out);
     return cudaGetLastError();
 }
 

@@ -53,16 +53,20 @@ cudaError_t launch_domain_cv_2d(const SceneView<2> &s, const WalkParams &p, cons
 cudaError_t launch_domain_cv_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                 double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                 cudaStream_t stream);
-// Learned control-variate tables (k_cv_tables.cu): per-triangle sources {centroid, sigma~ area}
-// and squared near radii; the residual Neumann data delta_j of each stored triangle; the
-// single-layer potential of sigma~ and its gradient at points ([n][4]); the (centroid, normal)
+// Learned control-variate tables (k_cv_tables.cu): per-triangle sources {centroid, sigma~ area},
+// squared near radii and the clusters of 32 stored triangles (4 float4 each: centre and far radius
+// for theta, moments to the quadrupole); the residual Neumann data delta_j of each stored triangle;
+// the single-layer potential of sigma~ and its gradient at points ([n][4]); the (centroid, normal)
 // network input of every stored element ([n][6]).
-cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float4 *src, float *near2,
-                              cudaStream_t stream);
-cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
-                               float c_coef, float *delta, cudaStream_t stream);
-cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float *sigma,
-                                const float *pts, uint32_t n_points, float *out, cudaStream_t stream);
+cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float theta, float4 *src,
+                              float *near2, float4 *clusters, cudaStream_t stream);
+cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
+                               const float *sigma, float c_coef, float *delta, cudaStream_t stream);
+// scratch: cv_point_order_words(n_points) 32-bit words (the points' Morton order and bounds).
+uint32_t cv_point_order_words(uint32_t n_points);
+cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
+                                const float *sigma, const float *pts, uint32_t n_points, uint32_t *scratch,
+                                float *out, cudaStream_t stream);
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream);
 // Random-gather ceiling of the uniform-sampling walk (k_probe.cu): samples per second of guide +
 // 64-byte record gathers over tables of the given sizes, on the current device.

@@ -260,12 +260,14 @@ def centroid_inputs(scene, device=None):
     return out
 
 
-def residual_control_variate(scene, mlp: MLP, domain: int, near_factor: float = 3.0, stream=None):
+def residual_control_variate(scene, mlp: MLP, domain: int, near_factor: float = 3.0, theta: float = 0.3,
+                             stream=None):
     """The residual control variate of a single-layer Neumann problem (wob_cv_residual_data):
     sigma~ = the network at every stored triangle's centroid, constant on the triangle; returns
     (residual scene, sigma~) where the residual scene is a copy of `scene` whose Neumann data
     carries the offsets delta = (T sigma~ - sigma~) / c. The forward estimator on the residual
-    scene plus control_variate_potential(sigma~) estimates u."""
+    scene plus control_variate_potential(sigma~) estimates u. theta: cluster acceptance of the
+    far field (0: every triangle)."""
     import torch
     from . import _ptr, _stream_ptr
     x = centroid_inputs(scene)
@@ -274,18 +276,19 @@ def residual_control_variate(scene, mlp: MLP, domain: int, near_factor: float = 
     mlp.forward(x, n, sigma, stream)
     sigma = sigma[:, 0].contiguous()
     delta = torch.zeros(n, dtype=torch.float32, device=x.device)
-    check(load().wob_cv_residual_data(scene.handle, _ptr(sigma), int(domain), float(near_factor), _ptr(delta),
-                                      _stream_ptr(stream)))
+    check(load().wob_cv_residual_data(scene.handle, _ptr(sigma), int(domain), float(near_factor), float(theta),
+                                      _ptr(delta), _stream_ptr(stream)))
     return scene.clone_with_offsets(delta, stream), sigma
 
 
-def control_variate_potential(scene, sigma, points, n_points: int, near_factor: float = 3.0, stream=None):
+def control_variate_potential(scene, sigma, points, n_points: int, near_factor: float = 3.0, theta: float = 0.3,
+                              stream=None):
     """S sigma~ and its gradient at points (wob_cv_potential): device tensor [n_points, 4]."""
     import torch
     from . import _ptr, _stream_ptr
     out = torch.zeros(n_points, 4, dtype=torch.float32, device=sigma.device)
-    check(load().wob_cv_potential(scene.handle, _ptr(sigma), float(near_factor), _ptr(points), int(n_points),
-                                  _ptr(out), _stream_ptr(stream)))
+    check(load().wob_cv_potential(scene.handle, _ptr(sigma), float(near_factor), float(theta), _ptr(points),
+                                  int(n_points), _ptr(out), _stream_ptr(stream)))
     return out
 
 
