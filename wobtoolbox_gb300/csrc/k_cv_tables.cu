@@ -25,15 +25,16 @@
 // consecutive ones (BVH storage order keeps them spatially compact), each with its centre z (mean
 // centroid), radius rho, largest near radius eta and the moments of its centroid sources about z
 // up to the quadrupole (M0 = sum w, M1 = sum w d, M2 = sum w d d^T, w = sigma~ A, d = c - z).
-// A warp takes 32 consecutive targets and the bounding sphere (W, omega) of their positions; a
-// cluster with |W - z| > max(rho / theta, rho + eta) + omega is far from every target of the warp
+// A block takes 32 consecutive targets and the bounding sphere (W, omega) of their positions; a
+// cluster with |W - z| > max(rho / theta, rho + eta) + omega is far from every target of the block
 // and enters through its quadrupole expansion of sum w / |x - c| (one evaluation instead of 32,
 // error of order (rho / |x - z|)^3 of the cluster's share); any other cluster is taken triangle by
 // triangle as above. theta = 0 takes every triangle (the dense sum). The decision is uniform
-// across the warp, so lanes never diverge between the two.
+// across the block, so lanes never diverge between the two.
 //
-// Work decomposition: one warp per 32 targets, 8 warps a block, every warp walks the cluster table
-// in order (records read as broadcasts). FP32 partial sums over 32 clusters, FP64 across them.
+// Work decomposition: one block per 32 targets (a lane each), its 8 warps splitting the cluster
+// table (records read as broadcasts), FP32 partial sums over 32 clusters, FP64 across them and
+// across the warps (in warp order: deterministic).
 // This unit is compiled with FMA contraction (it is not part of the bit-exact walk).
 #include "device_common.cuh"
 #include "launch.hpp"
@@ -43,6 +44,7 @@ namespace wobgb {
 namespace {
 
 constexpr int kCvBlock = 256;
+constexpr int kCvWarps = kCvBlock / 32;
 constexpr double kInv4Pi = 0.07957747154594767;
 
 struct TriVerts {
@@ -268,7 +270,9 @@ __device__ __forceinline__ void cluster_field(const float x[3], const float4 &q0
 }
 
 // kMode 0: residual data at the stored triangles' centroids; kMode 1: potential and gradient at
-// points (out: [n][4] = u, du/dx, du/dy, du/dz).
+// points (out: [n][4] = u, du/dx, du/dy, du/dz). A block takes 32 consecutive targets (one per
+// lane); its kCvWarps warps split the cluster table (warp w takes clusters w, w + kCvWarps, ...)
+// and their sums are added in warp order through shared memory at the end.
 template <int kMode>
 __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const float4 *__restrict__ src,
                                                           const float *__restrict__ near2,
@@ -276,13 +280,14 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
                                                           const float4 *__restrict__ cl, const float *__restrict__ pts,
                                                           const uint64_t *__restrict__ order, uint32_t n_targets,
                                                           float c_coef, float *__restrict__ out) {
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_acc[kCvWarps][4][32];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t slot = blockIdx.x * 32u + lane;
     const bool active = slot < n_targets;
     // points are taken in Morton order (order: sorted {code, index} keys), so that the 32 targets
-    // of a warp are close together; triangles are already (BVH storage order)
+    // of a block are close together; triangles are already (BVH storage order)
     const uint32_t tgt = (kMode == 1 && active) ? (uint32_t)__ldg(order + slot) : slot;
     const uint32_t act = __ballot_sync(0xffffffffu, active);
-    if (!act) return;
     float xd[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
     if (active) {
         if (kMode == 0) {
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
             for (int k = 0; k < 3; k++) xd[k] = pts[(size_t)tgt * 3 + k];
         }
     }
-    // the bounding sphere of the warp's targets
+    // the bounding sphere of the block's targets
     const float cnt = (float)__popc(act);
     const float Wx = warp_sum_f(xd[0]) / cnt, Wy = warp_sum_f(xd[1]) / cnt, Wz = warp_sum_f(xd[2]) / cnt;
     const float ox = xd[0] - Wx, oy = xd[1] - Wy, oz = xd[2] - Wz;
@@ -303,12 +308,13 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
     float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const uint32_t n_src = s.n_elems;
     const uint32_t n_cl = (n_src + kClusterSize - 1) / kClusterSize;
-    for (uint32_t k = 0; k < n_cl; k++) {
+    uint32_t taken = 0;
+    for (uint32_t k = wid; k < n_cl; k += kCvWarps) {
         const float4 q0 = __ldg(cl + 4 * k);
         const float Dx = Wx - q0.x, Dy = Wy - q0.y, Dz = Wz - q0.z;
         const float thr = q0.w + om;
         if (Dx * Dx + Dy * Dy + Dz * Dz > thr * thr) {
-            // far from every target of the warp: the cluster's expansion
+            // far from every target of the block: the cluster's expansion
             const float4 q1 = __ldg(cl + 4 * k + 1), q2 = __ldg(cl + 4 * k + 2), q3 = __ldg(cl + 4 * k + 3);
             float phi, g[3];
             cluster_field(xd, q0, q1, q2, q3, phi, g);
@@ -359,7 +365,7 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
                 }
             }
         }
-        if ((k & 31u) == 31u) {
+        if ((++taken & 31u) == 0u) {
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 acc[c] += a[c];
@@ -368,14 +374,19 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
         }
     }
 #pragma unroll
-    for (int c = 0; c < 4; c++) acc[c] += a[c];
-    if (!active) return;
+    for (int c = 0; c < 4; c++) s_acc[wid][c][lane] = acc[c] + a[c];
+    __syncthreads();
+    if (wid != 0 || !active) return;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < kCvWarps; w++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) t[c] += s_acc[w][c][lane];
     if (kMode == 0) {
         const double c = (double)c_coef;
-        const double Tsig = c * kInv4Pi * acc[0];
+        const double Tsig = c * kInv4Pi * t[0];
         out[tgt] = (float)((Tsig - (double)__ldg(sigma + tgt)) / c);
     } else {
-        for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * acc[k]);
+        for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * t[k]);
     }
 }
 
@@ -419,9 +430,8 @@ cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float n
 
 cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
                                const float *sigma, float c_coef, float *delta, cudaStream_t stream) {
-    cv_sum_kernel<0><<<(s.n_elems + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters,
-                                                                                     nullptr, nullptr, s.n_elems, c_coef,
-                                                                                     delta);
+    cv_sum_kernel<0><<<(s.n_elems + 31) / 32, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, nullptr, nullptr,
+                                                                     s.n_elems, c_coef, delta);
     return cudaGetLastError();
 }
 
@@ -444,8 +454,8 @@ cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const 
     pts_morton_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(pts, n_points, n2, bb, key);
     for (uint32_t k = 2; k <= n2; k <<= 1)
         for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(n2, j, k, key);
-    cv_sum_kernel<1><<<(n_points + kCvBlock - 1) / kCvBlock, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, pts,
-                                                                                    key, n_points, 0.0f, out);
+    cv_sum_kernel<1><<<(n_points + 31) / 32, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, pts, key,
+                                                                    n_points, 0.0f, out);
     return cudaGetLastError();
 }
 

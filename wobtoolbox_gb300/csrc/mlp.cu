@@ -289,6 +289,8 @@ struct wob_mlp_s {
     uint32_t train_cap = 0, partial_blocks = 0;
     float *xb = nullptr, *tb = nullptr, *sched = nullptr, *partial = nullptr, *partial_loss = nullptr;
     uint32_t *step = nullptr;
+    uint32_t *image = nullptr;  // packed BF16 weights of the fused step (zero padding)
+    uint32_t *err = nullptr;    // fused step's error word
     std::mutex mu;
 
     uint32_t n_layers() const { return hidden + 1; }
@@ -297,8 +299,10 @@ struct wob_mlp_s {
             if (*p) cudaFree(*p);
             *p = nullptr;
         }
-        if (step) cudaFree(step);
-        step = nullptr;
+        for (uint32_t **p : {&step, &image, &err}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
         cap = 0;
         train_cap = 0;
         partial_blocks = 0;
@@ -325,6 +329,14 @@ struct wob_mlp_s {
     cudaError_t ensure_fused(uint32_t batch) {
         cudaError_t e;
         if (!step && (e = cudaMalloc(&step, 4)) != cudaSuccess) return e;
+        if (!image) {
+            const size_t bytes = wobgb::fused_train_image_words() * 4;
+            if ((e = cudaMalloc(&image, bytes)) != cudaSuccess || (e = cudaMemset(image, 0, bytes)) != cudaSuccess)
+                return e;
+        }
+        if (!err) {
+            if ((e = cudaMalloc(&err, 4)) != cudaSuccess || (e = cudaMemset(err, 0, 4)) != cudaSuccess) return e;
+        }
         const uint32_t blocks = wobgb::fused_train_blocks(batch);
         if (blocks <= partial_blocks) return cudaSuccess;
         for (float **p : {&partial, &partial_loss}) {
@@ -557,7 +569,7 @@ int wob_mlp_gradient_fused(wob_mlp m, const float *inputs, const float *targets,
     if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
     if ((e = cudaMemsetAsync(m->step, 0, 4, st)) != cudaSuccess) return mfail_cuda(e, "MLP step counter");
     wobgb::FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, n, m->n_params, 0u, 0ull, m->step,
-                            m->partial, m->partial_loss};
+                            m->partial, m->partial_loss, m->image, m->err};
     e = wobgb::launch_fused_gradient(a, grad, loss, st);
     return e == cudaSuccess ? WOB_OK : mfail_cuda(e, "fused MLP gradient");
 }
@@ -594,6 +606,11 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
         return mfail_cuda(e, "preparing the training stream");
     }
     const uint32_t adam_base = (uint32_t)m->adam_steps;
+    // the fused step reads the weights from their packed image, which each update keeps current
+    if (fused && (e = launch_pack_weights(m->params, m->n_params, m->out_dim, m->image, cs)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e, "packing the weights");
+    }
     if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
         cleanup();
         return mfail_cuda(e, "capturing the training step");
@@ -601,7 +618,7 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
     cudaError_t e_body = cudaSuccess;
     if (fused) {
         FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, batch, m->n_params, 1u, seed, m->step,
-                         m->partial, m->partial_loss};
+                         m->partial, m->partial_loss, m->image, m->err};
         e_body = launch_fused_train_step(a, m->params, m->adam_m, m->adam_v, steps, lr, adam_base, loss_history, cs);
     } else {
         train_schedule_kernel<<<1, 1, 0, cs>>>(m->step, steps, lr, adam_base, m->sched);
@@ -629,6 +646,15 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
     }
     m->adam_steps += steps;
     cleanup();
+    if (fused) {
+        uint32_t bits = 0;
+        if ((e = cudaMemcpy(&bits, m->err, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return mfail_cuda(e, "reading the training error word");
+        if (bits) {
+            cudaMemset(m->err, 0, 4);
+            return mfail(WOB_ERR_DEVICE_LIMIT, "a training block's weight staging did not complete within its wait bound");
+        }
+    }
     return WOB_OK;
 }
 

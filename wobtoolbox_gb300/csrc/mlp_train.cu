@@ -1,8 +1,12 @@
 // Fused training step of the Fourier-feature MLP (mlp.cu's network with 4 hidden layers): one
 // kernel runs the batch gather, the forward pass and the backward pass of 64 rows per block with
 // every weight and activation in shared memory and writes the block's gradient; a second kernel
-// sums the blocks' gradients in a fixed order (so a step is deterministic) and applies Adam; a
-// third advances the step counter. wob_mlp_train replays the three as a CUDA graph.
+// sums the blocks' gradients in a fixed order (so a step is deterministic), applies Adam and
+// writes the updated weights as a packed BF16 image in both operand layouts; a third advances the
+// step counter. wob_mlp_train replays the three as a CUDA graph. Each block of the next step
+// stages that image (83 KB) into shared memory with one TMA bulk copy (cp.async.bulk, completion
+// on an mbarrier, the wait bounded), instead of every block reading and converting the FP32
+// parameters itself.
 //
 // Network and parameter layout as in mlp.cu: phi = [sin, cos](2 pi B v) (32 frequencies of the
 // 6 inputs), 4 hidden layers 64 -> 64 with SiLU, a linear 64 -> out_dim head; FP32 parameters,
@@ -119,8 +123,32 @@ __device__ __forceinline__ void store_col_sums(float acc[8][4], float *dst, int 
     }
 }
 
+constexpr size_t kImageWords = (size_t)(kLayers + kHidden) * kMat;  // Wf then Wb, as in shared memory
+constexpr uint32_t kImageBytes = (uint32_t)(kImageWords * 4);
+static_assert(kImageBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+// try_wait polls before a block gives up on its staging copy (each poll may suspend the thread
+// for a while; the copy normally lands within microseconds).
+constexpr uint32_t kStageWaitPolls = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kStageWaitPolls; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrainArgs g) {
-    extern __shared__ uint32_t smem[];
+    extern __shared__ __align__(128) uint32_t smem[];
+    __shared__ __align__(8) uint64_t stage_bar;
     uint32_t *Wf = smem;                      // layer l: [out][in]
     uint32_t *Wb = Wf + kLayers * kMat;       // layer l >= 1: [in][out] at index l - 1
     uint32_t *act = Wb + kHidden * kMat;      // [row][in] of the layer being evaluated
@@ -139,20 +167,21 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     const int out_dim = (int)g.out_dim;
     const uint32_t step = *g.step;
 
-    // weights in both layouts (rows of the head beyond out_dim are zero), biases, bias gradients
+    // weights in both layouts: one bulk copy of the packed image (rows of the head beyond out_dim
+    // and the row padding are zero there); biases by plain loads meanwhile
+    const uint32_t bar = smem_u32(&stage_bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kImageBytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(Wf)), "l"(g.image), "r"(kImageBytes), "r"(bar)
+                     : "memory");
+    }
     for (int l = 0; l < kLayers; l++) {
         const int fo = l == kHidden ? out_dim : kW;
         const float *Wl = g.params + (size_t)l * kLayerParams;
-        for (int idx = tid; idx < kW * 32; idx += kThreads) {
-            const int o = idx >> 5, p = idx & 31;
-            const float w0 = o < fo ? Wl[o * kW + 2 * p] : 0.0f, w1 = o < fo ? Wl[o * kW + 2 * p + 1] : 0.0f;
-            Wf[l * kMat + o * kLd + p] = pack2(w0, w1);
-            if (l >= 1) {  // [in = o][out pair p]
-                const float v0 = 2 * p < fo ? Wl[(2 * p) * kW + o] : 0.0f;
-                const float v1 = 2 * p + 1 < fo ? Wl[(2 * p + 1) * kW + o] : 0.0f;
-                Wb[(l - 1) * kMat + o * kLd + p] = pack2(v0, v1);
-            }
-        }
         for (int o = tid; o < kW; o += kThreads) bias[l * kW + o] = o < fo ? Wl[fo * kW + o] : 0.0f;
     }
     // the block's batch rows: Philox4x32-10 on (row, step, 0, "tran") keyed by the seed
@@ -169,7 +198,14 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
         for (int k = 0; k < out_dim; k++) tgt[r * kW + k] = ok ? g.targets[(size_t)idx * out_dim + k] : 0.0f;
     }
     if (tid < 4) red[tid] = 0.0f;
-    __syncthreads();
+    __syncthreads();  // the barrier's initialisation is visible to every thread from here
+    if (!mbar_wait_bounded(bar, 0u)) {
+        // the staging copy did not land: flag it, give it one more bounded wait so that it does not
+        // write into a later block's shared memory, and leave this block's gradient unwritten
+        if (tid == 0) atomicOr(g.err, 1u);
+        mbar_wait_bounded(bar, 0u);
+        return;
+    }
     // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t
     for (int idx = tid; idx < kTM * 32; idx += kThreads) {
         const int r = idx >> 5, f = idx & 31;
@@ -291,17 +327,64 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     if (tid == 0) g.partial_loss[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
 }
 
-// Sums the blocks' gradients (in block order) and applies Adam with the cosine schedule of the
-// current step; block 0 records the step's loss.
-__global__ void mlp_reduce_adam_kernel(float *__restrict__ p, float *__restrict__ m, float *__restrict__ v,
-                                       const float *__restrict__ partial, const float *__restrict__ partial_loss,
-                                       uint32_t n_blocks, uint32_t n_params, const uint32_t *__restrict__ step,
-                                       uint32_t steps, float lr0, uint32_t adam_base, float *__restrict__ loss_hist) {
-    const uint32_t s = *step;
+// Parameter i's place in the packed image: its BF16 halves in the forward operand W [out][in]
+// and, for layers >= 1, in the backward operand W^T [in][out]; biases have none (returns false).
+__device__ __forceinline__ bool image_slots(uint32_t i, uint32_t out_dim, uint32_t &f, uint32_t &b) {
+    uint32_t l = i / kLayerParams;
+    if (l > (uint32_t)kHidden) l = kHidden;
+    const uint32_t r = i - l * kLayerParams;
+    const uint32_t fo = l == (uint32_t)kHidden ? out_dim : (uint32_t)kW;
+    if (r >= fo * kW) return false;
+    const uint32_t o = r / kW, in = r % kW;
+    f = (l * kMat + o * kLd) * 2u + in;
+    b = l >= 1 ? (((uint32_t)kLayers + l - 1u) * kMat + in * kLd) * 2u + o : 0xFFFFFFFFu;
+    return true;
+}
+__device__ __forceinline__ void image_store(uint32_t *image, uint32_t i, uint32_t out_dim, float v) {
+    uint32_t f, b;
+    if (!image_slots(i, out_dim, f, b)) return;
+    __nv_bfloat16 *h = reinterpret_cast<__nv_bfloat16 *>(image);
+    const __nv_bfloat16 x = __float2bfloat16_rn(v);
+    h[f] = x;
+    if (b != 0xFFFFFFFFu) h[b] = x;
+}
+
+__global__ void pack_weights_kernel(const float *__restrict__ p, uint32_t n_params, uint32_t out_dim,
+                                    uint32_t *__restrict__ image) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_params) {
-        float gsum = 0.0f;
-        for (uint32_t b = 0; b < n_blocks; b++) gsum += partial[(size_t)b * n_params + i];
+    if (i < n_params) image_store(image, i, out_dim, p[i]);
+}
+
+// Block-ordered gradient sums: a block of 256 threads takes 32 parameters, 8 threads each summing
+// every 8th block gradient in order, the 8 partial sums added in order (a fixed order: the step is
+// deterministic).
+constexpr int kRedSplit = 8;
+__device__ __forceinline__ float ordered_gradient(const float *__restrict__ partial, uint32_t n_blocks,
+                                                  uint32_t n_params, uint32_t i, float (*red)[33]) {
+    const uint32_t q = threadIdx.x & 31u, sl = threadIdx.x >> 5;
+    float s = 0.0f;
+    if (i < n_params)
+        for (uint32_t b = sl; b < n_blocks; b += kRedSplit) s += partial[(size_t)b * n_params + i];
+    red[sl][q] = s;
+    __syncthreads();
+    float t = 0.0f;
+    if (sl == 0)
+        for (int k = 0; k < kRedSplit; k++) t += red[k][q];
+    return t;
+}
+
+// Sums the blocks' gradients and applies Adam with the cosine schedule of the current step, then
+// stores the new weights into the packed image; block 0 records the step's loss.
+__global__ void __launch_bounds__(256) mlp_reduce_adam_kernel(
+    float *__restrict__ p, float *__restrict__ m, float *__restrict__ v, const float *__restrict__ partial,
+    const float *__restrict__ partial_loss, uint32_t n_blocks, uint32_t n_params, uint32_t out_dim,
+    uint32_t *__restrict__ image, const uint32_t *__restrict__ step, uint32_t steps, float lr0, uint32_t adam_base,
+    float *__restrict__ loss_hist) {
+    __shared__ float red[kRedSplit][33];
+    const uint32_t s = *step;
+    const uint32_t i = blockIdx.x * 32u + (threadIdx.x & 31u);
+    const float gsum = ordered_gradient(partial, n_blocks, n_params, i, red);
+    if (threadIdx.x < 32 && i < n_params) {
         const float lr = lr0 * 0.5f * (1.0f + cospif((float)s / (float)steps));
         const float t = (float)(adam_base + s + 1u);
         const float bc1 = 1.0f - powf(0.9f, t), bc2 = 1.0f - powf(0.999f, t);
@@ -309,7 +392,9 @@ __global__ void mlp_reduce_adam_kernel(float *__restrict__ p, float *__restrict_
         const float vi = 0.999f * v[i] + 0.001f * gsum * gsum;
         m[i] = mi;
         v[i] = vi;
-        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+        const float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+        p[i] = pi;
+        image_store(image, i, out_dim, pi);
     }
     if (loss_hist && blockIdx.x == 0 && threadIdx.x == 0) {
         float l = 0.0f;
@@ -320,15 +405,14 @@ __global__ void mlp_reduce_adam_kernel(float *__restrict__ p, float *__restrict_
 
 __global__ void mlp_step_advance_kernel(uint32_t *step) { *step += 1u; }
 
-__global__ void mlp_reduce_grad_kernel(const float *__restrict__ partial, const float *__restrict__ partial_loss,
-                                       uint32_t n_blocks, uint32_t n_params, float *__restrict__ grad,
-                                       float *__restrict__ loss) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_params) {
-        float gsum = 0.0f;
-        for (uint32_t b = 0; b < n_blocks; b++) gsum += partial[(size_t)b * n_params + i];
-        grad[i] = gsum;
-    }
+__global__ void __launch_bounds__(256) mlp_reduce_grad_kernel(const float *__restrict__ partial,
+                                                              const float *__restrict__ partial_loss, uint32_t n_blocks,
+                                                              uint32_t n_params, float *__restrict__ grad,
+                                                              float *__restrict__ loss) {
+    __shared__ float red[kRedSplit][33];
+    const uint32_t i = blockIdx.x * 32u + (threadIdx.x & 31u);
+    const float gsum = ordered_gradient(partial, n_blocks, n_params, i, red);
+    if (threadIdx.x < 32 && i < n_params) grad[i] = gsum;
     if (loss && blockIdx.x == 0 && threadIdx.x == 0) {
         float l = 0.0f;
         for (uint32_t b = 0; b < n_blocks; b++) l += partial_loss[b];
@@ -339,25 +423,34 @@ __global__ void mlp_reduce_grad_kernel(const float *__restrict__ partial, const 
 }  // namespace
 
 size_t fused_train_smem_bytes() { return kSmemWords * 4 + kSmemFloats * 4; }
+size_t fused_train_image_words() { return kImageWords; }
 uint32_t fused_train_blocks(uint32_t batch) { return (batch + kTM - 1) / kTM; }
+
+cudaError_t launch_pack_weights(const float *params, uint32_t n_params, uint32_t out_dim, uint32_t *image,
+                                cudaStream_t stream) {
+    pack_weights_kernel<<<(n_params + 255) / 256, 256, 0, stream>>>(params, n_params, out_dim, image);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, float *adam_m, float *adam_v,
                                     uint32_t steps, float lr, uint32_t adam_base, float *loss_hist,
                                     cudaStream_t stream) {
     const uint32_t blocks = fused_train_blocks(a.batch);
     mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
-    mlp_reduce_adam_kernel<<<(a.n_params + 255) / 256, 256, 0, stream>>>(params, adam_m, adam_v, a.partial,
-                                                                         a.partial_loss, blocks, a.n_params, a.step,
-                                                                         steps, lr, adam_base, loss_hist);
+    mlp_reduce_adam_kernel<<<(a.n_params + 31) / 32, 256, 0, stream>>>(
+        params, adam_m, adam_v, a.partial, a.partial_loss, blocks, a.n_params, a.out_dim, const_cast<uint32_t *>(a.image),
+        a.step, steps, lr, adam_base, loss_hist);
     mlp_step_advance_kernel<<<1, 1, 0, stream>>>(a.step);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fused_gradient(const FusedTrainArgs &a, float *grad, float *loss, cudaStream_t stream) {
     const uint32_t blocks = fused_train_blocks(a.batch);
+    cudaError_t e = launch_pack_weights(a.params, a.n_params, a.out_dim, const_cast<uint32_t *>(a.image), stream);
+    if (e != cudaSuccess) return e;
     mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
-    mlp_reduce_grad_kernel<<<(a.n_params + 255) / 256, 256, 0, stream>>>(a.partial, a.partial_loss, blocks, a.n_params,
-                                                                         grad, loss);
+    mlp_reduce_grad_kernel<<<(a.n_params + 31) / 32, 256, 0, stream>>>(a.partial, a.partial_loss, blocks, a.n_params,
+                                                                       grad, loss);
     return cudaGetLastError();
 }
 

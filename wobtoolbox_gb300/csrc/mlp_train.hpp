@@ -18,9 +18,17 @@ struct FusedTrainArgs {
     uint32_t *step;        // device step counter (batch draws and the learning-rate schedule)
     float *partial;        // [blocks][n_params]: each block's gradient
     float *partial_loss;   // [blocks]
+    const uint32_t *image; // packed BF16 weights, both operand layouts (fused_train_image_words words)
+    uint32_t *err;         // bit 0: a block's weight staging did not complete within its wait bound
 };
 
 size_t fused_train_smem_bytes();
+size_t fused_train_image_words();
+// The packed weight image of params (launch_fused_train_step keeps it current after each update;
+// call this before the first step and whenever the parameters were changed by other means). The
+// image's padding words must be zero (zero the allocation once).
+cudaError_t launch_pack_weights(const float *params, uint32_t n_params, uint32_t out_dim, uint32_t *image,
+                                cudaStream_t stream);
 uint32_t fused_train_blocks(uint32_t batch);
 cudaError_t prepare_fused_train();
 // One step: fused forward/backward, block-ordered gradient sum + Adam (cosine learning rate from
