@@ -594,25 +594,15 @@ def run_batch(args):
         s.close()
 
 
-def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, plain_budget=20.0, cv_budget=5.0,
-                    train_steps=2000, near_factor=3.0, theta=0.3, seed=SEED):
-    """Time to RMSE `target` against the analytic solution, plain forward WoB vs the learned
-    residual control variate, on the exterior Neumann workload: displaced icosphere (0.15 sum
-    c_lm Y_lm, l <= 4) subdivided `subdiv` times (7: 327,680 triangles), Neumann data of
-    u = sum_{k<3} q_k / (4 pi |x - s_k|) with s_k inside at radius <= 0.5 and q_k ~ U[-1, 1];
-    forward single-layer estimator (data/config_general_3d_exterior_Neumann.json), 4 bounces;
-    evaluation at the 256^2 points of the z = 0 slice over [-2, 2]^2 outside the surface.
-
-    Both estimators run progressive iterations (plain_paths / cv_paths new paths per point each) and
-    the RMSE of the running estimate is taken after each; times are wall-clock on a synchronised
-    device, excluding only the RMSE evaluation. The control variate's clock starts before its
-    training labels: labels (65,536 boundary points x 256-path walk estimates of the density,
-    clamped to the 0.999 quantile of their magnitude), 2000 device Adam steps of the 32-frequency 4 x 64 SiLU network, the network at every
-    triangle's centroid, the residual Neumann data, the residual scene, the control variate's
-    potential at the points, then the residual walks. Returns a dict."""
+def exterior_neumann_case(dev, subdiv=7, seed=SEED):
+    """The exterior Neumann workload (data/config_general_3d_exterior_Neumann.json at the mesh
+    size of the learned-CV configuration): displaced icosphere (0.15 sum c_lm Y_lm, l <= 4)
+    subdivided `subdiv` times (7: 327,680 triangles), Neumann data of u = sum_{k<3} q_k / (4 pi
+    |x - s_k|) with s_k inside at radius <= 0.5 and q_k ~ U[-1, 1]; the points of the 256^2 z = 0
+    slice over [-2, 2]^2 outside the surface (half-line parity on the GPU). Returns (scene, points,
+    exact u at the points, faces)."""
     import torch
     import wobtoolbox_gb300 as wob
-    from wobtoolbox_gb300 import cv
     from wobtoolbox_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     V, F, _ = W.displaced_icosphere(subdiv, 0.15, 4, seed)
@@ -637,6 +627,121 @@ def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, pl
     del hits, hp
     pts = np.ascontiguousarray(cand[outside])
     exact_u = W.point_sources(pts, src, q)[:, 0]
+    return scene, pts, exact_u, F
+
+
+def run_fwd3d(args):
+    """The plain walk of the learned-CV workload alone (exterior_neumann_case: forward single
+    layer, line-intersection sampling, 4 bounces, 327,680 triangles, 54,025 slice points): bounces
+    per second over `--steps` solves of `--fwd-paths` paths per point, L2 flushed between steps,
+    the kernel configuration autotuned (or pinned with --fwd-config), with the lockstep kernel's
+    rate (configuration 0) measured beside it. --small: the first 4096 points, 128 paths (the
+    profiling case)."""
+    import ctypes as C
+    import torch
+    import wobtoolbox_gb300 as wob
+    rank, world, local = dist_init(args)
+    lib = wob.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    scene, pts, _, F = exterior_neumann_case(dev, args.cv_subdiv, SEED)
+    paths = args.fwd_paths
+    if args.small:
+        pts, paths = np.ascontiguousarray(pts[:4096]), 128
+    n = len(pts)
+    d = torch.from_numpy(pts).to(dev)
+    L = 4
+    p = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.ExteriorDomain,
+                            estimator=wob.ForwardEstimator, problem=wob.NeumannProblem, path_length=L, seed=SEED,
+                            num_sample_paths=paths)
+    var = C.c_int32(-1)
+    wob.check(lib.wob_tunable_variant(scene.handle, C.byref(p.to_c()), C.byref(var)))
+    saved = C.c_int32(0)
+    wob.check(lib.wob_get_domain_config(var.value, C.byref(saved)))
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    s_ = torch.zeros(n, 4, dtype=torch.float64, device=dev)
+    b_ = torch.zeros(1, dtype=torch.int64, device=dev)
+
+    def timed(steps, base):
+        ms = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            scene.solve_domain(dataclasses.replace(p, path_offset=(base + k) * paths), d, n, s_, None, b_, stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    try:
+        if args.fwd_config >= 0:
+            wob.check(lib.wob_set_domain_config(var.value, args.fwd_config))
+            tuned = None
+        else:
+            tuned = scene.autotune_domain(p, d, n, stream)
+        cfg = C.c_int32(0)
+        wob.check(lib.wob_get_domain_config(var.value, C.byref(cfg)))
+        timed(args.warmup, 0)
+        b_.zero_()
+        with ClockSampler(local) as clocks:
+            ms = timed(args.steps, 100)
+        bounces = int(b_.item())
+        clk = clocks.summary()
+        lock_ms = None
+        if not args.small and cfg.value != 0:
+            wob.check(lib.wob_set_domain_config(var.value, 0))
+            timed(1, 200)
+            lock_ms = min(timed(max(1, args.steps // 2), 300))
+    finally:
+        lib.wob_set_domain_config(var.value, saved.value)
+    value = bounces / (sum(ms) / 1e3)
+    wave = cfg.value % 4 != 0
+    chunk = [1 << 22, 1 << 21, 1 << 20, 1 << 19][cfg.value // 4]
+    chunks = -(-n // max(1, chunk // paths))
+    out = {
+        "metric": "bounces/s, 3D forward single-layer walk (line-intersection sampling)", "value": value,
+        "unit": "bounces/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(ms) / len(ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"exterior Neumann, forward single layer, {L} bounces, displaced icosphere "
+                               f"{len(F)} triangles, {n} slice points outside the surface, {paths} paths per point "
+                               "per step",
+                   "kernel_config": cfg.value,
+                   "kernel": (f"split-phase wavefront, trace shape {cfg.value % 4}, {chunk} paths per chunk" if wave
+                              else "lockstep walk"),
+                   "autotune": None if tuned is None else {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
+                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)"},
+        "lockstep_ms_per_step": lock_ms,
+        "speedup_vs_lockstep": (lock_ms / (sum(ms) / len(ms))) if lock_ms else None,
+        "clocks": clk,
+        "gpu_launches": args.steps * (chunks * (2 + 2 * (L - 1)) if wave else 1),
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    scene.close()
+
+
+def cv_time_to_rmse(dev, subdiv=7, target=1e-3, plain_paths=256, cv_paths=32, plain_budget=20.0, cv_budget=5.0,
+                    train_steps=2000, near_factor=3.0, theta=0.3, seed=SEED):
+    """Time to RMSE `target` against the analytic solution, plain forward WoB vs the learned
+    residual control variate, on the exterior Neumann workload: displaced icosphere (0.15 sum
+    c_lm Y_lm, l <= 4) subdivided `subdiv` times (7: 327,680 triangles), Neumann data of
+    u = sum_{k<3} q_k / (4 pi |x - s_k|) with s_k inside at radius <= 0.5 and q_k ~ U[-1, 1];
+    forward single-layer estimator (data/config_general_3d_exterior_Neumann.json), 4 bounces;
+    evaluation at the 256^2 points of the z = 0 slice over [-2, 2]^2 outside the surface.
+
+    Both estimators run progressive iterations (plain_paths / cv_paths new paths per point each) and
+    the RMSE of the running estimate is taken after each; times are wall-clock on a synchronised
+    device, excluding only the RMSE evaluation. The control variate's clock starts before its
+    training labels: labels (65,536 boundary points x 256-path walk estimates of the density,
+    clamped to the 0.999 quantile of their magnitude), 2000 device Adam steps of the 32-frequency 4 x 64 SiLU network, the network at every
+    triangle's centroid, the residual Neumann data, the residual scene, the control variate's
+    potential at the points, then the residual walks. Returns a dict."""
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import cv
+    scene, pts, exact_u, F = exterior_neumann_case(dev, subdiv, seed)
     n_pts = len(pts)
     d_pts = torch.from_numpy(pts).to(dev)
     base = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.ExteriorDomain,
@@ -1187,8 +1292,8 @@ def main():
     ap.add_argument("--ref-points", type=int, default=768, help="points per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
-    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "mrhs3d", "build3d", "vpl2d",
-                                           "wos2d"],
+    ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "fwd3d", "mrhs3d", "build3d",
+                                           "vpl2d", "wos2d"],
                     default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
@@ -1201,6 +1306,9 @@ def main():
     ap.add_argument("--cv-near", type=float, default=3.0, help="near-field factor of the control-variate tables")
     ap.add_argument("--cv-theta", type=float, default=0.3,
                     help="cluster acceptance of the control-variate tables' far field (0: every triangle)")
+    ap.add_argument("--fwd-paths", type=int, default=256, help="paths per point per step of --workload fwd3d")
+    ap.add_argument("--fwd-config", type=int, default=-1,
+                    help="--workload fwd3d: kernel configuration (0 lockstep; 1-3 + 4k wavefront; -1 autotune)")
     ap.add_argument("--no-time-to-rmse", action="store_true",
                     help="skip the plain vs learned-CV time-to-RMSE leg of the default workload")
     ap.add_argument("--mrhs-subdiv", type=int, default=8, help="icosphere subdivision of --workload mrhs3d")
@@ -1226,6 +1334,8 @@ def main():
         run_batch(args)
     elif args.workload == "cv3d":
         run_cv(args)
+    elif args.workload == "fwd3d":
+        run_fwd3d(args)
     elif args.workload == "mrhs3d":
         run_multi_rhs(args)
     elif args.workload == "build3d":

@@ -174,8 +174,11 @@ int wob_solve_domain_host(wob_scene scene, const wob_params *params, const float
  * the specialised walk kernels are compiled for several occupancy targets (minimum resident
  * blocks per SM 1, 5, 6, 8) and run with a cap on the paths one lane takes per warp unit (the
  * launcher's choice up to 8, or 4, 2, 1) -- WOB_TUNE_CONFIGS configurations, index = occupancy +
- * 4 x cap. This times each on the first points (device pointer, about 2^21 paths) with the given
- * parameters and makes the fastest the one used for that kernel variant from then on
+ * 4 x cap; the 3D forward single-layer walk's shapes are the lockstep kernel and the split-phase
+ * wavefront's three trace shapes, its second index the wavefront's chunk size. This times each on
+ * the first points (device pointer, about 2^23 paths, the paths per lane that a launch over all
+ * n_points would take) with the given parameters and makes the fastest the one used for that
+ * kernel variant from then on
  * (process-wide). chosen = index of the chosen configuration (-1: these parameters use no
  * tunable kernel), ms_per_config[k] = time of configuration k (room for WOB_TUNE_CONFIGS),
  * n_configs = number of configurations. Allocates a temporary output buffer and synchronises

@@ -34,7 +34,7 @@ def boundary_data(u_at, verts, normals, types, alpha):
     return g.astype(F32)
 
 
-def scene2d(problem: int, exterior: bool, n_seg: int = 96, seed: int = 1):
+def scene2d(problem: int, exterior: bool, n_seg: int = 96, seed: int = 1, n_points: int = 10):
     verts, normals = W.star_polygon(n_seg, 3, 0.25)
     if exterior:  # apps/general_2d.cu:204-207
         verts = (verts * F32(0.5)).astype(F32)
@@ -50,12 +50,12 @@ def scene2d(problem: int, exterior: bool, n_seg: int = 96, seed: int = 1):
     pts = grid[mask]
     if exterior:
         pts = pts[np.linalg.norm(pts - np.array([0, 0.0625], F32), axis=1) > 0.15]
-    pts = pts[np.random.default_rng(seed).permutation(len(pts))[:10]]
+    pts = pts[np.random.default_rng(seed).permutation(len(pts))[:n_points]]
     return dict(verts=verts, normals=normals, bvals=g, types=types, alphas=alphas,
                 points=np.ascontiguousarray(pts, dtype=F32), u=lambda p: _u2d(p, exterior))
 
 
-def scene3d(problem: int, exterior: bool, subdiv: int = 2, seed: int = 3):
+def scene3d(problem: int, exterior: bool, subdiv: int = 2, seed: int = 3, n_points: int = 10):
     V, F, _ = W.displaced_icosphere(subdiv, 0.1, 4, seed)
     verts, normals = W.mesh_elements(V, F)
     types = types_for(problem, len(F), seed)
@@ -68,9 +68,9 @@ def scene3d(problem: int, exterior: bool, subdiv: int = 2, seed: int = 3):
     g = boundary_data(u_at, verts, normals, types, alpha)
     alphas = np.full((len(F), 3), alpha, dtype=F32)
     rng = np.random.default_rng(seed)
-    dirs = rng.standard_normal((10, 3))
+    dirs = rng.standard_normal((n_points, 3))
     dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
-    radius = rng.uniform(0.1, 0.5, 10) if not exterior else rng.uniform(1.8, 2.5, 10)
+    radius = rng.uniform(0.1, 0.5, n_points) if not exterior else rng.uniform(1.8, 2.5, n_points)
     pts = (dirs * radius[:, None]).astype(F32)
     return dict(verts=verts, normals=normals, bvals=g, types=types, alphas=alphas, points=pts, u=u_at)
 

@@ -211,6 +211,7 @@ int check_params(const wob_scene_s *s, const wob_params *p, wobgb::WalkParams &w
     w.ppt = 1;
     w.ppt_cap = 0;
     w.no_alloc = 0;
+    w.ppt_points = 0;
     w.mode = 0;
     w.n_pot = 0;
     w.m_ker = 0;
@@ -724,9 +725,11 @@ int wob_autotune_domain(wob_scene s, const wob_params *params, const float *poin
     if (n_configs) *n_configs = 0;
     if (v < 0 || n_points == 0) return WOB_OK;
     if (!points) return fail(WOB_ERR_INVALID_ARGUMENT, "points is NULL");
-    // Time each configuration on enough points for about 2^21 paths (or all points).
-    const uint64_t want = ((1ull << 21) + w.n_paths - 1) / w.n_paths;
+    // Time each configuration on enough points for about 2^23 paths (or all points), with the paths
+    // per lane that a launch over all n_points would choose (a subset would choose fewer).
+    const uint64_t want = ((1ull << 23) + w.n_paths - 1) / w.n_paths;
     const uint32_t n_sub = (uint32_t)(want < n_points ? want : n_points);
+    w.ppt_points = n_points;
     DeviceGuard g(s->device);
     cudaStream_t cs = (cudaStream_t)stream;
     double *tmp = nullptr;

@@ -15,7 +15,7 @@ namespace wobgb {
 constexpr float kEps10 = 10.0f * 1.1920928955078125e-7f;  // 10 FLT_EPSILON (scene.cuh:418, 531)
 constexpr uint32_t kHitBuffer = 64;                         // hit buffer of scene.cuh:481
 constexpr uint32_t kStackSize = 64;
-constexpr int kWalkBlock = 128;   // threads per block of every kernel that runs 3D line queries
+constexpr int kWalkBlock = 128;   // threads per block of the walk kernels (and of the shared stack columns)
 constexpr int kSharedStack = 24;  // entries of a thread's 3D traversal stack held in shared memory
 constexpr int kLeafBatch = 8;     // leaves a 3D line query holds before testing them
 constexpr uint32_t kChildEmptyD = 0xFFFFFFFFu;
@@ -542,17 +542,11 @@ __device__ __forceinline__ uint32_t leaf_hits(const SceneView<D> &s, uint32_t co
     return count;
 }
 
-// The 3D line query. Depth-first over the 4-wide BVH, children in order, so the leaves (and the
-// hits) come in storage order:
-// - the first child a node's test keeps is visited next straight from a register; only its
-//   later siblings are pushed (in reverse order), so descending costs no stack traffic;
-// - the stack's first kSharedStack entries live in shared memory, one 4-byte column per thread
-//   (entry-major: lanes at different depths still touch distinct banks), deeper entries in a
-//   local array; the held leaves likewise;
-// - leaves are postponed: a lane takes nodes until it holds kLeafBatch leaves or has nothing
-//   left, then tests the held leaves in the order it met them, so the lanes of a warp run node
-//   tests together and triangle tests together instead of alternating between them.
-// Every kernel that calls it runs kWalkBlock threads per block.
+// Shared-memory columns of a thread's traversal stack and held leaves (entry-major: lanes at
+// different depths still touch distinct banks), for kernels that run nothing but line queries
+// (the wavefront's trace kernel). A kernel that references them gets the arrays as static shared
+// memory, so walk kernels keep their stacks in local memory instead (line_query3), where the
+// shared memory would only take L1 capacity from their gathers.
 __device__ __forceinline__ uint32_t *stack_column() {
     __shared__ uint32_t s_stack[kSharedStack * kWalkBlock];
     return s_stack + threadIdx.x;
@@ -562,10 +556,16 @@ __device__ __forceinline__ uint32_t *leaf_column() {
     return s_leaf + threadIdx.x;
 }
 
+// The 3D line query. Depth-first over the 4-wide BVH, children in order, so the leaves (and the
+// hits) come in storage order:
+// - the first child a node's test keeps is visited next straight from a register; only its
+//   later siblings are pushed (in reverse order), so descending costs no stack traffic;
+// - leaves are postponed: a lane takes nodes until it holds kLeafBatch leaves or has nothing
+//   left, then tests the held leaves in the order it met them, so the lanes of a warp run node
+//   tests together and triangle tests together instead of alternating between them.
 __device__ __forceinline__ uint32_t line_query3(const SceneView<3> &s, const V<3> &o, const V<3> &d, uint32_t *hits) {
-    uint32_t *const my_stack = stack_column();
-    uint32_t *const my_leaf = leaf_column();
-    uint32_t spill[kStackSize - kSharedStack];
+    uint32_t stack[kStackSize];
+    uint32_t leaves[kLeafBatch];
     const LineSlab3 L = line_slab3(o, d);
     int sp = 0;
     uint32_t code = 0u;  // root node
@@ -580,8 +580,7 @@ __device__ __forceinline__ uint32_t line_query3(const SceneView<3> &s, const V<3
                 break;
             }
             if (code & 0x80000000u) {
-                my_leaf[nl * kWalkBlock] = code;
-                nl++;
+                leaves[nl++] = code;
             } else {
                 uint4 ch;
                 uint32_t keep = node_hits(s, code, L, ch);
@@ -598,11 +597,7 @@ __device__ __forceinline__ uint32_t line_query3(const SceneView<3> &s, const V<3
                     const uint32_t first = (uint32_t)(__ffs(keep) - 1);
 #pragma unroll
                     for (int k = 3; k >= 1; k--)
-                        if ((uint32_t)k > first && ((keep >> k) & 1u)) {
-                            if (sp < kSharedStack) my_stack[sp * kWalkBlock] = cs[k];
-                            else spill[sp - kSharedStack] = cs[k];
-                            sp++;
-                        }
+                        if ((uint32_t)k > first && ((keep >> k) & 1u)) stack[sp++] = cs[k];
                     code = cs[first];
                     continue;
                 }
@@ -611,10 +606,9 @@ __device__ __forceinline__ uint32_t line_query3(const SceneView<3> &s, const V<3
                 live = false;
                 break;
             }
-            sp--;
-            code = sp < kSharedStack ? my_stack[sp * kWalkBlock] : spill[sp - kSharedStack];
+            code = stack[--sp];
         }
-        for (int l = 0; l < nl; l++) count = leaf_hits<3>(s, my_leaf[l * kWalkBlock], o, d, hits, count);
+        for (int l = 0; l < nl; l++) count = leaf_hits<3>(s, leaves[l], o, d, hits, count);
     }
     return count;
 }

@@ -13,7 +13,7 @@
 
 namespace wobgb {
 
-constexpr int kBlock = kWalkBlock;  // the 3D line query keeps its stack in shared memory columns of this block
+constexpr int kBlock = kWalkBlock;  // threads per block of the walk kernels
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -272,7 +272,7 @@ cudaError_t launch_domain_variant(const SceneView<D> &s, const WalkParams &p_in,
                                   double *sum, double *sumsq, unsigned long long *bounces, float *per_path,
                                   cudaStream_t stream) {
     WalkParams p = p_in;
-    p.ppt = choose_ppt(n_points, p.n_paths);
+    p.ppt = choose_ppt(p.ppt_points ? p.ppt_points : n_points, p.n_paths);
     if (p.ppt_cap && p.ppt > p.ppt_cap) p.ppt = p.ppt_cap;
     const uint64_t units = (uint64_t)n_points * ((p.n_paths + 32u * p.ppt - 1u) / (32u * p.ppt));
     if (per_path) {

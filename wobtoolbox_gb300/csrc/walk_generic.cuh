@@ -21,6 +21,7 @@ struct WalkParams {
     uint32_t ppt;   // paths per lane in one warp unit (set by the launcher, >= 1)
     uint32_t ppt_cap;  // 0: the launcher's choice; else at most this many (an autotuned setting)
     uint32_t no_alloc;  // 1: only kernels that allocate nothing (the allocation-free entry point)
+    uint32_t ppt_points;  // 0: paths per lane chosen for the launch's points; else for this many (autotune)
     uint32_t mode;  // boundary kernel: 0 = boundary estimate, 1 = unknown boundary density
     uint32_t n_pot, m_ker;  // control-variate estimator: samples of <G_x, sigma~> and of K sigma~
 };
@@ -408,14 +409,12 @@ template <int D, int kBie = -1, int kStrat = kStratRuntime, bool kVol = true, bo
                 w = w * fbu(y_prev, y, ip, true);
                 y_prev = y;
             } else if (!kVol || p.n_volume == 0) {
-                // no draw between the two samples (fbk draws only for a source term): take both at once
+                // no draw between the two samples (fbk draws only for a source term): take both at
+                // once. The last bounce's transport (second sample, fbu) goes unused but is kept:
+                // a straight-line loop body measured faster here (the headline workload) than an
+                // exit before it, and nothing draws after the walk, so no value changes
                 BPoint<D> ya;
                 float ipa;
-                if (last) {
-                    ya = sample_uniform<D>(s, rng, ipa);
-                    contrib = contrib + w * fbk(y_prev, ya, ipa);
-                    break;
-                }
                 sample_uniform_pair<D>(s, rng, ya, ipa, y, ip);
                 contrib = contrib + w * fbk(y_prev, ya, ipa);
                 w = w * fbu(y_prev, y, ip, true);
