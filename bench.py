@@ -270,6 +270,24 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def slice_inside(scene, cand, dev):
+    """Inside test of points against a closed 3D scene on the GPU: an odd number of crossings of a
+    half-line (probe_dirs) through the point. Returns a numpy bool mask."""
+    import torch
+    n_c = len(cand)
+    d_c = torch.from_numpy(np.ascontiguousarray(cand)).to(dev)
+    d_dir = torch.from_numpy(probe_dirs(n_c)).to(dev)
+    counts = torch.zeros(n_c, dtype=torch.int32, device=dev)
+    hits = torch.zeros(n_c, 64, dtype=torch.int32, device=dev)
+    hp = torch.zeros(n_c, 64, 3, dtype=torch.float32, device=dev)
+    scene.line_query(d_c, d_dir, n_c, counts, hits, hp)
+    m = torch.clamp(counts, max=64)
+    valid = torch.arange(64, device=dev)[None, :] < m[:, None]
+    t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
+    crossings = ((t > 0) & valid).sum(1)
+    return (crossings % 2 == 1).cpu().numpy()
+
+
 def run_ours(args):
     import torch
     import wobtoolbox_gb300 as wob
@@ -292,22 +310,8 @@ def run_ours(args):
     else:
         sc = build_scene_arrays()
         scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
-        # inside test of every slice point on the GPU: odd number of crossings of a half-line
         cand = W.slice_points_z0(GRID, EXTENT)
-        n_c = len(cand)
-        d_c = torch.from_numpy(cand).to(dev)
-        d_dir = torch.from_numpy(probe_dirs(n_c)).to(dev)
-        counts = torch.zeros(n_c, dtype=torch.int32, device=dev)
-        hits = torch.zeros(n_c, 64, dtype=torch.int32, device=dev)
-        hp = torch.zeros(n_c, 64, 3, dtype=torch.float32, device=dev)
-        scene.line_query(d_c, d_dir, n_c, counts, hits, hp)
-        m = torch.clamp(counts, max=64)
-        valid = torch.arange(64, device=dev)[None, :] < m[:, None]
-        t = ((hp - d_c[:, None, :]) * d_dir[:, None, :]).sum(-1)
-        crossings = ((t > 0) & valid).sum(1)
-        inside = (crossings % 2 == 1).cpu().numpy()
-        del hits, hp
-        pts = np.ascontiguousarray(cand[inside])
+        pts = np.ascontiguousarray(cand[slice_inside(scene, cand, dev)])
         paths = PATHS
         p = params()
         exact_u = None
@@ -1136,13 +1140,164 @@ def run_build(args):
 VPL_FLOPS_PER_PAIR_2D = 60  # FP32 operations of one (point, VPL) pair: G, dG/dx, three products and sums
 
 
+def run_fmad(args):
+    """What the bit-exact build costs: the hot workloads with FMA contraction on. The contraction-
+    enabled variant of the library (wobtoolbox_gb300/_lib/fma/, every CUDA unit with -fmad=true,
+    built here on demand) runs in the same process beside the default build; each workload is timed
+    on both (CUDA events, L2 flushed between steps) and the two builds' per-point estimates, drawn
+    with different seeds, are compared by z-scores (the fast build is not path-for-path identical
+    to the oracle, so it is validated statistically against the exact one):
+      robin3d -- the headline step (timing only: the alpha = 2 series diverges, see DESIGN.md);
+      dl2d    -- configs[0] at 1024 paths x 8 bounces;
+      fwd3d   -- the 327,680-triangle forward walk, 256 paths;
+      vpl2d   -- the VPL aggregation over the same VPLs (deterministic: relative difference)."""
+    import ctypes as C
+    import torch
+    import wobtoolbox_gb300 as wob
+    from wobtoolbox_gb300 import _capi
+    from wobtoolbox_gb300 import build as B
+    from wobtoolbox_gb300 import workloads as W
+    rank, world, local = dist_init(args)
+    exact = wob.load()
+    fma = _capi.load_library(B.build(fma=True))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def make(lib, verts, normals, bvals, types, alphas=None):
+        f = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+        v, n_, b_, a_ = f(verts), f(normals), f(bvals), f(alphas)
+        t = np.ascontiguousarray(types, np.int32)
+        h = C.c_void_p()
+        st = lib.wob_scene_create(v.shape[1], len(v), v.ctypes.data, n_.ctypes.data, b_.ctypes.data,
+                                  None if a_ is None else a_.ctypes.data, t.ctypes.data, C.byref(h))
+        if st != 0:
+            raise RuntimeError(lib.wob_last_error().decode())
+        return h
+
+    def solve(lib, h, p, d, n, s_, q_, steps, base_offset, tune):
+        pc = p.to_c()
+        if tune:
+            chosen, nc = C.c_int32(-1), C.c_int32(0)
+            ms = (C.c_float * 64)()
+            lib.wob_autotune_domain(h, C.byref(pc), d.data_ptr(), n, C.byref(chosen), ms, C.byref(nc),
+                                    C.c_void_p(stream.cuda_stream))
+        times = []
+        for k in range(steps + 1):  # launch 0 warms up; its sums are discarded
+            if k == 1:
+                s_.zero_()
+                q_.zero_()
+            flush.fill_(float(k))
+            pk = dataclasses.replace(p, path_offset=base_offset + k * p.num_sample_paths).to_c()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = lib.wob_solve_domain(h, C.byref(pk), d.data_ptr(), n, s_.data_ptr(), q_.data_ptr(), None,
+                                      C.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if st != 0:
+                raise RuntimeError(lib.wob_last_error().decode())
+            if k:
+                times.append(e0.elapsed_time(e1))
+        return min(times)
+
+    def compare(name, arrays, p, pts, steps, tune, z_test=True):
+        d = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
+        n = len(pts)
+        D = pts.shape[1]
+        res = {}
+        stats_ = {}
+        for label, lib, seed in (("exact", exact, SEED), ("fma", fma, SEED + 1)):
+            h = make(lib, *arrays)
+            s_ = torch.zeros(n, D + 1, dtype=torch.float64, device=dev)
+            q_ = torch.zeros_like(s_)
+            res[label] = solve(lib, h, dataclasses.replace(p, seed=seed), d, n, s_, q_, steps, 0, tune)
+            stats_[label] = (s_[:, 0].cpu().numpy(), q_[:, 0].cpu().numpy())
+            lib.wob_scene_destroy(h)
+        out = {"exact_ms": res["exact"], "fma_ms": res["fma"], "speedup": res["exact"] / res["fma"]}
+        if z_test:
+            N = steps * p.num_sample_paths
+            (sa, qa), (sb, qb) = stats_["exact"], stats_["fma"]
+            ma, mb = sa / N, sb / N
+            va, vb = np.maximum(qa / N - ma ** 2, 0), np.maximum(qb / N - mb ** 2, 0)
+            z = (ma - mb) / np.sqrt(np.maximum(va / N + vb / N, 1e-300))
+            from scipy import stats as sst
+            out.update({"points": n, "paths_per_point": N, "max_abs_z": float(np.abs(z).max()),
+                        "bonferroni_bound": float(sst.norm.isf(1e-3 / (2 * n))), "mean_z": float(z.mean())})
+        return out
+
+    results = {}
+    sc = build_scene_arrays()
+    cand = W.slice_points_z0(GRID, EXTENT)
+    tmp = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
+    pts = np.ascontiguousarray(cand[slice_inside(tmp, cand, dev)])
+    tmp.close()
+    results["robin3d"] = compare("robin3d", (sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"]),
+                                 dataclasses.replace(params(), num_sample_paths=PATHS), pts, 2, True, z_test=False)
+    c0 = W.config0_scene()
+    p0 = wob.EstimatorParams(bie_model=wob.IndirectDoubleLayer, domain=wob.InteriorDomain,
+                             estimator=wob.BackwardEstimator, problem=wob.DirichletProblem, path_length=8,
+                             num_sample_paths=1024, seed=SEED)
+    results["dl2d"] = compare("dl2d", (c0["verts"], c0["normals"], c0["bvals"], c0["types"], None), p0,
+                              c0["points"], 2, True)
+    scene3, pts3, _, _ = exterior_neumann_case(dev, args.cv_subdiv, SEED)
+    v3, n3, b3, t3, _ = scene3.stored_arrays()
+    scene3.close()
+    p3 = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.ExteriorDomain,
+                             estimator=wob.ForwardEstimator, problem=wob.NeumannProblem, path_length=4, seed=SEED,
+                             num_sample_paths=256)
+    results["fwd3d"] = compare("fwd3d", (v3, n3, b3, t3, None), p3, pts3, 4, False)
+    # VPL aggregation over one set of VPLs (from the exact build's walks), both builds
+    verts, nrm, data, ty, circles = W.vpl_flow_scene()
+    g, keep = W.vpl_flow_points(256, circles)
+    vpts = torch.from_numpy(np.ascontiguousarray(g[keep])).to(dev)
+    M = 100000
+    pv = wob.EstimatorParams(bie_model=wob.IndirectSingleLayer, domain=wob.InteriorDomain,
+                             estimator=wob.BackwardEstimator, problem=wob.NeumannProblem, path_length=4,
+                             num_resampling_candidates=1024, eps=1e-4, seed=SEED)
+    vp = torch.zeros(M, 2, dtype=torch.float32, device=dev)
+    vm = torch.zeros(M, dtype=torch.float32, device=dev)
+    h = make(exact, verts, nrm, data, ty)
+    exact.wob_vpl_paths(h, C.byref(pv.to_c()), M, vp.data_ptr(), vm.data_ptr(), None, C.c_void_p(stream.cuda_stream))
+    agg = {}
+    for label, lib in (("exact", exact), ("fma", fma)):
+        hh = h if lib is exact else make(fma, verts, nrm, data, ty)
+        ms = []
+        for k in range(4):
+            sv = torch.zeros(len(vpts), 3, dtype=torch.float64, device=dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lib.wob_vpl_aggregate(hh, 1e-4, vp.data_ptr(), vm.data_ptr(), M, vpts.data_ptr(), len(vpts), sv.data_ptr(),
+                                  C.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k:
+                ms.append(e0.elapsed_time(e1))
+        agg[label] = (min(ms), sv[:, 0].cpu().numpy())
+        if lib is fma:
+            fma.wob_scene_destroy(hh)
+    exact.wob_scene_destroy(h)
+    rel = np.abs(agg["exact"][1] - agg["fma"][1]).max() / np.abs(agg["exact"][1]).max()
+    results["vpl2d_aggregation"] = {"exact_ms": agg["exact"][0], "fma_ms": agg["fma"][0],
+                                    "speedup": agg["exact"][0] / agg["fma"][0], "max_rel_diff": float(rel)}
+    out = {"metric": "time per step, bit-exact build (-fmad=false) vs contraction-enabled build (-fmad=true)",
+           "value": results["robin3d"]["speedup"], "unit": "x (exact time / contracted time, headline step)",
+           "n_gpus": world, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "headline robin3d, dl2d (configs[0]), fwd3d (configs[3]'s walk), VPL aggregation",
+                      "note": "per-point estimates of the two builds drawn with different seeds; z = difference / "
+                              "combined standard error"},
+           "results": results}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_vpl(args):
     """VPL potential flow (apps/potential_flow_with_vpl.cu with data/config_potential_flow_with_vpl.json:
     100,000 paths per iteration, 4 bounces, 1024 RIS candidates, eps 1e-4, 256^2 grid minus the four
     obstacles): per iteration the VPL walks and the dense aggregation over every (point, VPL) pair,
-    each timed with CUDA events. The aggregation is FP32-issue bound; its roofline is the FP32
-    operation rate 152 SMs x 128 lanes x SM clock (no FMA: the kernels keep every product and sum
-    separately rounded)."""
+    each timed with CUDA events. The aggregation is FP32-issue bound; its roofline is the FP32 FMA
+    rate 2 x 152 SMs x 128 lanes x SM clock (the bit-exact build keeps every product and sum
+    separately rounded, so half of that is its ceiling; --workload fmad measures the difference)."""
     import torch
     import wobtoolbox_gb300 as wob
     from wobtoolbox_gb300 import workloads as W
@@ -1189,7 +1344,7 @@ def run_vpl(args):
     agg = sum(t_agg) / len(t_agg)
     pth = sum(t_paths) / len(t_paths)
     mhz = clocks.get("sm_mhz") or 2070.0
-    peak = 152 * 128 * mhz * 1e6 / 1e12
+    peak = 2 * 152 * 128 * mhz * 1e6 / 1e12  # FP32 with FMA counted as two operations
     achieved = pairs * VPL_FLOPS_PER_PAIR_2D / agg / 1e12
     u = (s[:, 0] / (args.steps * M)).cpu().numpy()
     gx = (s[:, 1] / (args.steps * M)).cpu().numpy()
@@ -1202,9 +1357,10 @@ def run_vpl(args):
                       "iteration_ms": {"vpl_walks": pth * 1e3, "aggregation": agg * 1e3},
                       "walk_bounces_per_s": int(b.item()) / sum(t_paths),
                       "mean_grad_x_far_field": float(np.mean(gx[np.abs(pts[:, 1]) > 0.45]))},
-           "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s (FP32, no FMA)",
+           "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s (FP32)",
                         "frac": achieved / peak, "flops_per_pair": VPL_FLOPS_PER_PAIR_2D,
-                        "peak_source": "152 SMs x 128 FP32 lanes x median SM clock during the run"},
+                        "peak_source": "152 SMs x 128 FP32 lanes x 2 (FMA) x median SM clock during the run; "
+                                       "the bit-exact build issues no FMA, so half of this is its ceiling"},
            "clocks": clocks}
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -1293,7 +1449,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profiling case: 1/16 of the points, 512 paths")
     ap.add_argument("--workload", choices=["robin3d", "dl2d", "batch2d", "cv3d", "fwd3d", "mrhs3d", "build3d",
-                                           "vpl2d", "wos2d"],
+                                           "vpl2d", "wos2d", "fmad"],
                     default="robin3d",
                     help="robin3d: the headline 3D Robin icosphere workload; dl2d: 2D double-layer star; "
                          "batch2d: 256 batched 2D scenes vs sequential launches")
@@ -1344,6 +1500,8 @@ def main():
         run_vpl(args)
     elif args.workload == "wos2d":
         run_wos(args)
+    elif args.workload == "fmad":
+        run_fmad(args)
     else:
         run_ours(args)
 

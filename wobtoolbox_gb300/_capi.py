@@ -75,7 +75,15 @@ def load() -> C.CDLL:
         return _lib
     if not os.path.exists(LIB_PATH):
         raise WobError(3, f"engine library not built: {LIB_PATH} (run __graft_entry__.build())")
-    lib = C.CDLL(LIB_PATH)
+    _lib = load_library(LIB_PATH)
+    return _lib
+
+
+def load_library(path: str) -> C.CDLL:
+    """Loads a build of the engine library from `path` with every signature set (a second build,
+    such as the contraction-enabled measurement variant, lives beside the default one in the same
+    process: each library has its own device code and state)."""
+    lib = C.CDLL(path)
     vp, u32, u64, i32, f32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_float
     P = C.POINTER
     sigs = {
@@ -142,7 +150,6 @@ def load() -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
     return lib
 
 

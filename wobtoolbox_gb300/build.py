@@ -19,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_build", platform.machine())  # objects per host architecture
 LIB = os.path.join(OUT, "libwob_gb300.so")
+FMA_OUT = os.path.join(OUT, "fma")
+FMA_LIB = os.path.join(FMA_OUT, "libwob_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -112,14 +114,19 @@ def _obj_stale(obj: str, src: str, headers: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in [src] + headers)
 
 
-def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
-    """Compiles the library if any source changed; returns its path."""
-    os.makedirs(OUT, exist_ok=True)
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False, fma: bool = False) -> str:
+    """Compiles the library if any source changed; returns its path. fma=True builds the
+    measurement variant into _lib/fma/ instead: every CUDA unit with FMA contraction (-fmad=true),
+    host code unchanged, no apps -- its paths are not bit-identical to the oracle's; it exists to
+    measure what the bit-exact build costs (bench.py --workload fmad)."""
+    out_dir, build_dir, lib_path = (FMA_OUT, BUILD + "_fma", FMA_LIB) if fma else (OUT, BUILD, LIB)
+    os.makedirs(out_dir, exist_ok=True)
+    os.makedirs(build_dir, exist_ok=True)
     deps = _deps()
-    if not force and not ptxas_info and not _stale(LIB, deps):
-        build_apps()
-        return LIB
+    if not force and not ptxas_info and not _stale(lib_path, deps):
+        if not fma:
+            build_apps()
+        return lib_path
     nvcc = nvcc_path()
     cxx = os.environ.get("CXX", "g++")
     jobs = []
@@ -127,15 +134,15 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))]
     headers += [os.path.join(INCLUDE, "wob_capi.h"), os.path.abspath(__file__)]
     for src in CU_SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(build_dir, src.replace(".cu", ".o"))
         objs.append(obj)
         if not (force or ptxas_info) and not _obj_stale(obj, os.path.join(CSRC, src), headers):
             continue
         extra = ["-Xptxas", "-v"] if ptxas_info else []
-        jobs.append([nvcc] + cu_flags(extra, contract=src in CONTRACTED_SOURCES) +
+        jobs.append([nvcc] + cu_flags(extra, contract=fma or src in CONTRACTED_SOURCES) +
                     ["-c", os.path.join(CSRC, src), "-o", obj])
     for src in CPP_SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cpp", ".o"))
+        obj = os.path.join(build_dir, src.replace(".cpp", ".o"))
         objs.append(obj)
         if not force and not _obj_stale(obj, os.path.join(CSRC, src), headers):
             continue
@@ -149,12 +156,13 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
                 raise RuntimeError("build failed:\n" + " ".join(j) + "\n" + proc.stdout + proc.stderr)
             if verbose or ptxas_info:
                 sys.stderr.write(proc.stderr)
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fPIC"])
-    os.replace(tmp, LIB)
-    build_apps(force=True)
-    return LIB
+    os.replace(tmp, lib_path)
+    if not fma:
+        build_apps(force=True)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv, fma="--fma" in sys.argv))
