@@ -712,8 +712,9 @@ def run_fwd3d(args):
                                f"{len(F)} triangles, {n} slice points outside the surface, {paths} paths per point "
                                "per step",
                    "kernel_config": cfg.value,
-                   "kernel": (f"split-phase wavefront, trace shape {cfg.value % 4}, {chunk} paths per chunk" if wave
-                              else "lockstep walk"),
+                   "kernel": (f"split-phase wavefront, trace shape {cfg.value % 4}"
+                              f"{' (compressed nodes)' if cfg.value % 4 == 3 else ''}, {chunk} paths per chunk"
+                              if wave else "lockstep walk"),
                    "autotune": None if tuned is None else {"chosen_config": tuned[0], "ms_per_config": tuned[1]},
                    "l2": "flushed between timed steps (256 MiB write, outside the timed events)"},
         "lockstep_ms_per_step": lock_ms,

@@ -11,8 +11,9 @@
 //   trace    -- persistent: every lane takes the next pending query (one atomic per warp for all
 //               lanes that need one) as soon as its previous query has ended, so a lane never
 //               waits for another lane's query; the traversal is line_query3's (shared-memory
-//               stack columns, first kept child from a register, postponed leaves), and the hit is
-//               chosen where the hits are (line_hit_choice, the path's own next draw);
+//               stack columns, first kept child from a register, postponed leaves), optionally on
+//               64-byte compressed nodes built per solve, and the hit is chosen where the hits are
+//               (line_hit_choice, the path's own next draw);
 //   consume  -- one thread per path: the hit's point, the transport weight, the next bounce's terms
 //               and the next direction (repeated path_length - 1 times with trace);
 //   reduce   -- one warp per point: FP64 sums and squares over its paths.
@@ -121,9 +122,96 @@ __global__ void __launch_bounds__(kWalkBlock) wave_start_kernel(SceneView<3> s, 
     a.draws[j] = w.rng.drawn();
 }
 
-// The trace phase. kLeaves: leaves a lane holds before testing them (line_query3's kLeafBatch).
-template <int kMinB, int kLeaves>
-__global__ void __launch_bounds__(kWalkBlock, kMinB) wave_trace_kernel(SceneView<3> s, WalkParams p, WaveArgs a) {
+// Compressed BVH nodes for the trace phase: 64 bytes instead of 128 (two 32-byte sectors a visit
+// instead of four). Each child's box is stored as 8-bit offsets on a power-of-two grid over the
+// node's own box: words 0-2 the node box's lower corner o (float), word 3 the grid's biased
+// exponents per axis (byte a), words 4-7 the children, words 8-13 the quantized bounds (word 8 + a:
+// lower bound on axis a, byte k for child k; word 11 + a: upper bounds), words 14-15 zero. Lower
+// bounds are rounded down and upper bounds up (in double), so every decoded box contains its
+// child's padded box up to one float rounding of o + q 2^e -- far inside the boxes' 1e-5 padding:
+// the box test stays conservative and the hits (decided by the exact triangle test) are unchanged.
+constexpr int kQNodeWords = 16;
+
+__global__ void compress_nodes_kernel(const float4 *__restrict__ soa, uint32_t n_nodes, uint32_t *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const float *q = reinterpret_cast<const float *>(soa + 8 * (size_t)i);
+    const uint32_t *c = reinterpret_cast<const uint32_t *>(q + 24);
+    uint32_t w[kQNodeWords] = {};
+    double lo[3], ext[3];
+    for (int a = 0; a < 3; a++) {
+        double mn = 1e300, mx = -1e300;
+        for (int k = 0; k < 4; k++) {
+            if (c[k] == kChildEmptyD) continue;
+            mn = fmin(mn, (double)q[4 * a + k]);
+            mx = fmax(mx, (double)q[12 + 4 * a + k]);
+        }
+        if (mn > mx) mn = mx = 0.0;
+        const float o = (float)mn <= mn ? (float)mn : nextafterf((float)mn, -INFINITY);  // o <= every lower bound
+        lo[a] = (double)o;
+        ext[a] = mx - lo[a];
+        int e = 0;
+        frexp(ext[a] / 255.0, &e);  // 2^e > ext / 255: 255 steps of 2^e cover the box
+        if (ext[a] <= 0.0) e = -126;
+        e = e < -126 ? -126 : (e > 127 ? 127 : e);
+        w[a] = __float_as_uint(o);
+        w[3] |= (uint32_t)(e + 127) << (8 * a);
+        const double step = ldexp(1.0, e);
+        for (int k = 0; k < 4; k++) {
+            double ql = 0.0, qh = 0.0;
+            if (c[k] != kChildEmptyD) {
+                ql = floor(((double)q[4 * a + k] - lo[a]) / step);
+                qh = ceil(((double)q[12 + 4 * a + k] - lo[a]) / step);
+            }
+            ql = fmin(fmax(ql, 0.0), 255.0);
+            qh = fmin(fmax(qh, 0.0), 255.0);
+            w[8 + a] |= (uint32_t)ql << (8 * k);
+            w[11 + a] |= (uint32_t)qh << (8 * k);
+        }
+    }
+    for (int k = 0; k < 4; k++) w[4 + k] = c[k];
+    uint4 *dst = reinterpret_cast<uint4 *>(out + (size_t)i * kQNodeWords);
+    for (int v = 0; v < 4; v++) dst[v] = make_uint4(w[4 * v], w[4 * v + 1], w[4 * v + 2], w[4 * v + 3]);
+}
+
+// The slab test against a compressed node's four children: per axis the decoded bound is
+// o + q 2^e (q exact in float, the product exact), then the FMA slab bound as in node_hits.
+__device__ __forceinline__ uint32_t qnode_hits(const uint32_t *__restrict__ qn, uint32_t node, const LineSlab3 &L,
+                                               uint4 &child) {
+    const float4 *p = reinterpret_cast<const float4 *>(qn + (size_t)node * kQNodeWords);
+    const F8 r0 = ldg8(p), r1 = ldg8(p + 2);
+    const float o[3] = {r0.a.x, r0.a.y, r0.a.z};
+    const uint32_t ex = __float_as_uint(r0.a.w);
+    child = make_uint4(__float_as_uint(r0.b.x), __float_as_uint(r0.b.y), __float_as_uint(r0.b.z),
+                       __float_as_uint(r0.b.w));
+    const uint32_t qlo[3] = {__float_as_uint(r1.a.x), __float_as_uint(r1.a.y), __float_as_uint(r1.a.z)};
+    const uint32_t qhi[3] = {__float_as_uint(r1.a.w), __float_as_uint(r1.b.x), __float_as_uint(r1.b.y)};
+    float step[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) step[a] = __uint_as_float(((ex >> (8 * a)) & 0xFFu) << 23);
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float tl[3], th[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float bl = __fmaf_rn((float)((qlo[a] >> (8 * k)) & 0xFFu), step[a], o[a]);
+            const float bh = __fmaf_rn((float)((qhi[a] >> (8 * k)) & 0xFFu), step[a], o[a]);
+            tl[a] = __fmaf_rn(bl, L.r[a], L.nor[a]);
+            th[a] = __fmaf_rn(bh, L.r[a], L.nor[a]);
+        }
+        const float tn = fmax3f(fminf(tl[0], th[0]), fminf(tl[1], th[1]), fminf(tl[2], th[2]));
+        const float tf = fmin3f(fmaxf(tl[0], th[0]), fmaxf(tl[1], th[1]), fmaxf(tl[2], th[2]));
+        if (tn <= tf) mask |= 1u << k;
+    }
+    return mask;
+}
+
+// The trace phase. kLeaves: leaves a lane holds before testing them (line_query3's kLeafBatch);
+// kQuant: node visits read the compressed nodes (qnodes) instead of the scene's.
+template <int kMinB, int kLeaves, bool kQuant>
+__global__ void __launch_bounds__(kWalkBlock, kMinB) wave_trace_kernel(SceneView<3> s, WalkParams p, WaveArgs a,
+                                                                      const uint32_t *__restrict__ qnodes) {
     static_assert(kLeaves <= kLeafBatch, "leaf columns hold kLeafBatch entries");
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t *const my_stack = stack_column();
@@ -178,7 +266,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinB) wave_trace_kernel(SceneView
                 nl++;
             } else {
                 uint4 ch;
-                uint32_t keep = node_hits(s, code, L, ch);
+                uint32_t keep = kQuant ? qnode_hits(qnodes, code, L, ch) : node_hits(s, code, L, ch);
                 const uint32_t cs[4] = {ch.x, ch.y, ch.z, ch.w};
 #pragma unroll
                 for (int k = 0; k < 4; k++)
@@ -299,9 +387,10 @@ __global__ void __launch_bounds__(kWalkBlock) wave_reduce_kernel(WalkParams p, W
     }
 }
 
-template <int kMinB, int kLeaves>
-cudaError_t trace(const SceneView<3> &s, const WalkParams &p, const WaveArgs &a, cudaStream_t stream) {
-    auto k = wave_trace_kernel<kMinB, kLeaves>;
+template <int kMinB, int kLeaves, bool kQuant>
+cudaError_t trace(const SceneView<3> &s, const WalkParams &p, const WaveArgs &a, const uint32_t *qnodes,
+                  cudaStream_t stream) {
+    auto k = wave_trace_kernel<kMinB, kLeaves, kQuant>;
     int per_sm = 0, dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -310,7 +399,7 @@ cudaError_t trace(const SceneView<3> &s, const WalkParams &p, const WaveArgs &a,
     const uint64_t need = ((uint64_t)a.n + kWalkBlock - 1) / kWalkBlock;
     const uint64_t grid = std::min<uint64_t>(need, (uint64_t)std::max(1, per_sm) * (uint64_t)sms);
     if ((e = cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
-    k<<<(unsigned)grid, kWalkBlock, 0, stream>>>(s, p, a);
+    k<<<(unsigned)grid, kWalkBlock, 0, stream>>>(s, p, a, qnodes);
     return cudaGetLastError();
 }
 
@@ -324,10 +413,18 @@ cudaError_t launch_fwd_wave_3d(const SceneView<3> &s, const WalkParams &p, const
     const uint64_t slots = (uint64_t)std::min(chunk_pts, n_points) * p.n_paths;
     if (slots > 0xFFFFFFFFull / 2) return cudaErrorInvalidValue;
     const size_t n = (size_t)slots;
+    const bool quant = shape == 3;
     const size_t words = n * (1 + kYWords + 1 + 4 + 3 + 2) + 1;
+    const size_t q_off = (words * 4 + 255) / 256 * 256;  // bytes; the compressed nodes 256-byte aligned
+    const size_t bytes = q_off + (quant ? (size_t)s.n_nodes * kQNodeWords * 4 : 0);
     void *buf = nullptr;
-    cudaError_t e = cudaMallocAsync(&buf, words * 4, stream);
+    cudaError_t e = cudaMallocAsync(&buf, bytes, stream);
     if (e != cudaSuccess) return e;
+    uint32_t *qnodes = quant ? (uint32_t *)((char *)buf + q_off) : nullptr;
+    if (quant && s.n_nodes) {
+        compress_nodes_kernel<<<(s.n_nodes + 127) / 128, 128, 0, stream>>>(s.nodes, s.n_nodes, qnodes);
+        e = cudaGetLastError();
+    }
     WaveArgs a{};
     a.pts = pts;
     uint32_t *w = (uint32_t *)buf;
@@ -348,9 +445,9 @@ cudaError_t launch_fwd_wave_3d(const SceneView<3> &s, const WalkParams &p, const
         e = cudaGetLastError();
         for (uint32_t m = 1; m < p.path_length && e == cudaSuccess; m++) {
             switch (shape) {
-            case 1: e = trace<8, 8>(s, p, a, stream); break;
-            case 2: e = trace<6, 8>(s, p, a, stream); break;
-            default: e = trace<8, 4>(s, p, a, stream); break;
+            case 1: e = trace<8, 8, false>(s, p, a, nullptr, stream); break;
+            case 2: e = trace<6, 8, false>(s, p, a, nullptr, stream); break;
+            default: e = trace<6, 8, true>(s, p, a, qnodes, stream); break;
             }
             if (e != cudaSuccess) break;
             wave_consume_kernel<<<blocks, kWalkBlock, 0, stream>>>(s, p, a, m);

@@ -16,11 +16,12 @@ namespace wobgb {
 // shapes) and c / 4: paths-per-lane cap {launcher's choice (up to 8), 4, 2, 1} for the lockstep
 // kernels, paths per wavefront chunk {2^22, 2^21, 2^20, 2^19} for the wavefront.
 namespace {
-// defaults: the 3D forward walk starts on the wavefront (trace at >= 6 blocks/SM, 2^22-path chunks)
-std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}, {2}};
+// defaults: the 3D forward walk starts on the wavefront (trace at >= 6 blocks/SM on compressed nodes,
+// 2^22-path chunks)
+std::atomic<int> g_config[kNumTunable] = {{0}, {0}, {0}, {3}};
 const char *kFwdNames[kTuneOccupancies] = {"lockstep walk, >=5 blocks/SM", "wavefront, trace >=8 blocks/SM",
                                            "wavefront, trace >=6 blocks/SM",
-                                           "wavefront, trace >=8 blocks/SM, 4-leaf batches"};
+                                           "wavefront, trace >=6 blocks/SM, 64-byte compressed nodes"};
 const uint32_t kWaveSlotsOf[kTunePptCaps] = {1u << 22, 1u << 21, 1u << 20, 1u << 19};
 const int kMinBOf[kTuneOccupancies] = {1, 5, 6, 8};
 const uint32_t kPptCapOf[kTunePptCaps] = {0u, 4u, 2u, 1u};

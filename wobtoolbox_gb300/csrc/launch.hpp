@@ -101,9 +101,9 @@ inline uint32_t choose_ppt(uint64_t n_points, uint32_t n_paths) {
 }
 
 // Forward single-layer Neumann walk in 3D as a split-phase wavefront (k_fwd_wave.cu): shape 1
-// traces at >= 8 blocks/SM with 8-leaf batches, 2 at >= 6 blocks/SM, 3 at >= 8 blocks/SM with
-// 4-leaf batches; paths advance in chunks of at most max_slots paths (whole points). Allocates its
-// path state stream-ordered (cudaMallocAsync).
+// traces at >= 8 blocks/SM, 2 at >= 6 blocks/SM, 3 at >= 6 blocks/SM on 64-byte compressed nodes
+// (built per solve); paths advance in chunks of at most max_slots paths (whole points). Allocates
+// its path state stream-ordered (cudaMallocAsync).
 cudaError_t launch_fwd_wave_3d(const SceneView<3> &s, const WalkParams &p, const float *pts, uint32_t n_points,
                                double *sum, double *sumsq, unsigned long long *bounces, float *per_path, int shape,
                                uint32_t max_slots, cudaStream_t stream);
