@@ -174,8 +174,15 @@ __global__ void compress_nodes_kernel(const float4 *__restrict__ soa, uint32_t n
     for (int v = 0; v < 4; v++) dst[v] = make_uint4(w[4 * v], w[4 * v + 1], w[4 * v + 2], w[4 * v + 3]);
 }
 
-// The slab test against a compressed node's four children: per axis the decoded bound is
-// o + q 2^e (q exact in float, the product exact), then the FMA slab bound as in node_hits.
+// The slab test against a compressed node's four children. With the node's corner o and grid step
+// s = 2^e per axis, a child bound o + q s lies on the line at t = q (s r) + (o r - O r): s r is exact
+// (a power of two times r), o r - O r one FMA per axis and node, and each bound then one FMA. q is
+// formed exactly by a byte permute into the float 2^23 + q and one subtraction, which keeps the
+// conversion off the special-function pipe. The t's rounding is of the order of the uncompressed
+// test's, far inside the boxes' padding.
+__device__ __forceinline__ float qbyte(uint32_t word, uint32_t k) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + k)) - 8388608.0f;
+}
 __device__ __forceinline__ uint32_t qnode_hits(const uint32_t *__restrict__ qn, uint32_t node, const LineSlab3 &L,
                                                uint4 &child) {
     const float4 *p = reinterpret_cast<const float4 *>(qn + (size_t)node * kQNodeWords);
@@ -186,19 +193,20 @@ __device__ __forceinline__ uint32_t qnode_hits(const uint32_t *__restrict__ qn, 
                        __float_as_uint(r0.b.w));
     const uint32_t qlo[3] = {__float_as_uint(r1.a.x), __float_as_uint(r1.a.y), __float_as_uint(r1.a.z)};
     const uint32_t qhi[3] = {__float_as_uint(r1.a.w), __float_as_uint(r1.b.x), __float_as_uint(r1.b.y)};
-    float step[3];
+    float A[3], B[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) step[a] = __uint_as_float(((ex >> (8 * a)) & 0xFFu) << 23);
+    for (int a = 0; a < 3; a++) {
+        A[a] = __uint_as_float(((ex >> (8 * a)) & 0xFFu) << 23) * L.r[a];
+        B[a] = __fmaf_rn(o[a], L.r[a], L.nor[a]);
+    }
     uint32_t mask = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         float tl[3], th[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const float bl = __fmaf_rn((float)((qlo[a] >> (8 * k)) & 0xFFu), step[a], o[a]);
-            const float bh = __fmaf_rn((float)((qhi[a] >> (8 * k)) & 0xFFu), step[a], o[a]);
-            tl[a] = __fmaf_rn(bl, L.r[a], L.nor[a]);
-            th[a] = __fmaf_rn(bh, L.r[a], L.nor[a]);
+            tl[a] = __fmaf_rn(qbyte(qlo[a], (uint32_t)k), A[a], B[a]);
+            th[a] = __fmaf_rn(qbyte(qhi[a], (uint32_t)k), A[a], B[a]);
         }
         const float tn = fmax3f(fminf(tl[0], th[0]), fminf(tl[1], th[1]), fminf(tl[2], th[2]));
         const float tf = fmin3f(fmaxf(tl[0], th[0]), fmaxf(tl[1], th[1]), fmaxf(tl[2], th[2]));
