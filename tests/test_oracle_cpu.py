@@ -163,6 +163,7 @@ def test_estimators_unbiased_3d(oracle, combo):
     _strict_z(*zs)
 
 
+@pytest.mark.parametrize("bie", [0, 2])
 def test_backward_control_variate_oracle(oracle, bie):
     """Backward estimator with a per-element control variate on the unknown boundary function:
     with cv = 0 it is the plain estimator path for path; with any cv its mean agrees with the plain
