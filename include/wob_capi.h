@@ -399,7 +399,10 @@ int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters
  * expansion wherever the cluster's radius is below theta times its distance from every target of
  * a warp (and beyond the triangles' near radii); theta = 0 sums every triangle. theta = 0.3 adds
  * about 2e-4 (relative to the largest value) to the centroid rule's own error. 3D scenes.
- * wob_scene_clone: an independent copy of a scene (geometry, records, tables, volume cache).
+ * wob_scene_clone: an independent copy of a scene (geometry, records, tables, volume cache): the
+ * element records are copied, the device buffers that no entry point writes in place (BVH,
+ * intersection records, sampling tables, volume cache, line grid) are shared by reference count,
+ * so either scene may be destroyed first and a later change to one leaves the other as it was.
  * wob_scene_add_boundary_offsets: adds delta_j to the vertex values of stored element j (delta on
  * the device when delta_on_device != 0, else on the host) and rebuilds the |g| sampling tables;
  * synchronises the stream. The plain forward estimator on such a clone, plus S sigma~ from

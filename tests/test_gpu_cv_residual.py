@@ -8,8 +8,9 @@
 - the control-variate tables (wob_cv_residual_data, wob_cv_potential) against their float64
   restatement (oracle/cv_tables.py, the same near/far split) and, for the potential, against the
   closed form at every pair;
-- the residual scene (wob_scene_clone + wob_scene_add_boundary_offsets) walks bit-identically to
-  the oracle on its stored arrays;
+- the residual scene (wob_scene_clone + wob_scene_add_boundary_offsets, offsets from the device
+  or the host) walks bit-identically to the oracle on its stored arrays, leaves its source as it
+  was, and outlives it (the shared device buffers are reference counted);
 - end to end on the exterior Neumann problem: the trained control variate lowers the per-path
   variance of the forward estimator by more than 5x, and its estimate agrees with the plain
   estimator's.
@@ -92,6 +93,8 @@ def test_device_training_is_deterministic_and_learns(engine, cuda):
         torch.cuda.synchronize()
         h = hist.cpu().numpy()
         assert np.all(np.isfinite(h))
+        # the update's last block advances the step counter: every step wrote its own loss slot
+        assert np.all(h > 0), np.flatnonzero(h <= 0)[:10]
         assert h[-20:].mean() < 0.5 * h[:5].mean(), (h[:5], h[-20:])
         params.append(mlp.params()[0])
         mlp.close()
@@ -172,27 +175,40 @@ def test_cv_tables_match_float64(engine, cuda, theta):
 
 
 def test_residual_scene_walks_match_oracle(engine, oracle, cuda):
+    """Clones with offsets given on the device and on the host walk bit-identically to the oracle on
+    the offset arrays; the source keeps its own data, and the clones (which share the source's BVH
+    and tables by reference count) keep working after the source is destroyed."""
     torch = cuda
     case, scene = _ext_neumann_scene(engine)
     rng = np.random.default_rng(4)
     delta = (rng.standard_normal(scene.n_elems) * 0.05).astype(np.float32)
-    rscene = scene.clone_with_offsets(torch.from_numpy(delta).cuda())
+    v0, n0, b0, t0, a0 = scene.stored_arrays()
+    clones = [scene.clone_with_offsets(torch.from_numpy(delta).cuda()), scene.clone_with_offsets(delta)]
     p = engine.EstimatorParams(bie_model=0, domain=1, estimator=1, problem=1, path_length=4, num_sample_paths=64,
                                seed=12)
     pts = np.array([[1.8, 0.1, 0.0], [0.0, -1.9, 0.3], [1.2, 1.2, 0.2], [0.3, 0.2, 1.7]], np.float32)
     d = torch.from_numpy(pts).cuda()
-    vals = torch.zeros(len(pts), 64, 4, device="cuda")
-    rscene.debug_domain_paths(p, d, len(pts), vals)
-    torch.cuda.synchronize()
-    assert rscene.poll_error() == 0
-    v, n, b, t, a = rscene.stored_arrays()
-    v0, _, b0, _, _ = scene.stored_arrays()
-    assert np.array_equal(v, v0) and np.array_equal(b, (b0 + delta[:, None]).astype(np.float32))
-    _, _, _, ref = oracle.solve_domain(oracle.Elements(v, n, b, t, a), p, pts, per_path=True, accel=True)
-    got = vals.cpu().numpy()
-    assert np.array_equal(got, ref), np.abs(got - ref).max()
-    rscene.close()
+
+    def walk(sc):
+        vals = torch.zeros(len(pts), 64, 4, device="cuda")
+        sc.debug_domain_paths(p, d, len(pts), vals)
+        torch.cuda.synchronize()
+        assert sc.poll_error() == 0
+        return vals.cpu().numpy()
+
+    def oracle_paths(b):
+        return oracle.solve_domain(oracle.Elements(v0, n0, b, t0, a0), p, pts, per_path=True, accel=True)[3]
+
+    src = walk(scene)
     scene.close()
+    assert np.array_equal(src, oracle_paths(b0))
+    ref = oracle_paths((b0 + delta[:, None]).astype(np.float32))
+    for rscene in clones:
+        v, n, b, t, a = rscene.stored_arrays()
+        assert np.array_equal(v, v0) and np.array_equal(b, (b0 + delta[:, None]).astype(np.float32))
+        got = walk(rscene)
+        assert np.array_equal(got, ref), np.abs(got - ref).max()
+        rscene.close()
 
 
 def test_trained_residual_control_variate_gains(engine, cuda):

@@ -49,15 +49,29 @@ template <class F> int guarded(F &&body) {
 }
 
 // A device allocation freed with the scene.
+// A device allocation. Owned alone (release frees it) until share() hands it to a second scene;
+// from then on a reference count frees it with its last holder.
 struct DevBuf {
     void *ptr = nullptr;
     size_t bytes = 0;
+    std::shared_ptr<void> shared;  // set once the allocation is shared
     void release() {
-        if (ptr) cudaFree(ptr);
+        if (shared) shared.reset();
+        else if (ptr) cudaFree(ptr);
         ptr = nullptr;
         bytes = 0;
     }
 };
+
+// dst holds src's allocation too (for buffers that no entry point writes after the scene is built).
+void share(DevBuf &dst, DevBuf &src) {
+    dst.release();
+    if (!src.ptr) return;
+    if (!src.shared) src.shared = std::shared_ptr<void>(src.ptr, [](void *p) { cudaFree(p); });
+    dst.ptr = src.ptr;
+    dst.bytes = src.bytes;
+    dst.shared = src.shared;
+}
 
 cudaError_t upload(DevBuf &b, const void *src, size_t bytes) {
     b.release();
@@ -919,7 +933,30 @@ int scene_clone_impl(wob_scene src, wob_scene *out) {
     std::unique_ptr<wob_scene_s> owner(new wob_scene_s());
     wob_scene_s *s = owner.get();
     s->device = src->device;
-    s->host = src->host;
+    // host copy: what wob_scene_add_boundary_offsets and a further clone read (the element records,
+    // areas, storage order, |g| tables and scalars); the BVH, intersection records, area tables and
+    // line grid stay on the device only, shared with the source
+    const wobgb::HostScene &h0 = src->host;
+    wobgb::HostScene &h = s->host;
+    h.dim = h0.dim;
+    h.n = h0.n;
+    h.order = h0.order;
+    h.elems = h0.elems;
+    h.elem_aux = h0.elem_aux;
+    h.alpha_const = h0.alpha_const;
+    h.alpha_value = h0.alpha_value;
+    h.bv_cdf = h0.bv_cdf;
+    h.bv_guide = h0.bv_guide;
+    h.total_area = h0.total_area;
+    h.total_bv = h0.total_bv;
+    h.bv_valid = h0.bv_valid;
+    h.n_nodes = h0.n_nodes;
+    h.depth = h0.depth;
+    h.line_grid.K = h0.line_grid.K;
+    h.line_grid.M = h0.line_grid.M;
+    h.line_grid.cx = h0.line_grid.cx;
+    h.line_grid.cy = h0.line_grid.cy;
+    h.line_grid.far = h0.line_grid.far;
     s->has_volume = src->has_volume;
     s->area_G = src->area_G;
     s->bv_G = src->bv_G;
@@ -928,18 +965,19 @@ int scene_clone_impl(wob_scene src, wob_scene *out) {
     s->vol_G = src->vol_G;
     s->vol_size = src->vol_size;
     s->all_dirichlet = src->all_dirichlet;
-    cudaError_t e = cudaSuccess;
-    const std::pair<DevBuf *, const DevBuf *> bufs[] = {
-        {&s->elems, &src->elems}, {&s->elem_aux, &src->elem_aux}, {&s->isect, &src->isect}, {&s->nodes, &src->nodes},
-        {&s->area_cdf, &src->area_cdf}, {&s->area_guide, &src->area_guide}, {&s->bv_cdf, &src->bv_cdf},
-        {&s->bv_guide, &src->bv_guide}, {&s->vol_values, &src->vol_values}, {&s->vol_cdf, &src->vol_cdf},
-        {&s->vol_guide, &src->vol_guide}, {&s->lg_bins, &src->lg_bins}, {&s->lg_off, &src->lg_off},
-        {&s->lg_ent, &src->lg_ent}};
-    for (const auto &b : bufs)
-        if ((e = clone_buf(*b.first, *b.second)) != cudaSuccess) {
-            s->release_all();
-            return fail_cuda(e, "copying the scene");
-        }
+    // shared: buffers that no entry point writes in place (a later upload to either scene, such as
+    // the |g| tables wob_scene_add_boundary_offsets rebuilds, replaces that scene's reference
+    // only); copied: the element records, which wob_scene_add_boundary_offsets updates in place
+    for (auto b : {&wob_scene_s::elem_aux, &wob_scene_s::isect, &wob_scene_s::nodes, &wob_scene_s::area_cdf,
+                   &wob_scene_s::area_guide, &wob_scene_s::bv_cdf, &wob_scene_s::bv_guide, &wob_scene_s::vol_values,
+                   &wob_scene_s::vol_cdf, &wob_scene_s::vol_guide, &wob_scene_s::lg_bins, &wob_scene_s::lg_off,
+                   &wob_scene_s::lg_ent})
+        share(s->*b, src->*b);
+    cudaError_t e = clone_buf(s->elems, src->elems);
+    if (e != cudaSuccess) {
+        s->release_all();
+        return fail_cuda(e, "copying the scene");
+    }
     const uint32_t zero = 0;
     if ((e = upload(s->err, &zero, 4)) != cudaSuccess) {
         s->release_all();
@@ -972,13 +1010,25 @@ int scene_add_boundary_offsets_impl(wob_scene s, const float *delta, uint32_t n,
     const int first = h.dim == 2 ? 6 : 12;
     for (uint32_t i = 0; i < n; i++)
         for (int k = 0; k < h.dim; k++) h.elems[(size_t)i * EF + first + k] = h.elems[(size_t)i * EF + first + k] + d[i];
+    // the device records get the same adds (offsets read from the caller's device buffer, or from
+    // a scratch copy of the host array)
+    DevBuf scratch;
+    const float *dd = delta;
+    if (!on_device) {
+        if ((e = upload(scratch, d.data(), (size_t)n * 4)) != cudaSuccess) return fail_cuda(e, "uploading the offsets");
+        dd = (const float *)scratch.ptr;
+    }
+    e = wobgb::launch_add_boundary_offsets((float *)s->elems.ptr, dd, n, (uint32_t)EF, (uint32_t)first,
+                                           (uint32_t)h.dim, st);
     wobgb::rebuild_bv_tables(h);
     s->bv_G = (uint32_t)(h.bv_guide.size() / 4);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess ||
-        (e = cudaMemcpy(s->elems.ptr, h.elems.data(), h.elems.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+    if (e != cudaSuccess || (e = cudaStreamSynchronize(st)) != cudaSuccess ||
         (e = upload(s->bv_cdf, h.bv_cdf.data(), h.bv_cdf.size() * 4)) != cudaSuccess ||
-        (e = upload(s->bv_guide, h.bv_guide.data(), h.bv_guide.size() * 4)) != cudaSuccess)
-        return fail_cuda(e, "uploading the new boundary values");
+        (e = upload(s->bv_guide, h.bv_guide.data(), h.bv_guide.size() * 4)) != cudaSuccess) {
+        scratch.release();
+        return fail_cuda(e, "updating the boundary values");
+    }
+    scratch.release();
     return WOB_OK;
 }
 

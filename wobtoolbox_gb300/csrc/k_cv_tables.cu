@@ -411,7 +411,25 @@ __global__ void element_frames_kernel(SceneView<D> s, float *__restrict__ out) {
     }
 }
 
+// Record i's vertex boundary values (record floats [first, first + dim)) plus delta[i]: the same
+// single-precision add as the host copy's update, so the two copies stay identical.
+__global__ void add_boundary_offsets_kernel(float *__restrict__ elems, const float *__restrict__ delta, uint32_t n,
+                                            uint32_t record_floats, uint32_t first, uint32_t dim) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = delta[i];
+    float *r = elems + (size_t)i * record_floats + first;
+    for (uint32_t k = 0; k < dim; k++) r[k] = r[k] + d;
+}
+
 }  // namespace
+
+cudaError_t launch_add_boundary_offsets(float *elems, const float *delta, uint32_t n, uint32_t record_floats,
+                                        uint32_t first, uint32_t dim, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    add_boundary_offsets_kernel<<<(n + 255) / 256, 256, 0, stream>>>(elems, delta, n, record_floats, first, dim);
+    return cudaGetLastError();
+}
 
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream) {
     element_frames_kernel<D><<<(s.n_elems + 255) / 256, 256, 0, stream>>>(s, out);

@@ -68,6 +68,9 @@ cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const 
                                 const float *sigma, const float *pts, uint32_t n_points, uint32_t *scratch,
                                 float *out, cudaStream_t stream);
 template <int D> cudaError_t launch_element_frames(const SceneView<D> &s, float *out, cudaStream_t stream);
+// elems[i * record_floats + first + k] += delta[i] for k < dim (device copy of the element records).
+cudaError_t launch_add_boundary_offsets(float *elems, const float *delta, uint32_t n, uint32_t record_floats,
+                                        uint32_t first, uint32_t dim, cudaStream_t stream);
 // Random-gather ceiling of the uniform-sampling walk (k_probe.cu): samples per second of guide +
 // 64-byte record gathers over tables of the given sizes, on the current device.
 cudaError_t measure_gather_peak(uint32_t n_rec, uint32_t n_guide, uint32_t iters, int sm_count, double *samples_per_s,

@@ -288,7 +288,7 @@ struct wob_mlp_s {
     // training-loop state (wob_mlp_train)
     uint32_t train_cap = 0, partial_blocks = 0;
     float *xb = nullptr, *tb = nullptr, *sched = nullptr, *partial = nullptr, *partial_loss = nullptr;
-    uint32_t *step = nullptr;
+    uint32_t *step = nullptr;   // [2]: step counter, the fused update's count of finished blocks
     uint32_t *image = nullptr;  // packed BF16 weights of the fused step (zero padding)
     uint32_t *err = nullptr;    // fused step's error word
     std::mutex mu;
@@ -312,7 +312,7 @@ struct wob_mlp_s {
         cudaError_t e = ensure(batch);
         if (e != cudaSuccess) return e;
         if (!sched && (e = cudaMalloc(&sched, 16)) != cudaSuccess) return e;
-        if (!step && (e = cudaMalloc(&step, 4)) != cudaSuccess) return e;
+        if (!step && (e = cudaMalloc(&step, 8)) != cudaSuccess) return e;
         if (batch <= train_cap) return cudaSuccess;
         for (float **p : {&xb, &tb}) {
             if (*p) cudaFree(*p);
@@ -328,7 +328,7 @@ struct wob_mlp_s {
     bool fused_ok() const { return hidden == 4 && n_freq == 32 && out_dim <= 64; }
     cudaError_t ensure_fused(uint32_t batch) {
         cudaError_t e;
-        if (!step && (e = cudaMalloc(&step, 4)) != cudaSuccess) return e;
+        if (!step && (e = cudaMalloc(&step, 8)) != cudaSuccess) return e;
         if (!image) {
             const size_t bytes = wobgb::fused_train_image_words() * 4;
             if ((e = cudaMalloc(&image, bytes)) != cudaSuccess || (e = cudaMemset(image, 0, bytes)) != cudaSuccess)
@@ -567,7 +567,7 @@ int wob_mlp_gradient_fused(wob_mlp m, const float *inputs, const float *targets,
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = m->ensure_fused(n);
     if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
-    if ((e = cudaMemsetAsync(m->step, 0, 4, st)) != cudaSuccess) return mfail_cuda(e, "MLP step counter");
+    if ((e = cudaMemsetAsync(m->step, 0, 8, st)) != cudaSuccess) return mfail_cuda(e, "MLP step counter");
     wobgb::FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, n, m->n_params, 0u, 0ull, m->step,
                             m->partial, m->partial_loss, m->image, m->err};
     e = wobgb::launch_fused_gradient(a, grad, loss, st);
@@ -600,7 +600,7 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
     };
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaMemsetAsync(m->step, 0, 4, user)) != cudaSuccess || (e = cudaEventRecord(ev, user)) != cudaSuccess ||
+        (e = cudaMemsetAsync(m->step, 0, 8, user)) != cudaSuccess || (e = cudaEventRecord(ev, user)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(cs, ev, 0)) != cudaSuccess) {
         cleanup();
         return mfail_cuda(e, "preparing the training stream");

@@ -15,7 +15,7 @@ struct FusedTrainArgs {
     uint32_t n, out_dim, batch, n_params;
     uint32_t gather;       // 1: rows drawn by Philox from the n rows; 0: row r of the batch is row r
     uint64_t seed;
-    uint32_t *step;        // device step counter (batch draws and the learning-rate schedule)
+    uint32_t *step;        // [2]: step counter (batch draws, learning-rate schedule); blocks done with it
     float *partial;        // [blocks][n_params]: each block's gradient
     float *partial_loss;   // [blocks]
     const uint32_t *image; // packed BF16 weights, both operand layouts (fused_train_image_words words)
@@ -32,7 +32,8 @@ cudaError_t launch_pack_weights(const float *params, uint32_t n_params, uint32_t
 uint32_t fused_train_blocks(uint32_t batch);
 cudaError_t prepare_fused_train();
 // One step: fused forward/backward, block-ordered gradient sum + Adam (cosine learning rate from
-// lr over `steps`; bias corrections at step adam_base + s + 1), step counter + 1.
+// lr over `steps`; bias corrections at step adam_base + s + 1), step counter + 1 (by the update's
+// last block; step[1] must be zero before the first step).
 cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, float *adam_m, float *adam_v,
                                     uint32_t steps, float lr, uint32_t adam_base, float *loss_hist,
                                     cudaStream_t stream);
