@@ -652,7 +652,8 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
             return mfail_cuda(e, "reading the training error word");
         if (bits) {
             cudaMemset(m->err, 0, 4);
-            return mfail(WOB_ERR_DEVICE_LIMIT, "a training block's weight staging did not complete within its wait bound");
+            return mfail(WOB_ERR_DEVICE_LIMIT, (bits & 2u) ? "a training block's tensor-core product did not complete within its wait bound"
+                                                          : "a training block's weight staging did not complete within its wait bound");
         }
     }
     return WOB_OK;

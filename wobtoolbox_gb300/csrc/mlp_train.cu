@@ -1,29 +1,35 @@
 // Fused training step of the Fourier-feature MLP (mlp.cu's network with 4 hidden layers): one
-// kernel runs the batch gather, the forward pass and the backward pass of 64 rows per block (16
-// warps, each a 16 x 16 share of every 64 x 64 product) with every weight and activation in shared
-// memory and writes the block's gradient; a second kernel sums the blocks' gradients in a fixed
-// order (so a step is deterministic), applies Adam, writes the updated weights as a packed BF16
-// image in both operand layouts, and its last block advances the step counter. wob_mlp_train
-// replays the two as a CUDA graph. Each block of the next step
-// stages that image (83 KB) into shared memory with one TMA bulk copy (cp.async.bulk, completion
+// kernel runs the batch gather, the forward pass and the backward pass of 64 rows per block with
+// every weight and activation in shared memory and writes the block's gradient; a second kernel
+// sums the blocks' gradients in a fixed order (so a step is deterministic), applies Adam, writes
+// the updated weights as a packed BF16 image in both operand layouts, and its last block advances
+// the step counter. wob_mlp_train replays the two as a CUDA graph. Each block of the next step
+// stages that image (74 KB) into shared memory with one TMA bulk copy (cp.async.bulk, completion
 // on an mbarrier, the wait bounded), instead of every block reading and converting the FP32
 // parameters itself.
 //
 // Network and parameter layout as in mlp.cu: phi = [sin, cos](2 pi B v) (32 frequencies of the
 // 6 inputs), 4 hidden layers 64 -> 64 with SiLU, a linear 64 -> out_dim head; FP32 parameters,
-// for each layer W [out][in] row-major then b [out]. Every product runs on the BF16 tensor cores
-// (mma.sync m16n8k16, FP32 accumulation) with operands rounded to BF16 in shared memory, as in
-// mlp.cu; pre-activations are kept as BF16 for the SiLU derivative, bias gradients are summed in
-// FP32 from the FP32 products. No atomics: every sum has a fixed order, so training is
-// deterministic.
+// for each layer W [out][in] row-major then b [out]. pre-activations are kept as BF16 for the SiLU
+// derivative, bias gradients are summed in FP32 from the FP32 products. No atomics: every sum has
+// a fixed order, so training is deterministic.
 //
-// Shared-memory operands are 32-bit words holding two BF16 values adjacent along the reduction
-// index (the m16n8k16 fragment layout), rows padded to 36 words so that the 8 rows of 16 bytes an
-// ldmatrix / stmatrix phase moves fall in 32 distinct banks. For C[m][n] = sum_k A[m][k] B[k][n] the A operand is
-// stored [m][k/2] and the B operand [n][k/2]:
+// Products: every 64 x 64 x 64 product C[m][n] = sum_k A[m][k] B[n][k] is four tcgen05.mma
+// (kind::f16, BF16 operands from shared memory, M = 64, N = 64, K = 16 each) issued by one thread,
+// the FP32 accumulator in tensor memory (TMEM), completion signalled on an mbarrier by
+// tcgen05.commit. With M = 64 the accumulator's rows 16 q .. 16 q + 15 sit in TMEM lanes 32 q ..
+// 32 q + 15, the lane quarter that warps w with w % 4 = q may read: warp w reads rows
+// [16 (w % 4), +16) x columns [16 (w / 4), +16) with tcgen05.ld.16x256b (the mma.sync m16n8
+// accumulator layout: lane l holds rows l / 4 and l / 4 + 8, columns 2 (l % 4) and + 1 of each
+// 8-column tile) and runs the epilogue on them. Both operands are K-major:
 //   forward  Z = A W^T:     A = activation [row][in],   B = W   [out][in]
 //   weights  dW = dZ^T A:   A = dZ^T [out][row],        B = A^T [in][row]
 //   inputs   dA = dZ W:     A = dZ   [row][out],        B = W^T [in][out]
+// each stored in the no-swizzle core-matrix layout (cm_index): 8 x 8 BF16 core matrices of 128
+// contiguous bytes, K-adjacent ones 128 bytes apart (the descriptor's leading byte offset), 8-row
+// groups 1024 bytes apart (its stride byte offset). Epilogues write those layouts with stmatrix
+// (.trans for the transposed copies): the 8 rows of a core matrix are one 128-byte line, so a
+// phase touches 32 distinct banks.
 #include "../../include/wob_capi.h"
 
 #include "device_common.cuh"
@@ -38,121 +44,127 @@ namespace {
 
 constexpr int kTM = 64;          // rows per block
 constexpr int kW = 64;           // layer width
-constexpr int kLd = 36;          // words per shared-memory row (32 pairs + 4 padding)
-constexpr int kMat = kW * kLd;   // words per 64 x 64 operand
+constexpr int kMatHalves = kW * kW;   // BF16 values per 64 x 64 operand
+constexpr int kMat = kMatHalves / 2;  // 32-bit words per operand
 constexpr int kHidden = 4;
 constexpr int kLayers = kHidden + 1;
 constexpr int kIn = 6;
-// kColSplit x 4 warps: warp w computes rows [16 (w & 3), +16) x columns [kCols (w >> 2), +kCols)
-// of every 64 x 64 product; the warps of a row block meet at a named barrier where one reads what
-// another wrote
-constexpr int kColSplit = 4;
+// 16 warps: warp w handles rows [16 (w & 3), +16) x columns [16 (w >> 2), +16) of every product's
+// accumulator
 constexpr int kRowBlocks = kTM / 16;
+constexpr int kColSplit = 4;
 constexpr int kWarps = kRowBlocks * kColSplit;
 constexpr int kThreads = kWarps * 32;
 constexpr int kCols = kW / kColSplit;  // columns per warp
 constexpr int kNT = kCols / 8;         // 8-column tiles per warp
-static_assert(kNT % 2 == 0, "fragments move two tiles at a time");
+static_assert(kNT == 2, "the TMEM loads and the tile stores move two 8-column tiles");
 constexpr int kLayerParams = kW * kW + kW;
+// TMEM: columns [0, 64) take forward and input-gradient products, [64, 128) and [128, 192) the
+// weight gradients of odd and even layers (read out while the next layer's products run)
+constexpr uint32_t kTmemCols = 256;
 
-// operands: Wf (5), Wb (4), act (2: a layer reads one and writes the other), actT (5), Zs (4), dZ, dZT
-constexpr size_t kSmemWords = (size_t)(kLayers + kHidden + 2 + kLayers + kHidden + 2) * kMat;
+// operands: Wf (5), Wb (4), act, actT (5), Zs (4), dZ, dZT (2: layer l's in dZT + (l & 1) kMat, kept
+// until its weight-gradient product has been read out)
+constexpr size_t kSmemWords = (size_t)(kLayers + kHidden + 1 + kLayers + kHidden + 3) * kMat;
 constexpr size_t kSmemFloats = kLayers * kW + kLayers * kRowBlocks * kW + kTM * kIn + kTM * kW + kWarps;
 
+// BF16 index of element (r, k) of a 64 x 64 K-major operand in the no-swizzle core-matrix layout.
+__host__ __device__ constexpr uint32_t cm_index(uint32_t r, uint32_t k) {
+    return (r >> 3) * 512u + (k >> 3) * 64u + (r & 7u) * 8u + (k & 7u);
+}
+
+// Two floats rounded to BF16 in one word, lo in the low half (one cvt.rn.bf16x2.f32).
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
-    const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
-    return (uint32_t)__bfloat16_as_ushort(l) | ((uint32_t)__bfloat16_as_ushort(h) << 16);
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
 }
 __device__ __forceinline__ float lo_of(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float hi_of(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Four 8 x 8 BF16 matrices from shared memory in mma fragment layout (lane l gets row l / 4, word
-// l % 4 of each); lane l gives the address of row l % 8 of matrix l / 8 (16-byte aligned rows).
-__device__ __forceinline__ void ldsm_x4(uint32_t r[4], const uint32_t *row) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_u32(row))
-                 : "memory");
+// ---- tcgen05 helpers
+// Shared-memory descriptor of a no-swizzle K-major operand starting at byte address addr:
+// start >> 4 (bits 0-13), leading byte offset 128 >> 4 (bits 16-29), stride byte offset
+// 1024 >> 4 (bits 32-45), descriptor version 1 (bits 46-47), base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t operand_desc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           (1ull << 46);
 }
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9,
+// 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kW >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
 
-// acc[j][.] += sum_k A[m0 + .][k] B[k][n0 + 8 j + .] for one warp's 16 rows at m0 and kCols
-// columns at n0; K = 64. Fragment c[0..3] of tile j: rows m0 + gid (c0, c1) and m0 + gid + 8 (c2, c3),
-// columns n0 + 8 j + 2 tig and n0 + 8 j + 2 tig + 1. The A fragment of a k step is one ldmatrix.x4
-// (rows m0..m0+7 and m0+8..m0+15, k words 0-3 and 4-7), the B fragments of two tiles another.
-__device__ __forceinline__ void warp_gemm(float acc[kNT][4], const uint32_t *A, const uint32_t *B, int m0, int n0,
-                                          int lane) {
-    const int r = lane & 7, mi = lane >> 3;
-    const uint32_t *a_row = A + (m0 + 8 * (mi & 1) + r) * kLd + 4 * (mi >> 1);
-    const uint32_t *b_row = B + (n0 + 8 * (mi >> 1) + r) * kLd + 4 * (mi & 1);
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes made visible to the tensor cores' reads
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// D[tmem] (=|+=) A B^T over K = 64: four K = 16 steps, 256 bytes apart in both operands.
+__device__ __forceinline__ void issue_product(uint32_t d_tmem, const uint32_t *A, const uint32_t *B) {
+    const uint32_t a = smem_u32(A), b = smem_u32(B);
 #pragma unroll
     for (int kk = 0; kk < 4; kk++) {
-        uint32_t a[4];
-        ldsm_x4(a, a_row + kk * 8);
-#pragma unroll
-        for (int j = 0; j < kNT; j += 2) {
-            uint32_t b[4];
-            ldsm_x4(b, b_row + j * 8 * kLd + kk * 8);
-            mma16816(acc[j], a, b);
-            mma16816(acc[j + 1], a, b + 2);
-        }
+        const uint64_t ad = operand_desc(a + kk * 256u), bd = operand_desc(b + kk * 256u);
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+            "l"(ad), "l"(bd), "r"(kIdesc), "r"(kk));
     }
 }
-
-// Stores a warp's 16 x kCols tile of packed BF16 pairs p[j][h] (fragment layout: row m0 + gid + 8 h,
-// columns n0 + 8 j + 2 tig, +1) into M as [row][col / 2] words, or with kTrans as [col][row / 2]
-// words (the transposed operand), two tiles per stmatrix.x4.
-template <bool kTrans>
-__device__ __forceinline__ void store_tile(uint32_t *M, const uint32_t p[kNT][2], int m0, int n0, int lane) {
-    const int r = lane & 7, mi = lane >> 3;
-#pragma unroll
-    for (int j = 0; j < kNT; j += 2) {
-        const int row = m0 + 8 * (mi & 1), col = n0 + 8 * (j + (mi >> 1));
-        const uint32_t addr = smem_u32(kTrans ? M + (col + r) * kLd + row / 2 : M + (row + r) * kLd + col / 2);
-        if (kTrans)
-            asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(addr),
-                         "r"(p[j][0]), "r"(p[j][1]), "r"(p[j + 1][0]), "r"(p[j + 1][1])
-                         : "memory");
-        else
-            asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(p[j][0]),
-                         "r"(p[j][1]), "r"(p[j + 1][0]), "r"(p[j + 1][1])
-                         : "memory");
-    }
+// Arrives on the mbarrier once every tcgen05.mma this thread issued before has completed.
+__device__ __forceinline__ void commit_to(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
-
-__device__ __forceinline__ void zero_acc(float acc[kNT][4]) {
+// Rows [16 q, +16) x 16 columns of a product from TMEM (taddr: lane 32 q, first column) into
+// acc[j][.] in the m16n8 accumulator layout of 8-column tile j.
+__device__ __forceinline__ void load_acc(float acc[kNT][4], uint32_t taddr) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.16x256b.x2.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < kNT; j++)
 #pragma unroll
-        for (int r = 0; r < 4; r++) acc[j][r] = 0.0f;
+        for (int q = 0; q < 4; q++) acc[j][q] = __uint_as_float(r[4 * j + q]);
 }
 
-// The warps of row block rb wait for each other; barrier 0 is __syncthreads'.
-__device__ __forceinline__ void row_block_sync(int rb) {
-    asm volatile("bar.sync %0, %1;" ::"r"(1 + rb), "r"(kColSplit * 32) : "memory");
-}
-
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+// SiLU and its derivative with the fast exponential and division intrinsics (the values are rounded
+// to BF16 or multiply BF16-rounded gradients, so their few-ulp error does not show). For z below
+// about -88, exp(-z) overflows and __fdividef returns 0 for the huge or infinite denominator, the
+// limit of both functions.
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float silu_d(float z) {
-    const float s = 1.0f / (1.0f + expf(-z));
+    const float s = __fdividef(1.0f, 1.0f + __expf(-z));
     return s * (1.0f + z * (1.0f - s));
 }
 
-// BF16 value at (row, col) of an operand kept transposed, [col][row / 2] words.
-__device__ __forceinline__ void store_t(uint32_t *M, int row, int col, float v) {
-    reinterpret_cast<__nv_bfloat16 *>(M)[col * kLd * 2 + row] = __float2bfloat16_rn(v);
+// Stores a warp's 16 x 16 tile of packed BF16 pairs p[j][h] (accumulator layout: row m0 + gid +
+// 8 h, columns n0 + 8 j + 2 tig, +1) into operand M at (row, col), or with kTrans at (col, row)
+// (the transposed operand): one stmatrix.x4 of four 8 x 8 matrices, each one core matrix.
+template <bool kTrans>
+__device__ __forceinline__ void store_tile(uint32_t *M, const uint32_t p[kNT][2], int m0, int n0, int lane) {
+    const int r = lane & 7, mi = lane >> 3;
+    const int row = m0 + 8 * (mi & 1), col = n0 + 8 * (mi >> 1);
+    const uint32_t idx = kTrans ? cm_index(col + r, row) : cm_index(row + r, col);
+    const uint32_t addr = smem_u32(reinterpret_cast<__nv_bfloat16 *>(M) + idx);
+    if (kTrans)
+        asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(p[0][0]),
+                     "r"(p[0][1]), "r"(p[1][0]), "r"(p[1][1])
+                     : "memory");
+    else
+        asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(p[0][0]),
+                     "r"(p[0][1]), "r"(p[1][0]), "r"(p[1][1])
+                     : "memory");
 }
 
-// Column sums over the warp's 16 rows of the FP32 values in acc (fragment layout of tile j),
+// BF16 value at (r, k) of an operand.
+__device__ __forceinline__ void store_bf16(uint32_t *M, int r, int k, float v) {
+    reinterpret_cast<__nv_bfloat16 *>(M)[cm_index(r, k)] = __float2bfloat16_rn(v);
+}
+
+// Column sums over the warp's 16 rows of the FP32 values in acc (accumulator layout of tile j),
 // stored to the row block's row dst[n0 + 8 j + 2 tig (+1)] in shared memory (the row blocks' rows
 // are added in row-block order later, so the sum does not depend on scheduling).
 __device__ __forceinline__ void store_col_sums(float acc[kNT][4], float *dst, int n0, int lane, int tig) {
@@ -174,9 +186,9 @@ __device__ __forceinline__ void store_col_sums(float acc[kNT][4], float *dst, in
 constexpr size_t kImageWords = (size_t)(kLayers + kHidden) * kMat;  // Wf then Wb, as in shared memory
 constexpr uint32_t kImageBytes = (uint32_t)(kImageWords * 4);
 static_assert(kImageBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
-// try_wait polls before a block gives up on its staging copy (each poll may suspend the thread
-// for a while; the copy normally lands within microseconds).
-constexpr uint32_t kStageWaitPolls = 1u << 22;
+// try_wait polls before a block gives up on its staging copy or a product (each poll may suspend
+// the thread for a while; either normally completes within microseconds).
+constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t done;
@@ -188,21 +200,28 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return done != 0;
 }
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kStageWaitPolls; i++)
+    for (uint32_t i = 0; i < kWaitPolls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 
+// Error bits of FusedTrainArgs::err.
+constexpr uint32_t kErrStage = 1u;    // the weight image's bulk copy did not land within the bound
+constexpr uint32_t kErrProduct = 2u;  // a product's completion did not arrive within the bound
+
 __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrainArgs g) {
     extern __shared__ __align__(128) uint32_t smem[];
-    __shared__ __align__(8) uint64_t stage_bar;
+    // mbarriers: the weight image's staging, forward / input-gradient products, weight-gradient
+    // products of even and odd layers (one phase outstanding at a time on each), the teardown drain
+    __shared__ __align__(8) uint64_t stage_bar, mma_bar, wgrad_bar[2], drain_bar;
+    __shared__ uint32_t tmem_slot;
     uint32_t *Wf = smem;                      // layer l: [out][in]
     uint32_t *Wb = Wf + kLayers * kMat;       // layer l >= 1: [in][out] at index l - 1
-    uint32_t *act = Wb + kHidden * kMat;      // two buffers [row][in]: layer l reads act + (l & 1) kMat
-    uint32_t *actT = act + 2 * kMat;          // layer l's input: [in][row]
+    uint32_t *act = Wb + kHidden * kMat;      // [row][in] of the layer being evaluated
+    uint32_t *actT = act + kMat;              // layer l's input: [in][row]
     uint32_t *Zs = actT + kLayers * kMat;     // hidden layer l's pre-activation: [row][out]
     uint32_t *dZ = Zs + kHidden * kMat;       // [row][out]
-    uint32_t *dZT = dZ + kMat;                // [out][row]
+    uint32_t *dZT = dZ + kMat;                // two buffers [out][row]
     float *bias = reinterpret_cast<float *>(smem + kSmemWords);  // [5][64]
     float *dbias = bias + kLayers * kW;                          // [5][4 row blocks][64]
     float *xin = dbias + kLayers * kRowBlocks * kW;              // [64][6]
@@ -215,16 +234,24 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     const uint32_t step = *g.step;
 
     // weights in both layouts: one bulk copy of the packed image (rows of the head beyond out_dim
-    // and the row padding are zero there); biases by plain loads meanwhile
-    const uint32_t bar = smem_u32(&stage_bar);
+    // are zero there); biases by plain loads meanwhile; TMEM columns for the accumulators
+    const uint32_t bar = smem_u32(&stage_bar), pbar = smem_u32(&mma_bar), dbar = smem_u32(&drain_bar);
+    const uint32_t wbar0 = smem_u32(&wgrad_bar[0]), wbar1 = smem_u32(&wgrad_bar[1]);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        for (uint32_t b : {bar, pbar, wbar0, wbar1, dbar})
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kImageBytes) : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                      ::"r"(smem_u32(Wf)), "l"(g.image), "r"(kImageBytes), "r"(bar)
                      : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     for (int l = 0; l < kLayers; l++) {
         const int fo = l == kHidden ? out_dim : kW;
@@ -245,127 +272,201 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
         for (int k = 0; k < out_dim; k++) tgt[r * kW + k] = ok ? g.targets[(size_t)idx * out_dim + k] : 0.0f;
     }
     if (tid < kWarps) red[tid] = 0.0f;
-    __syncthreads();  // the barrier's initialisation is visible to every thread from here
-    if (!mbar_wait_bounded(bar, 0u)) {
-        // the staging copy did not land: flag it, give it one more bounded wait so that it does not
-        // write into a later block's shared memory, and leave this block's gradient unwritten
-        if (tid == 0) atomicOr(g.err, 1u);
+    tc_fence_before();
+    __syncthreads();  // the barriers' initialisation and the TMEM address are visible from here
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t t_lane = tmem + ((uint32_t)(32 * rb) << 16);  // this warp's lane quarter
+    // parities of the next completions: mma_bar; wgrad_bar[p] in bit p of wphase
+    uint32_t phase = 0, wphase = 0;
+    int w_pending = -1;                      // layer whose weight gradient waits in TMEM to be read out
+    bool ok = true;
+    uint32_t err = 0;
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0u))) {
+        // the staging copy did not land: give it one more bounded wait so that it does not write
+        // into a later block's shared memory, release TMEM and leave this block's gradient unwritten
+        err = kErrStage;
         mbar_wait_bounded(bar, 0u);
-        return;
+        ok = false;
     }
-    // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t
-    for (int idx = tid; idx < kTM * 32; idx += kThreads) {
-        const int r = idx >> 5, f = idx & 31;
-        float t = 0.0f;
+    if (ok) {
+        // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t
+        for (int idx = tid; idx < kTM * 32; idx += kThreads) {
+            const int r = idx >> 5, f = idx & 31;
+            float t = 0.0f;
 #pragma unroll
-        for (int k = 0; k < kIn; k++) t = t + g.freqs[f * kIn + k] * xin[r * kIn + k];
-        float s, c;
-        sincospi_own(2.0f * t, &s, &c);
-        reinterpret_cast<__nv_bfloat16 *>(act)[r * kLd * 2 + f] = __float2bfloat16_rn(s);
-        reinterpret_cast<__nv_bfloat16 *>(act)[r * kLd * 2 + 32 + f] = __float2bfloat16_rn(c);
-        store_t(actT, r, f, s);
-        store_t(actT, r, 32 + f, c);
-    }
-    __syncthreads();
-
-    // ---- forward: a warp reads all 64 columns of its row block's input and writes its kCols
-    // columns of the output buffer; the row block's barrier publishes them before the next layer
-    float acc[kNT][4];
-    for (int l = 0; l < kHidden; l++) {
-        const uint32_t *in = act + (l & 1) * kMat;
-        uint32_t *out = act + ((l + 1) & 1) * kMat;
-        zero_acc(acc);
-        warp_gemm(acc, in, Wf + l * kMat, m0, n0, lane);
-        uint32_t zp[kNT][2], hp[kNT][2];
-#pragma unroll
-        for (int j = 0; j < kNT; j++)
-#pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
-                const int col = n0 + j * 8 + 2 * tig;
-                const float z0 = acc[j][2 * hh] + bias[l * kW + col], z1 = acc[j][2 * hh + 1] + bias[l * kW + col + 1];
-                zp[j][hh] = pack2(z0, z1);
-                hp[j][hh] = pack2(silu_f(z0), silu_f(z1));
-            }
-        store_tile<false>(Zs + l * kMat, zp, m0, n0, lane);
-        store_tile<false>(out, hp, m0, n0, lane);
-        store_tile<true>(actT + (l + 1) * kMat, hp, m0, n0, lane);
-        row_block_sync(rb);
-    }
-    // head: y = act W^T + b; loss sum (y - t)^2 / count; acc becomes dY = 2 (y - t) / count
-    {
-        zero_acc(acc);
-        warp_gemm(acc, act + (kHidden & 1) * kMat, Wf + kHidden * kMat, m0, n0, lane);
-        const float count = (float)g.batch * (float)out_dim;
-        float ls = 0.0f;
-#pragma unroll
-        for (int j = 0; j < kNT; j++)
-#pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
-                const int row = m0 + gid + 8 * hh, col = n0 + j * 8 + 2 * tig;
-                const bool rok = blockIdx.x * kTM + row < g.batch;
-                float d0 = 0.0f, d1 = 0.0f;
-                if (rok && col < out_dim) d0 = acc[j][2 * hh] + bias[kHidden * kW + col] - tgt[row * kW + col];
-                if (rok && col + 1 < out_dim)
-                    d1 = acc[j][2 * hh + 1] + bias[kHidden * kW + col + 1] - tgt[row * kW + col + 1];
-                ls += d0 * d0 + d1 * d1;
-                acc[j][2 * hh] = 2.0f * d0 / count;
-                acc[j][2 * hh + 1] = 2.0f * d1 / count;
-            }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
-        if (lane == 0) red[warp] = ls / count;
-    }
-    // ---- backward: at the top of each iteration acc holds dL/dZ_l for this warp's rows and
-    // columns (FP32)
-    for (int l = kHidden; l >= 0; l--) {
-        store_col_sums(acc, dbias + (l * kRowBlocks + rb) * kW, n0, lane, tig);
-        {
-            uint32_t dp[kNT][2];
-#pragma unroll
-            for (int j = 0; j < kNT; j++)
-#pragma unroll
-                for (int hh = 0; hh < 2; hh++) dp[j][hh] = pack2(acc[j][2 * hh], acc[j][2 * hh + 1]);
-            store_tile<false>(dZ, dp, m0, n0, lane);
-            store_tile<true>(dZT, dp, m0, n0, lane);
+            for (int k = 0; k < kIn; k++) t = t + g.freqs[f * kIn + k] * xin[r * kIn + k];
+            float s, c;
+            sincospi_own(2.0f * t, &s, &c);
+            store_bf16(act, r, f, s);
+            store_bf16(act, r, 32 + f, c);
+            store_bf16(actT, f, r, s);
+            store_bf16(actT, 32 + f, r, c);
         }
+        fence_async_smem();
         __syncthreads();
-        const int fo = l == kHidden ? out_dim : kW;
-        // weight gradient dW[o][i] = sum_r dZ[r][o] act_l[r][i]: warp w takes o in [m0, m0 + 16),
-        // i in [n0, n0 + kCols)
-        if (m0 < fo) {
-            float wacc[kNT][4];
-            zero_acc(wacc);
-            warp_gemm(wacc, dZT, actT + l * kMat, m0, n0, lane);
-            float *dst = g.partial + (size_t)blockIdx.x * g.n_params + (size_t)l * kLayerParams;
+
+        float acc[kNT][4];
+        // ---- forward: Z_l = act W_l^T in TMEM columns [0, 64); ok is block-uniform at the top of
+        // each layer (the __syncthreads_and that ends the previous one)
+        for (int l = 0; l < kHidden && ok; l++) {
+            if (tid == 0) {
+                tc_fence_after();
+                issue_product(tmem, act, Wf + l * kMat);
+                commit_to(pbar);
+            }
+            ok = mbar_wait_bounded(pbar, phase);
+            phase ^= 1u;
+            tc_fence_after();
+            load_acc(acc, t_lane + n0);
+            uint32_t zp[kNT][2], hp[kNT][2];
 #pragma unroll
             for (int j = 0; j < kNT; j++)
 #pragma unroll
                 for (int hh = 0; hh < 2; hh++) {
-                    const int o = m0 + gid + 8 * hh, i = n0 + j * 8 + 2 * tig;
-                    // scalar stores: a block's gradient row starts at block * n_params floats, and
-                    // n_params is odd for an odd head width, so pairs are not 8-byte aligned
-                    if (o < fo) {
-                        dst[o * kW + i] = wacc[j][2 * hh];
-                        dst[o * kW + i + 1] = wacc[j][2 * hh + 1];
+                    const int col = n0 + j * 8 + 2 * tig;
+                    const float z0 = acc[j][2 * hh] + bias[l * kW + col], z1 = acc[j][2 * hh + 1] + bias[l * kW + col + 1];
+                    zp[j][hh] = pack2(z0, z1);
+                    hp[j][hh] = pack2(silu_f(z0), silu_f(z1));
+                }
+            // the product has read act (its completion arrived), so act takes the layer's output
+            store_tile<false>(Zs + l * kMat, zp, m0, n0, lane);
+            store_tile<false>(act, hp, m0, n0, lane);
+            store_tile<true>(actT + (l + 1) * kMat, hp, m0, n0, lane);
+            fence_async_smem();
+            tc_fence_before();
+            ok = __syncthreads_and(ok);
+        }
+        // `run` is the block-wide verdict (a __syncthreads_and), `ok` this thread's own waits since
+        bool run = ok;
+        // head: y = act W^T + b; loss sum (y - t)^2 / count; acc becomes dY = 2 (y - t) / count
+        if (run) {
+            if (tid == 0) {
+                tc_fence_after();
+                issue_product(tmem, act, Wf + kHidden * kMat);
+                commit_to(pbar);
+            }
+            ok = mbar_wait_bounded(pbar, phase);
+            phase ^= 1u;
+            tc_fence_after();
+            load_acc(acc, t_lane + n0);
+            const float count = (float)g.batch * (float)out_dim;
+            float ls = 0.0f;
+#pragma unroll
+            for (int j = 0; j < kNT; j++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int row = m0 + gid + 8 * hh, col = n0 + j * 8 + 2 * tig;
+                    const bool rok = blockIdx.x * kTM + row < g.batch;
+                    float d0 = 0.0f, d1 = 0.0f;
+                    if (rok && col < out_dim) d0 = acc[j][2 * hh] + bias[kHidden * kW + col] - tgt[row * kW + col];
+                    if (rok && col + 1 < out_dim)
+                        d1 = acc[j][2 * hh + 1] + bias[kHidden * kW + col + 1] - tgt[row * kW + col + 1];
+                    ls += d0 * d0 + d1 * d1;
+                    acc[j][2 * hh] = 2.0f * d0 / count;
+                    acc[j][2 * hh + 1] = 2.0f * d1 / count;
+                }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+            if (lane == 0) red[warp] = ls / count;
+        }
+        // ---- backward: at the top of each iteration acc holds dL/dZ_l for this warp's rows and
+        // columns (FP32). dA = dZ W_l goes to TMEM columns [0, 64) and is committed first (the next
+        // layer waits for it); dW_l = dZ^T act_l (dZ^T from buffer l & 1) to columns 64 + 64 (l & 1),
+        // committed on wgrad_bar[l & 1] and read out one iteration later, while the next layer's
+        // products run. Buffer and columns l & 1 are next written by layer l - 2, after that readout
+        // (and the barrier that starts layer l - 1).
+        auto drain_wgrad = [&]() {
+            // weight gradient dW[o][i] of layer w_pending: warp w takes o in [m0, m0 + 16), i in
+            // [n0, n0 + 16)
+            const int lw = w_pending, pw = lw & 1;
+            ok = mbar_wait_bounded(pw ? wbar1 : wbar0, (wphase >> pw) & 1u) && ok;
+            wphase ^= 1u << pw;
+            tc_fence_after();
+            const int fo = lw == kHidden ? out_dim : kW;
+            if (m0 < fo) {
+                float wacc[kNT][4];
+                load_acc(wacc, t_lane + 64u + 64u * (uint32_t)(lw & 1) + n0);
+                float *dst = g.partial + (size_t)blockIdx.x * g.n_params + (size_t)lw * kLayerParams;
+#pragma unroll
+                for (int j = 0; j < kNT; j++)
+#pragma unroll
+                    for (int hh = 0; hh < 2; hh++) {
+                        const int o = m0 + gid + 8 * hh, i = n0 + j * 8 + 2 * tig;
+                        // scalar stores: a block's gradient row starts at block * n_params floats, and
+                        // n_params is odd for an odd head width, so pairs are not 8-byte aligned
+                        if (o < fo) {
+                            dst[o * kW + i] = wacc[j][2 * hh];
+                            dst[o * kW + i + 1] = wacc[j][2 * hh + 1];
+                        }
                     }
+            }
+            w_pending = -1;
+        };
+        for (int l = kHidden; l >= 0 && run; l--) {
+            store_col_sums(acc, dbias + (l * kRowBlocks + rb) * kW, n0, lane, tig);
+            {
+                uint32_t dp[kNT][2];
+#pragma unroll
+                for (int j = 0; j < kNT; j++)
+#pragma unroll
+                    for (int hh = 0; hh < 2; hh++) dp[j][hh] = pack2(acc[j][2 * hh], acc[j][2 * hh + 1]);
+                store_tile<false>(dZ, dp, m0, n0, lane);
+                store_tile<true>(dZT + (l & 1) * kMat, dp, m0, n0, lane);
+            }
+            fence_async_smem();
+            tc_fence_before();
+            run = __syncthreads_and(ok);
+            if (!run) break;
+            if (tid == 0) {
+                tc_fence_after();
+                if (l > 0) {
+                    issue_product(tmem, dZ, Wb + (l - 1) * kMat);
+                    commit_to(pbar);
+                }
+                issue_product(tmem + 64u + 64u * (uint32_t)(l & 1), dZT + (l & 1) * kMat, actT + l * kMat);
+                commit_to((l & 1) ? wbar1 : wbar0);
+            }
+            if (w_pending >= 0) drain_wgrad();  // the previous layer's dW, in the other columns
+            w_pending = l;
+            if (l == 0) break;
+            // dZ_{l-1} = dA silu'(Z_{l-1}) for this warp's rows and columns (dA has read dZ once
+            // mma_bar arrives, so the next iteration may overwrite it)
+            ok = mbar_wait_bounded(pbar, phase) && ok;
+            phase ^= 1u;
+            tc_fence_after();
+            load_acc(acc, t_lane + n0);
+#pragma unroll
+            for (int j = 0; j < kNT; j++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int row = m0 + gid + 8 * hh, col = n0 + j * 8 + 2 * tig;
+                    const uint32_t zw = reinterpret_cast<const uint32_t *>(
+                        reinterpret_cast<const __nv_bfloat16 *>(Zs + (l - 1) * kMat) + cm_index(row, col))[0];
+                    acc[j][2 * hh] *= silu_d(lo_of(zw));
+                    acc[j][2 * hh + 1] *= silu_d(hi_of(zw));
                 }
         }
-        if (l == 0) break;
-        // input gradient dA = dZ W_l (this warp's rows and columns), then dZ_{l-1} = dA silu'(Z_{l-1})
-        zero_acc(acc);
-        warp_gemm(acc, dZ, Wb + (l - 1) * kMat, m0, n0, lane);
-#pragma unroll
-        for (int j = 0; j < kNT; j++)
-#pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
-                const int row = m0 + gid + 8 * hh, col = n0 + j * 8 + 2 * tig;
-                const uint32_t zw = Zs[(l - 1) * kMat + row * kLd + (col >> 1)];
-                acc[j][2 * hh] *= silu_d(lo_of(zw));
-                acc[j][2 * hh + 1] *= silu_d(hi_of(zw));
-            }
-        __syncthreads();  // every warp is done reading dZ and dZ^T before they are overwritten
+        if (run && w_pending >= 0) drain_wgrad();
+        if (!ok) err = kErrProduct;
     }
+    // teardown: on an error, one more commit (on drain_bar, bounded wait) covers every product this
+    // block issued; every TMEM load has finished; then the TMEM columns are released
+    const bool all_ok = __syncthreads_and(err == 0);
+    if (!all_ok && tid == 0) {
+        commit_to(dbar);
+        mbar_wait_bounded(dbar, 0u);
+    }
+    tc_fence_before();
     __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+    if (!all_ok) {
+        if (tid == 0) atomicOr(g.err, err ? err : kErrProduct);
+        return;
+    }
     // the block's bias gradients and loss
     float *dst = g.partial + (size_t)blockIdx.x * g.n_params;
     for (int l = 0; l < kLayers; l++) {
@@ -392,8 +493,8 @@ __device__ __forceinline__ bool image_slots(uint32_t i, uint32_t out_dim, uint32
     const uint32_t fo = l == (uint32_t)kHidden ? out_dim : (uint32_t)kW;
     if (r >= fo * kW) return false;
     const uint32_t o = r / kW, in = r % kW;
-    f = (l * kMat + o * kLd) * 2u + in;
-    b = l >= 1 ? (((uint32_t)kLayers + l - 1u) * kMat + in * kLd) * 2u + o : 0xFFFFFFFFu;
+    f = l * (uint32_t)kMatHalves + cm_index(o, in);
+    b = l >= 1 ? ((uint32_t)kLayers + l - 1u) * (uint32_t)kMatHalves + cm_index(in, o) : 0xFFFFFFFFu;
     return true;
 }
 __device__ __forceinline__ void image_store(uint32_t *image, uint32_t i, uint32_t out_dim, float v) {

@@ -19,7 +19,7 @@ struct FusedTrainArgs {
     float *partial;        // [blocks][n_params]: each block's gradient
     float *partial_loss;   // [blocks]
     const uint32_t *image; // packed BF16 weights, both operand layouts (fused_train_image_words words)
-    uint32_t *err;         // bit 0: a block's weight staging did not complete within its wait bound
+    uint32_t *err;         // bit 0: a block's weight staging, bit 1: a product did not complete within its wait bound
 };
 
 size_t fused_train_smem_bytes();
