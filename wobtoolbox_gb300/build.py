@@ -29,8 +29,9 @@ CU_SOURCES = ["capi.cu", "kernels_dispatch.cu", "k2_generic_domain.cu", "k2_gene
               "k2_multi_rhs.cu", "k3_multi_rhs.cu", "mlp.cu", "scene_build_gpu.cu",
               "k_vpl.cu", "k_wos.cu", "k_sl.cu", "k_cv_tables.cu", "mlp_train.cu", "k_probe.cu", "k_fwd_wave.cu", "k_sample.cu"]
 # Units outside the bit-exact walk, compiled with FMA contraction: the control-variate tables
-# (checked against a float64 restatement with a tolerance, not path for path).
-CONTRACTED_SOURCES = {"k_cv_tables.cu"}
+# (checked against a float64 restatement with a tolerance, not path for path) and the fused
+# training step (checked against float64 autograd with a tolerance).
+CONTRACTED_SOURCES = {"k_cv_tables.cu", "mlp_train.cu"}
 CPP_SOURCES = ["scene_build.cpp"]
 
 
