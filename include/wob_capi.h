@@ -467,6 +467,15 @@ int wob_mlp_train(wob_mlp mlp, const float *inputs, const float *targets, uint32
                   uint32_t batch, float lr, uint64_t seed, float *loss_history, void *stream);
 int wob_mlp_gradient_fused(wob_mlp mlp, const float *inputs, const float *targets, uint32_t n, float *grad,
                            float *loss, void *stream);
+/*
+ * wob_mlp_inject_wait_timeout: a test of the fused step's failure path. With polls > 0 every block
+ * of the following fused steps waits `polls` polls on an mbarrier nothing arrives on before its
+ * first product and takes the timeout as a product that did not complete: the block sets the error
+ * word, drains its products, releases its tensor memory and returns; the update is skipped, so the
+ * parameters keep their values, and wob_mlp_train returns WOB_ERR_DEVICE_LIMIT. polls = 0 turns it
+ * off. No GPU fault or hang is involved.
+ */
+int wob_mlp_inject_wait_timeout(wob_mlp mlp, uint32_t polls);
 
 /*
  * All hits of the infinite lines origin + t dir (the query of scene.cuh:483-486 / 787-790).

@@ -9,6 +9,11 @@
   WOB_ERR_DEVICE_LIMIT, and restoring the default gives the unbounded results again.
 - Elements of zero area inside a valid scene carry no sampling weight and meet no line: walks on
   such scenes stay finite and bit-identical to the oracle.
+- The fused training step's waits on its tensor-core products are bounded: with
+  wob_mlp_inject_wait_timeout every block waits on an mbarrier nothing arrives on, the wait runs
+  out, the blocks drain and release their tensor memory, the update is skipped (the parameters
+  keep their values) and wob_mlp_train returns WOB_ERR_DEVICE_LIMIT; with the injection off the
+  same network trains normally afterwards.
 """
 from __future__ import annotations
 
@@ -116,3 +121,32 @@ def test_zero_area_elements_walk_finite(engine, oracle, cuda, dim):
     _, _, _, ref = oracle.solve_domain(oracle.Elements(sv, sn, sb, st, sa), params, pts, per_path=True)
     assert np.array_equal(got, ref)
     scene.close()
+
+
+def test_training_wait_timeout_is_reported(engine, cuda):
+    from wobtoolbox_gb300 import cv
+    torch = cuda
+    lib = engine.load()
+    rng = np.random.default_rng(5)
+    n = 4096
+    x = rng.uniform(-1, 1, (n, 6)).astype(np.float32)
+    t = (np.sin(2 * x[:, 0]) + 0.3 * x[:, 1]).astype(np.float32)
+    dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    mlp = cv.MLP(32, 4, 1, 0.5, seed=1)
+    p0 = mlp.params()[0].copy()
+    engine.check(lib.wob_mlp_inject_wait_timeout(mlp._h, 1000))
+    hist = torch.zeros(5, device="cuda")
+    with pytest.raises(engine.WobError) as err:
+        mlp.train(dx, dt, n, 5, 1024, 1e-3, seed=3, loss_history=hist)
+    assert err.value.status == WOB_ERR_DEVICE_LIMIT and "product" in str(err.value), str(err.value)
+    torch.cuda.synchronize()
+    assert np.array_equal(mlp.params()[0], p0)  # no update from a step with a missing gradient
+    assert not hist.any()
+    engine.check(lib.wob_mlp_inject_wait_timeout(mlp._h, 0))
+    hist = torch.zeros(50, device="cuda")
+    mlp.train(dx, dt, n, 50, 1024, 3e-3, seed=3, loss_history=hist)
+    torch.cuda.synchronize()
+    h = hist.cpu().numpy()
+    assert np.all(h > 0) and h[-5:].mean() < h[:5].mean(), h
+    assert not np.array_equal(mlp.params()[0], p0)
+    mlp.close()

@@ -33,7 +33,7 @@ EXPORTED = [
     "wob_scene_set_control_variate", "wob_solve_domain_cv", "wob_cv_residual_data", "wob_cv_potential",
     "wob_scene_clone", "wob_scene_add_boundary_offsets", "wob_scene_element_frames", "wob_scene_sample_boundary", "wob_clip_magnitude_quantile", "wob_measure_gather_peak", "wob_scene_set_step_limits", "wob_mlp_create", "wob_mlp_destroy",
     "wob_mlp_num_params", "wob_mlp_get_params", "wob_mlp_set_params", "wob_mlp_forward", "wob_mlp_gradient",
-    "wob_mlp_adam_step", "wob_mlp_train", "wob_mlp_gradient_fused", "wob_scene_set_rhs", "wob_solve_domain_multi",
+    "wob_mlp_adam_step", "wob_mlp_train", "wob_mlp_gradient_fused", "wob_mlp_inject_wait_timeout", "wob_scene_set_rhs", "wob_solve_domain_multi",
     "wob_solve_unknown_boundary_multi",
     "wob_scene_set_rhs_control_variate", "wob_solve_domain_multi_cv", "wob_scene_create_device",
     "wob_vpl_paths", "wob_vpl_aggregate", "wob_solve_wos", "wob_closest_point",
@@ -134,6 +134,7 @@ def load_library(path: str) -> C.CDLL:
         "wob_mlp_adam_step": (C.c_int, [vp, vp, vp, u32, f32, vp, vp]),
         "wob_mlp_train": (C.c_int, [vp, vp, vp, u32, u32, u32, f32, u64, vp, vp]),
         "wob_mlp_gradient_fused": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
+        "wob_mlp_inject_wait_timeout": (C.c_int, [vp, u32]),
         "wob_scene_set_rhs": (C.c_int, [vp, vp, u32]),
         "wob_solve_domain_multi": (C.c_int, [vp, P(wob_params), vp, u32, vp, vp, vp, vp, vp]),
         "wob_solve_unknown_boundary_multi": (C.c_int, [vp, P(wob_params), vp, vp, vp, vp, vp, vp, u32, vp, vp, vp,

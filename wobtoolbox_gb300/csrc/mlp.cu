@@ -291,6 +291,7 @@ struct wob_mlp_s {
     uint32_t *step = nullptr;   // [2]: step counter, the fused update's count of finished blocks
     uint32_t *image = nullptr;  // packed BF16 weights of the fused step (zero padding)
     uint32_t *err = nullptr;    // fused step's error word
+    uint32_t inject_wait_polls = 0;  // wob_mlp_inject_wait_timeout
     std::mutex mu;
 
     uint32_t n_layers() const { return hidden + 1; }
@@ -558,6 +559,13 @@ int wob_mlp_adam_step(wob_mlp m, const float *inputs, const float *targets, uint
     return e == cudaSuccess ? WOB_OK : mfail_cuda(e, "Adam step");
 }
 
+int wob_mlp_inject_wait_timeout(wob_mlp m, uint32_t polls) {
+    if (!m) return mfail(WOB_ERR_INVALID_ARGUMENT, "mlp is NULL");
+    std::lock_guard<std::mutex> lock(m->mu);
+    m->inject_wait_polls = polls;
+    return WOB_OK;
+}
+
 int wob_mlp_gradient_fused(wob_mlp m, const float *inputs, const float *targets, uint32_t n, float *grad, float *loss,
                            void *stream) {
     if (!m || !inputs || !targets || !grad || n == 0)
@@ -569,7 +577,7 @@ int wob_mlp_gradient_fused(wob_mlp m, const float *inputs, const float *targets,
     if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
     if ((e = cudaMemsetAsync(m->step, 0, 8, st)) != cudaSuccess) return mfail_cuda(e, "MLP step counter");
     wobgb::FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, n, m->n_params, 0u, 0ull, m->step,
-                            m->partial, m->partial_loss, m->image, m->err};
+                            m->partial, m->partial_loss, m->image, m->err, m->inject_wait_polls};
     e = wobgb::launch_fused_gradient(a, grad, loss, st);
     return e == cudaSuccess ? WOB_OK : mfail_cuda(e, "fused MLP gradient");
 }
@@ -618,7 +626,7 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
     cudaError_t e_body = cudaSuccess;
     if (fused) {
         FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, batch, m->n_params, 1u, seed, m->step,
-                         m->partial, m->partial_loss, m->image, m->err};
+                         m->partial, m->partial_loss, m->image, m->err, m->inject_wait_polls};
         e_body = launch_fused_train_step(a, m->params, m->adam_m, m->adam_v, steps, lr, adam_base, loss_history, cs);
     } else {
         train_schedule_kernel<<<1, 1, 0, cs>>>(m->step, steps, lr, adam_base, m->sched);
@@ -644,7 +652,14 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
         cleanup();
         return mfail_cuda(e, "finishing the training steps");
     }
-    m->adam_steps += steps;
+    // the bias corrections continue from the updates that ran: the step counter (a failed fused
+    // step skips its update and stops the count)
+    uint32_t ran = steps;
+    if ((e = cudaMemcpy(&ran, m->step, 4, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+        cleanup();
+        return mfail_cuda(e, "reading the step counter");
+    }
+    m->adam_steps += ran;
     cleanup();
     if (fused) {
         uint32_t bits = 0;

@@ -199,8 +199,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     return done != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitPolls; i++)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t polls = kWaitPolls) {
+    for (uint32_t i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -305,6 +305,9 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
         }
         fence_async_smem();
         __syncthreads();
+        // injected failure (tests): a bounded wait on drain_bar, on which nothing arrives before the
+        // teardown, runs out like a product whose completion never came
+        if (g.inject_wait_polls) ok = __syncthreads_and(mbar_wait_bounded(dbar, 0u, g.inject_wait_polls));
 
         float acc[kNT][4];
         // ---- forward: Z_l = act W_l^T in TMEM columns [0, 64); ok is block-uniform at the top of
@@ -548,8 +551,11 @@ __global__ void __launch_bounds__(256) mlp_reduce_adam_kernel(
     float *__restrict__ p, float *__restrict__ m, float *__restrict__ v, const float *__restrict__ partial,
     const float *__restrict__ partial_loss, uint32_t n_blocks, uint32_t n_params, uint32_t out_dim,
     uint32_t *__restrict__ image, uint32_t *__restrict__ step, uint32_t steps, float lr0, uint32_t adam_base,
-    float *__restrict__ loss_hist) {
+    float *__restrict__ loss_hist, const uint32_t *__restrict__ err) {
     __shared__ float red[kRedSplit][33];
+    // a block of the fused step failed (its gradient is missing): no update, no step advance, so the
+    // parameters stay those of the last complete step
+    if (*err) return;
     const uint32_t s = *step;
     const uint32_t i = blockIdx.x * 32u + (threadIdx.x & 31u);
     const float gsum = ordered_gradient(partial, n_blocks, n_params, i, red);
@@ -612,7 +618,7 @@ cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, floa
     mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
     mlp_reduce_adam_kernel<<<(a.n_params + 31) / 32, 256, 0, stream>>>(
         params, adam_m, adam_v, a.partial, a.partial_loss, blocks, a.n_params, a.out_dim, const_cast<uint32_t *>(a.image),
-        a.step, steps, lr, adam_base, loss_hist);
+        a.step, steps, lr, adam_base, loss_hist, a.err);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,10 @@ struct FusedTrainArgs {
     float *partial_loss;   // [blocks]
     const uint32_t *image; // packed BF16 weights, both operand layouts (fused_train_image_words words)
     uint32_t *err;         // bit 0: a block's weight staging, bit 1: a product did not complete within its wait bound
+    // Nonzero (tests of the failure path): before its first product every block also waits this
+    // many polls on an mbarrier nothing arrives on, and takes that as a product whose completion
+    // did not arrive.
+    uint32_t inject_wait_polls;
 };
 
 size_t fused_train_smem_bytes();
