@@ -27,7 +27,10 @@ quadrupole expansion of their centroid sources about the cluster's mean centroid
 cluster is farther than max(rho / theta, rho + eta) (rho: its radius about z, eta: its largest
 near radius) plus omega from the centre W of the 32 consecutive targets of a warp (omega: their
 radius about W), the triangles in storage order and the evaluation points in Morton order
-(_morton_order). _cluster_far restates that decision and _cluster_field the expansion.
+(_morton_order). The same test is made first for groups of 8 clusters (256 triangles) and groups of
+8 of those (2048 triangles), with records of the same form from their member sources: a far group
+is one expansion, a near one is looked into (_hierarchy_split). _cluster_far restates the decision
+and _cluster_field the expansion.
 """
 from __future__ import annotations
 
@@ -164,22 +167,31 @@ def _morton_order(points):
     return np.lexsort((np.arange(len(p)), code))
 
 
-def _cluster_split(tx, cen, w, near2, theta, size=32, order=None):
-    """Per target: the far clusters' expansion (phi, grad) and the mask [targets, sources] of the
-    sources still summed pair by pair, for targets tx in warps of 32 consecutive ones."""
-    z, r_far, M0, M1, M2 = _clusters(cen, w, near2, theta, size)
+def _cluster_split(tx, cen, w, near2, theta, size=32, order=None, fan=8):
+    """Per target: the far records' expansion (phi, grad) and the mask [targets, sources] of the
+    sources still summed pair by pair, for targets tx in warps of 32 consecutive ones. Records of
+    three sizes (size, size * fan, size * fan^2 consecutive sources); one is taken when it is far
+    and none of its ancestors is (k_cv_tables.cu's cv_sum_kernel)."""
+    levels = [_clusters(cen, w, near2, theta, size * fan ** L) for L in range(3)]
     phi = np.zeros(len(tx)); g = np.zeros((len(tx), 3))
     pair = np.ones((len(tx), len(cen)), bool)
     order = np.arange(len(tx)) if order is None else order
     for g0 in range(0, len(tx), 32):
         grp = order[g0:g0 + 32]
-        far = _cluster_far(tx[grp], z, r_far)
-        if far.any():
-            ph, gr = _cluster_field(tx[grp], z[far], M0[far], M1[far], M2[far])
-            phi[grp] += ph
-            g[grp] += gr
-            for k in np.nonzero(far)[0]:
-                pair[np.ix_(grp, np.arange(k * size, min(len(cen), (k + 1) * size)))] = False
+        covered = None  # per level-0 record: inside a record already taken
+        for L in (2, 1, 0):
+            z, r_far, M0, M1, M2 = levels[L]
+            far = _cluster_far(tx[grp], z, r_far)
+            if covered is not None:  # ancestors at level L + 1: record k's parent is k // fan
+                far &= ~covered[np.arange(len(z)) // fan]
+            if far.any():
+                ph, gr = _cluster_field(tx[grp], z[far], M0[far], M1[far], M2[far])
+                phi[grp] += ph
+                g[grp] += gr
+                span = size * fan ** L
+                for k in np.nonzero(far)[0]:
+                    pair[np.ix_(grp, np.arange(k * span, min(len(cen), (k + 1) * span)))] = False
+            covered = far if covered is None else (far | covered[np.arange(len(z)) // fan])
     return phi, g, pair
 
 

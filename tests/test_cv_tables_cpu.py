@@ -47,8 +47,9 @@ def _median_order(cen, ids=None):
 
 
 def test_cluster_expansion_close_to_pairwise():
-    """theta = 0.3: clusters of 32 taken by their quadrupole expansion change the residual data
-    and the potential by well under the pairwise split's own error; theta = 0 is the pairwise sum."""
+    """theta = 0.3: clusters of 32 and groups of 256 and 2048 triangles taken by their quadrupole
+    expansion change the residual data and the potential by well under the pairwise split's own
+    error; theta = 0 is the pairwise sum."""
     from wobtoolbox_gb300 import workloads as W
     V, F, _ = W.displaced_icosphere(4, 0.15, 4, 0)
     verts, normals = W.mesh_elements(V, F)

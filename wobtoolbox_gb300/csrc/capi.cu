@@ -1042,14 +1042,14 @@ int cv_sources(wob_scene s, const float *sigma, float near_factor, float theta, 
     if (!(near_factor >= 0.0f) || !(near_factor < 1e6f)) return fail(WOB_ERR_INVALID_ARGUMENT, "near_factor must be in [0, 1e6)");
     if (!(theta >= 0.0f) || !(theta < 1.0f)) return fail(WOB_ERR_INVALID_ARGUMENT, "theta must be in [0, 1)");
     const size_t n = s->host.n;
-    const size_t n_cl = (n + 31) / 32;
+    const size_t n_rec = wobgb::cv_cluster_records((uint32_t)n);  // clusters and their two group levels
     cudaError_t e;
     if ((e = cudaMalloc(&cs.src.ptr, n * 16)) != cudaSuccess || (e = cudaMalloc(&cs.near2.ptr, n * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&cs.clusters.ptr, n_cl * 64)) != cudaSuccess)
+        (e = cudaMalloc(&cs.clusters.ptr, n_rec * 64)) != cudaSuccess)
         return fail_cuda(e, "allocating the control-variate sources");
     cs.src.bytes = n * 16;
     cs.near2.bytes = n * 4;
-    cs.clusters.bytes = n_cl * 64;
+    cs.clusters.bytes = n_rec * 64;
     e = wobgb::launch_cv_sources(s->view<3>(), sigma, near_factor, theta, (float4 *)cs.src.ptr, (float *)cs.near2.ptr,
                                  (float4 *)cs.clusters.ptr, st);
     return e == cudaSuccess ? WOB_OK : fail_cuda(e, "launching the control-variate sources");

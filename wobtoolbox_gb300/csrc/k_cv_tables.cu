@@ -21,20 +21,22 @@
 // triangle's own term in the residual data is zero: n_j is normal to triangle j, so dG/dn_x
 // vanishes on it.
 //
-// Far field by clusters (a two-level treecode): the stored triangles are cut into clusters of 32
-// consecutive ones (BVH storage order keeps them spatially compact), each with its centre z (mean
-// centroid), radius rho, largest near radius eta and the moments of its centroid sources about z
-// up to the quadrupole (M0 = sum w, M1 = sum w d, M2 = sum w d d^T, w = sigma~ A, d = c - z).
-// A block takes 32 consecutive targets and the bounding sphere (W, omega) of their positions; a
-// cluster with |W - z| > max(rho / theta, rho + eta) + omega is far from every target of the block
-// and enters through its quadrupole expansion of sum w / |x - c| (one evaluation instead of 32,
-// error of order (rho / |x - z|)^3 of the cluster's share); any other cluster is taken triangle by
-// triangle as above. theta = 0 takes every triangle (the dense sum). The decision is uniform
-// across the block, so lanes never diverge between the two.
+// Far field by a treecode over consecutive stored triangles (BVH storage order keeps them
+// spatially compact): clusters of 32, groups of 8 clusters (256 triangles) and groups of 8 of
+// those (2048), each record with its centre z (mean centroid), radius rho, largest near radius eta
+// and the moments of its centroid sources about z up to the quadrupole (M0 = sum w, M1 = sum w d,
+// M2 = sum w d d^T, w = sigma~ A, d = c - z). A block takes 32 consecutive targets and the
+// bounding sphere (W, omega) of their positions; a record with |W - z| > max(rho / theta,
+// rho + eta) + omega is far from every target of the block and enters through its quadrupole
+// expansion of sum w / |x - c| (one evaluation per target for all its triangles, error of order
+// (rho / |x - z|)^3 of its share). The block starts from the largest groups and looks into the
+// near ones; a near cluster is taken triangle by triangle as above. theta = 0 takes every
+// triangle (the dense sum). The decisions are uniform across the block, so lanes never diverge.
 //
-// Work decomposition: one block per 32 targets (a lane each), its 8 warps splitting the cluster
-// table (records read as broadcasts), FP32 partial sums over 32 clusters, FP64 across them and
-// across the warps (in warp order: deterministic).
+// Work decomposition: one block per 32 targets (a lane each); its 8 warps make the same decisions
+// and take the work by index (a far group to warp index mod 8, the 8 clusters of a near group one
+// each), records read as broadcasts; FP32 partial sums over 32 items, FP64 across them and across
+// the warps (in warp order: deterministic).
 // This unit is compiled with FMA contraction (it is not part of the bit-exact walk).
 #include "device_common.cuh"
 #include "launch.hpp"
@@ -248,6 +250,61 @@ __global__ void cv_cluster_kernel(uint32_t n, const float4 *__restrict__ src, co
     }
 }
 
+// Groups of kGroupFan^L clusters (L = 1, 2: 256 and 2048 consecutive stored triangles), one block
+// of 256 threads each: the same record as a cluster's, from the member sources directly (centre =
+// mean centroid, exact radius, largest near radius, moments about the centre).
+constexpr int kGroupFan = 8;
+constexpr int kGroupBlock = 256;
+__device__ __forceinline__ float block_reduce(float v, bool is_max, float *red) {
+    v = is_max ? warp_max_f(v) : warp_sum_f(v);
+    if ((threadIdx.x & 31u) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float t = red[0];
+    for (int w = 1; w < kGroupBlock / 32; w++) t = is_max ? fmaxf(t, red[w]) : t + red[w];
+    __syncthreads();
+    return t;
+}
+template <uint32_t kSize>
+__global__ void __launch_bounds__(kGroupBlock) cv_group_kernel(uint32_t n, const float4 *__restrict__ src,
+                                                               const float *__restrict__ near2, float theta,
+                                                               float4 *__restrict__ rec) {
+    __shared__ float red[kGroupBlock / 32];
+    const uint32_t g = blockIdx.x, i0 = g * kSize, i1 = min(n, i0 + kSize);
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (uint32_t i = i0 + threadIdx.x; i < i1; i += kGroupBlock) {
+        const float4 q = __ldg(src + i);
+        sx += q.x;
+        sy += q.y;
+        sz += q.z;
+    }
+    const float cnt = (float)(i1 - i0);
+    const float zx = block_reduce(sx, false, red) / cnt, zy = block_reduce(sy, false, red) / cnt,
+                zz = block_reduce(sz, false, red) / cnt;
+    float r2 = 0.0f, e2 = 0.0f, m[10] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t i = i0 + threadIdx.x; i < i1; i += kGroupBlock) {
+        const float4 q = __ldg(src + i);
+        const float dx = q.x - zx, dy = q.y - zy, dz = q.z - zz, w = q.w;
+        r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+        e2 = fmaxf(e2, __ldg(near2 + i));
+        m[0] += w;
+        m[1] += w * dx; m[2] += w * dy; m[3] += w * dz;
+        m[4] += w * dx * dx; m[5] += w * dy * dy; m[6] += w * dz * dz;
+        m[7] += w * dx * dy; m[8] += w * dx * dz; m[9] += w * dy * dz;
+    }
+    const float rho = sqrtf(block_reduce(r2, true, red)), eta = sqrtf(block_reduce(e2, true, red));
+#pragma unroll
+    for (int k = 0; k < 10; k++) m[k] = block_reduce(m[k], false, red);
+    if (threadIdx.x == 0) {
+        const float r_far = theta > 0.0f ? fmaxf(rho / theta, rho + eta) : __int_as_float(0x7f800000);
+        rec[4 * g + 0] = make_float4(zx, zy, zz, r_far);
+        rec[4 * g + 1] = make_float4(m[0], m[1], m[2], m[3]);
+        rec[4 * g + 2] = make_float4(m[4], m[5], m[6], m[7]);
+        rec[4 * g + 3] = make_float4(m[8], m[9], m[4] + m[5] + m[6], 0.0f);
+    }
+}
+
+__host__ __device__ __forceinline__ uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
 // sum w / |x - c| over a cluster by its quadrupole expansion about z (R = x - z):
 //   phi = M0 / R + (R . M1) / R^3 + (3 R.M2.R - R^2 tr M2) / (2 R^5),
 // and its gradient term by term.
@@ -307,69 +364,105 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const uint32_t n_src = s.n_elems;
-    const uint32_t n_cl = (n_src + kClusterSize - 1) / kClusterSize;
+    const uint32_t n_cl = div_up(n_src, kClusterSize), n_g1 = div_up(n_cl, kGroupFan), n_g2 = div_up(n_g1, kGroupFan);
+    const float4 *g1 = cl + 4 * (size_t)n_cl, *g2 = g1 + 4 * (size_t)n_g1;
     uint32_t taken = 0;
-    for (uint32_t k = wid; k < n_cl; k += kCvWarps) {
-        const float4 q0 = __ldg(cl + 4 * k);
+    // far from every target of the block: |W - z| > r_far + omega
+    auto is_far = [&](const float4 &q0) {
         const float Dx = Wx - q0.x, Dy = Wy - q0.y, Dz = Wz - q0.z;
         const float thr = q0.w + om;
-        if (Dx * Dx + Dy * Dy + Dz * Dz > thr * thr) {
-            // far from every target of the block: the cluster's expansion
-            const float4 q1 = __ldg(cl + 4 * k + 1), q2 = __ldg(cl + 4 * k + 2), q3 = __ldg(cl + 4 * k + 3);
-            float phi, g[3];
-            cluster_field(xd, q0, q1, q2, q3, phi, g);
-            if (kMode == 0) {
-                a[0] -= g[0] * nn[0] + g[1] * nn[1] + g[2] * nn[2];
-            } else {
-                a[0] += phi;
-                a[1] += g[0];
-                a[2] += g[1];
-                a[3] += g[2];
-            }
+        return Dx * Dx + Dy * Dy + Dz * Dz > thr * thr;
+    };
+    // a record's expansion at this lane's target; FP32 partial sums flushed to FP64 every 32 items
+    auto expand = [&](const float4 *r, const float4 &q0) {
+        const float4 q1 = __ldg(r + 1), q2 = __ldg(r + 2), q3 = __ldg(r + 3);
+        float phi, g[3];
+        cluster_field(xd, q0, q1, q2, q3, phi, g);
+        if (kMode == 0) {
+            a[0] -= g[0] * nn[0] + g[1] * nn[1] + g[2] * nn[2];
         } else {
-            const uint32_t i0 = k * kClusterSize, i1 = min(n_src, i0 + kClusterSize);
-            for (uint32_t i = i0; i < i1; i++) {
-                const float4 q = __ldg(src + i);
-                const float n2 = __ldg(near2 + i);
-                const float dx = xd[0] - q.x, dy = xd[1] - q.y, dz = xd[2] - q.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                const bool near = r2 < n2;
-                if (!near) {
-                    const float rinv = rsqrtf(r2);
-                    const float r3 = rinv * rinv * rinv;
-                    if (kMode == 0) {
-                        a[0] += q.w * (dx * nn[0] + dy * nn[1] + dz * nn[2]) * r3;
-                    } else {
-                        a[0] += q.w * rinv;
-                        const float wr3 = q.w * r3;
-                        a[1] -= wr3 * dx;
-                        a[2] -= wr3 * dy;
-                        a[3] -= wr3 * dz;
-                    }
-                }
-                if (__any_sync(0xffffffffu, near && active)) {
-                    if (near && active && !(kMode == 0 && i == tgt)) {
-                        const TriVerts tri = load_tri(s, i);
-                        float P, G[3];
-                        triangle_potential(xd, tri, P, G);
-                        const float sg = __ldg(sigma + i);
-                        if (kMode == 0) {
-                            a[0] -= sg * (G[0] * nn[0] + G[1] * nn[1] + G[2] * nn[2]);
-                        } else {
-                            a[0] += sg * P;
-                            a[1] += sg * G[0];
-                            a[2] += sg * G[1];
-                            a[3] += sg * G[2];
-                        }
-                    }
-                }
-            }
+            a[0] += phi;
+            a[1] += g[0];
+            a[2] += g[1];
+            a[3] += g[2];
         }
+    };
+    auto flush = [&]() {
         if ((++taken & 31u) == 0u) {
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 acc[c] += a[c];
                 a[c] = 0.0f;
+            }
+        }
+    };
+    // Every warp walks the same decisions (uniform across the block); the work is dealt by index:
+    // a far group or level-1 group to warp (index mod 8), the clusters of a near level-1 group one
+    // per warp, so the near field spreads over the warps as in a flat pass over the clusters.
+    for (uint32_t k2 = 0; k2 < n_g2; k2++) {
+        const float4 h2 = __ldg(g2 + 4 * k2);
+        if (is_far(h2)) {
+            if (k2 % kCvWarps == wid) {
+                expand(g2 + 4 * k2, h2);
+                flush();
+            }
+            continue;
+        }
+        const uint32_t k1_end = min(n_g1, (k2 + 1) * kGroupFan);
+        for (uint32_t k1 = k2 * kGroupFan; k1 < k1_end; k1++) {
+            const float4 h1 = __ldg(g1 + 4 * k1);
+            if (is_far(h1)) {
+                if (k1 % kCvWarps == wid) {
+                    expand(g1 + 4 * k1, h1);
+                    flush();
+                }
+                continue;
+            }
+            const uint32_t k_end = min(n_cl, (k1 + 1) * kGroupFan);
+            for (uint32_t k = k1 * kGroupFan + wid; k < k_end; k += kCvWarps) {
+                const float4 q0 = __ldg(cl + 4 * k);
+                if (is_far(q0)) {
+                    expand(cl + 4 * k, q0);
+                } else {
+                    const uint32_t i0 = k * kClusterSize, i1 = min(n_src, i0 + kClusterSize);
+                    for (uint32_t i = i0; i < i1; i++) {
+                        const float4 q = __ldg(src + i);
+                        const float n2 = __ldg(near2 + i);
+                        const float dx = xd[0] - q.x, dy = xd[1] - q.y, dz = xd[2] - q.z;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const bool near = r2 < n2;
+                        if (!near) {
+                            const float rinv = rsqrtf(r2);
+                            const float r3 = rinv * rinv * rinv;
+                            if (kMode == 0) {
+                                a[0] += q.w * (dx * nn[0] + dy * nn[1] + dz * nn[2]) * r3;
+                            } else {
+                                a[0] += q.w * rinv;
+                                const float wr3 = q.w * r3;
+                                a[1] -= wr3 * dx;
+                                a[2] -= wr3 * dy;
+                                a[3] -= wr3 * dz;
+                            }
+                        }
+                        if (__any_sync(0xffffffffu, near && active)) {
+                            if (near && active && !(kMode == 0 && i == tgt)) {
+                                const TriVerts tri = load_tri(s, i);
+                                float P, G[3];
+                                triangle_potential(xd, tri, P, G);
+                                const float sg = __ldg(sigma + i);
+                                if (kMode == 0) {
+                                    a[0] -= sg * (G[0] * nn[0] + G[1] * nn[1] + G[2] * nn[2]);
+                                } else {
+                                    a[0] += sg * P;
+                                    a[1] += sg * G[0];
+                                    a[2] += sg * G[1];
+                                    a[3] += sg * G[2];
+                                }
+                            }
+                        }
+                    }
+                }
+                flush();
             }
         }
     }
@@ -441,9 +534,18 @@ template cudaError_t launch_element_frames<3>(const SceneView<3> &, float *, cud
 cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float theta, float4 *src,
                               float *near2, float4 *clusters, cudaStream_t stream) {
     cv_sources_kernel<<<(s.n_elems + 255) / 256, 256, 0, stream>>>(s, sigma, near_factor, src, near2);
-    const uint32_t n_cl = (s.n_elems + kClusterSize - 1) / kClusterSize;
+    const uint32_t n_cl = div_up(s.n_elems, kClusterSize), n_g1 = div_up(n_cl, kGroupFan), n_g2 = div_up(n_g1, kGroupFan);
     cv_cluster_kernel<<<(n_cl * 32 + 255) / 256, 256, 0, stream>>>(s.n_elems, src, near2, theta, clusters);
+    cv_group_kernel<kClusterSize * kGroupFan><<<n_g1, kGroupBlock, 0, stream>>>(s.n_elems, src, near2, theta,
+                                                                               clusters + 4 * (size_t)n_cl);
+    cv_group_kernel<kClusterSize * kGroupFan * kGroupFan><<<n_g2, kGroupBlock, 0, stream>>>(
+        s.n_elems, src, near2, theta, clusters + 4 * (size_t)(n_cl + n_g1));
     return cudaGetLastError();
+}
+
+uint32_t cv_cluster_records(uint32_t n_elems) {
+    const uint32_t n_cl = div_up(n_elems, kClusterSize), n_g1 = div_up(n_cl, kGroupFan);
+    return n_cl + n_g1 + div_up(n_g1, kGroupFan);
 }
 
 cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,

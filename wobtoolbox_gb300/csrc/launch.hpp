@@ -60,6 +60,9 @@ cudaError_t launch_domain_cv_3d(const SceneView<3> &s, const WalkParams &p, cons
 // network input of every stored element ([n][6]).
 cudaError_t launch_cv_sources(const SceneView<3> &s, const float *sigma, float near_factor, float theta, float4 *src,
                               float *near2, float4 *clusters, cudaStream_t stream);
+// Records (64 bytes each) of the cluster table: clusters of 32 stored triangles, then groups of 8
+// clusters, then groups of 8 of those.
+uint32_t cv_cluster_records(uint32_t n_elems);
 cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
                                const float *sigma, float c_coef, float *delta, cudaStream_t stream);
 // scratch: cv_point_order_words(n_points) 32-bit words (the points' Morton order and bounds).
