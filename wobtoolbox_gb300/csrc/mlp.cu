@@ -594,8 +594,11 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
     const bool fused = m->fused_ok();
     cudaError_t e = fused ? m->ensure_fused(batch) : m->ensure_train(batch);
     if (e != cudaSuccess) return mfail_cuda(e, "MLP training workspace");
-    // The step sequence is captured once into a CUDA graph on a private stream, ordered after the
-    // caller's stream by an event, and replayed `steps` times.
+    // kSteps steps are captured once into a CUDA graph on a private stream, ordered after the
+    // caller's stream by an event, and the graph replayed; the remaining steps (steps mod kSteps)
+    // are launched directly. The fused step's kernels use programmatic dependent launches, which
+    // the capture keeps as graph edges.
+    const uint32_t kSteps = steps < 16u ? steps : 16u;
     cudaStream_t cs = nullptr;
     cudaEvent_t ev = nullptr;
     cudaGraph_t graph = nullptr;
@@ -623,27 +626,35 @@ int wob_mlp_train(wob_mlp m, const float *inputs, const float *targets, uint32_t
         cleanup();
         return mfail_cuda(e, "capturing the training step");
     }
-    cudaError_t e_body = cudaSuccess;
-    if (fused) {
-        FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, batch, m->n_params, 1u, seed, m->step,
-                         m->partial, m->partial_loss, m->image, m->err, m->inject_wait_polls};
-        e_body = launch_fused_train_step(a, m->params, m->adam_m, m->adam_v, steps, lr, adam_base, loss_history, cs);
-    } else {
+    auto one_step = [&]() -> cudaError_t {
+        if (fused) {
+            FusedTrainArgs a{m->params, m->freqs, inputs, targets, n, m->out_dim, batch, m->n_params, 1u, seed, m->step,
+                             m->partial, m->partial_loss, m->image, m->err, m->inject_wait_polls};
+            return launch_fused_train_step(a, m->params, m->adam_m, m->adam_v, steps, lr, adam_base, loss_history, cs);
+        }
         train_schedule_kernel<<<1, 1, 0, cs>>>(m->step, steps, lr, adam_base, m->sched);
         train_gather_kernel<<<(batch + 127) / 128, 128, 0, cs>>>(inputs, targets, n, m->out_dim, batch, seed, m->sched,
                                                                  m->xb, m->tb);
-        e_body = backward_impl(m, m->xb, m->tb, batch, cs);
+        cudaError_t eb = backward_impl(m, m->xb, m->tb, batch, cs);
         adam_sched_kernel<<<(m->n_params + 255) / 256, 256, 0, cs>>>(m->params, m->grad, m->adam_m, m->adam_v,
                                                                      m->n_params, m->sched, 0.9f, 0.999f, 1e-8f);
         if (loss_history) train_record_loss_kernel<<<1, 1, 0, cs>>>(m->loss, m->sched, loss_history);
-    }
+        return eb != cudaSuccess ? eb : cudaGetLastError();
+    };
+    cudaError_t e_body = cudaSuccess;
+    for (uint32_t i = 0; i < kSteps && e_body == cudaSuccess; i++) e_body = one_step();
     e = cudaStreamEndCapture(cs, &graph);
     if (e_body != cudaSuccess || e != cudaSuccess || (e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
         cleanup();
         return mfail_cuda(e_body != cudaSuccess ? e_body : e, "building the training graph");
     }
-    for (uint32_t i = 0; i < steps; i++)
+    for (uint32_t i = 0; i < steps / kSteps; i++)
         if ((e = cudaGraphLaunch(exec, cs)) != cudaSuccess) {
+            cleanup();
+            return mfail_cuda(e, "launching the training steps");
+        }
+    for (uint32_t i = 0; i < steps % kSteps; i++)
+        if ((e = one_step()) != cudaSuccess) {
             cleanup();
             return mfail_cuda(e, "launching a training step");
         }

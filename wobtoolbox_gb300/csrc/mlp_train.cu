@@ -231,27 +231,35 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
     const int rb = warp & (kRowBlocks - 1), m0 = rb * 16, n0 = (warp / kRowBlocks) * kCols;
     const int out_dim = (int)g.out_dim;
-    const uint32_t step = *g.step;
 
-    // weights in both layouts: one bulk copy of the packed image (rows of the head beyond out_dim
-    // are zero there); biases by plain loads meanwhile; TMEM columns for the accumulators
+    // mbarriers and TMEM columns for the accumulators first: they depend on no earlier kernel, so
+    // under a programmatic dependent launch they overlap the previous update's tail
     const uint32_t bar = smem_u32(&stage_bar), pbar = smem_u32(&mma_bar), dbar = smem_u32(&drain_bar);
     const uint32_t wbar0 = smem_u32(&wgrad_bar[0]), wbar1 = smem_u32(&wgrad_bar[1]);
     if (tid == 0) {
         for (uint32_t b : {bar, pbar, wbar0, wbar1, dbar})
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kImageBytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(Wf)), "l"(g.image), "r"(kImageBytes), "r"(bar)
-                     : "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                      "r"(kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // the previous update (weights, image, step counter) complete and visible from here (returns
+    // at once without a programmatic dependency); the next kernel may start launching
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+    const uint32_t step = *g.step;
+    // weights in both layouts: one bulk copy of the packed image (rows of the head beyond out_dim
+    // are zero there); biases by plain loads meanwhile
+    if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kImageBytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(Wf)), "l"(g.image), "r"(kImageBytes), "r"(bar)
+                     : "memory");
     }
     for (int l = 0; l < kLayers; l++) {
         const int fo = l == kHidden ? out_dim : kW;
@@ -553,6 +561,9 @@ __global__ void __launch_bounds__(256) mlp_reduce_adam_kernel(
     uint32_t *__restrict__ image, uint32_t *__restrict__ step, uint32_t steps, float lr0, uint32_t adam_base,
     float *__restrict__ loss_hist, const uint32_t *__restrict__ err) {
     __shared__ float red[kRedSplit][33];
+    // the fused step's gradients complete and visible from here; the next step may start launching
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
     // a block of the fused step failed (its gradient is missing): no update, no step advance, so the
     // parameters stay those of the last complete step
     if (*err) return;
@@ -611,15 +622,34 @@ cudaError_t launch_pack_weights(const float *params, uint32_t n_params, uint32_t
     return cudaGetLastError();
 }
 
+// A launch that may begin while the stream's previous kernel is still running (programmatic
+// dependent launch): the kernel waits for that kernel's completion itself (griddepcontrol.wait).
+template <typename... Params, typename... Args>
+cudaError_t launch_after_previous(void (*kernel)(Params...), uint32_t grid, uint32_t block, size_t smem,
+                                  cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 cudaError_t launch_fused_train_step(const FusedTrainArgs &a, float *params, float *adam_m, float *adam_v,
                                     uint32_t steps, float lr, uint32_t adam_base, float *loss_hist,
                                     cudaStream_t stream) {
     const uint32_t blocks = fused_train_blocks(a.batch);
-    mlp_train_fused_kernel<<<blocks, kThreads, fused_train_smem_bytes(), stream>>>(a);
-    mlp_reduce_adam_kernel<<<(a.n_params + 31) / 32, 256, 0, stream>>>(
-        params, adam_m, adam_v, a.partial, a.partial_loss, blocks, a.n_params, a.out_dim, const_cast<uint32_t *>(a.image),
-        a.step, steps, lr, adam_base, loss_hist, a.err);
-    return cudaGetLastError();
+    cudaError_t e = launch_after_previous(mlp_train_fused_kernel, blocks, kThreads, fused_train_smem_bytes(), stream, a);
+    if (e != cudaSuccess) return e;
+    return launch_after_previous(mlp_reduce_adam_kernel, (a.n_params + 31) / 32, 256, 0, stream, params, adam_m, adam_v,
+                                 (const float *)a.partial, (const float *)a.partial_loss, blocks, a.n_params, a.out_dim,
+                                 const_cast<uint32_t *>(a.image), a.step, steps, lr, adam_base, loss_hist,
+                                 (const uint32_t *)a.err);
 }
 
 cudaError_t launch_fused_gradient(const FusedTrainArgs &a, float *grad, float *loss, cudaStream_t stream) {
