@@ -336,7 +336,8 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
                                                           const float *__restrict__ sigma,
                                                           const float4 *__restrict__ cl, const float *__restrict__ pts,
                                                           const uint64_t *__restrict__ order, uint32_t n_targets,
-                                                          float c_coef, float *__restrict__ out) {
+                                                          float c_coef, float *__restrict__ out,
+                                                          double *__restrict__ part_sums) {
     __shared__ double s_acc[kCvWarps][4][32];
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t slot = blockIdx.x * 32u + lane;
@@ -399,7 +400,9 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
     // Every warp walks the same decisions (uniform across the block); the work is dealt by index:
     // a far group or level-1 group to warp (index mod 8), the clusters of a near level-1 group one
     // per warp, so the near field spreads over the warps as in a flat pass over the clusters.
-    for (uint32_t k2 = 0; k2 < n_g2; k2++) {
+    // the largest groups are split over gridDim.y blocks of the same targets (part blockIdx.y takes
+    // k2 = part, part + gridDim.y, ...), whose sums part_sums holds for cv_parts_kernel
+    for (uint32_t k2 = blockIdx.y; k2 < n_g2; k2 += gridDim.y) {
         const float4 h2 = __ldg(g2 + 4 * k2);
         if (is_far(h2)) {
             if (k2 % kCvWarps == wid) {
@@ -474,7 +477,10 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
     for (int w = 0; w < kCvWarps; w++)
 #pragma unroll
         for (int c = 0; c < 4; c++) t[c] += s_acc[w][c][lane];
-    if (kMode == 0) {
+    if (gridDim.y > 1) {
+        double *ps = part_sums + ((size_t)blockIdx.y * n_targets + slot) * 4;
+        for (int k = 0; k < 4; k++) ps[k] = t[k];
+    } else if (kMode == 0) {
         const double c = (double)c_coef;
         const double Tsig = c * kInv4Pi * t[0];
         out[tgt] = (float)((Tsig - (double)__ldg(sigma + tgt)) / c);
@@ -482,6 +488,25 @@ __global__ void __launch_bounds__(kCvBlock) cv_sum_kernel(SceneView<3> s, const 
         for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * t[k]);
     }
 }
+
+// The potential from its parts, added in part order (deterministic): part_sums [parts][slot][4]
+// by Morton slot, out [n][4] by point.
+__global__ void cv_parts_kernel(const double *__restrict__ part_sums, uint32_t parts, const uint64_t *__restrict__ order,
+                                uint32_t n, float *__restrict__ out) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    const uint32_t tgt = (uint32_t)__ldg(order + slot);
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t p = 0; p < parts; p++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) t[k] += part_sums[((size_t)p * n + slot) * 4 + k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[(size_t)tgt * 4 + k] = (float)(kInv4Pi * t[k]);
+}
+
+// Blocks of the same 32 points the potential's largest groups are split over: with one block per
+// 32 points there are too few blocks to fill the GPU for the slice-sized point sets.
+constexpr uint32_t kPotentialParts = 4;
 
 // The network's input at every stored element: (centroid, normal), 2D padded with zeros.
 template <int D>
@@ -551,14 +576,15 @@ uint32_t cv_cluster_records(uint32_t n_elems) {
 cudaError_t launch_cv_residual(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
                                const float *sigma, float c_coef, float *delta, cudaStream_t stream) {
     cv_sum_kernel<0><<<(s.n_elems + 31) / 32, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, nullptr, nullptr,
-                                                                     s.n_elems, c_coef, delta);
+                                                                     s.n_elems, c_coef, delta, nullptr);
     return cudaGetLastError();
 }
 
 uint32_t cv_point_order_words(uint32_t n_points) {
     uint32_t n2 = 1;
     while (n2 < n_points) n2 <<= 1;
-    return 2 * n2 + 8;  // n2 keys of 8 bytes, then the 6 bound words
+    // n2 keys of 8 bytes, the 6 bound words (padded to 8), the parts' FP64 sums
+    return 2 * n2 + 8 + kPotentialParts * n_points * 8;
 }
 
 cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const float *near2, const float4 *clusters,
@@ -574,8 +600,10 @@ cudaError_t launch_cv_potential(const SceneView<3> &s, const float4 *src, const 
     pts_morton_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(pts, n_points, n2, bb, key);
     for (uint32_t k = 2; k <= n2; k <<= 1)
         for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_kernel<<<(n2 + 255) / 256, 256, 0, stream>>>(n2, j, k, key);
-    cv_sum_kernel<1><<<(n_points + 31) / 32, kCvBlock, 0, stream>>>(s, src, near2, sigma, clusters, pts, key,
-                                                                    n_points, 0.0f, out);
+    double *part_sums = reinterpret_cast<double *>(scratch + 2 * (size_t)n2 + 8);
+    cv_sum_kernel<1><<<dim3((n_points + 31) / 32, kPotentialParts), kCvBlock, 0, stream>>>(
+        s, src, near2, sigma, clusters, pts, key, n_points, 0.0f, out, part_sums);
+    cv_parts_kernel<<<(n_points + 255) / 256, 256, 0, stream>>>(part_sums, kPotentialParts, key, n_points, out);
     return cudaGetLastError();
 }
 
