@@ -290,6 +290,22 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
     int w_pending = -1;                      // layer whose weight gradient waits in TMEM to be read out
     bool ok = true;
     uint32_t err = 0;
+    // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t,
+    // computed while the weight image's copy is in flight (act and actT lie outside its destination)
+    for (int idx = tid; idx < kTM * 32; idx += kThreads) {
+        const int r = idx >> 5, f = idx & 31;
+        float t = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kIn; k++) t = t + g.freqs[f * kIn + k] * xin[r * kIn + k];
+        float s, c;
+        sincospi_own(2.0f * t, &s, &c);
+        store_bf16(act, r, f, s);
+        store_bf16(act, r, 32 + f, c);
+        store_bf16(actT, f, r, s);
+        store_bf16(actT, 32 + f, r, c);
+    }
+    fence_async_smem();
+    // the barrier of the staging wait also publishes the features to the tensor cores
     if (!__syncthreads_and(mbar_wait_bounded(bar, 0u))) {
         // the staging copy did not land: give it one more bounded wait so that it does not write
         // into a later block's shared memory, release TMEM and leave this block's gradient unwritten
@@ -298,21 +314,6 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_fused_kernel(FusedTrain
         ok = false;
     }
     if (ok) {
-        // Fourier features (mlp.cu's fourier_kernel): phi[r][f] = sin 2 pi t, phi[r][32 + f] = cos 2 pi t
-        for (int idx = tid; idx < kTM * 32; idx += kThreads) {
-            const int r = idx >> 5, f = idx & 31;
-            float t = 0.0f;
-#pragma unroll
-            for (int k = 0; k < kIn; k++) t = t + g.freqs[f * kIn + k] * xin[r * kIn + k];
-            float s, c;
-            sincospi_own(2.0f * t, &s, &c);
-            store_bf16(act, r, f, s);
-            store_bf16(act, r, 32 + f, c);
-            store_bf16(actT, f, r, s);
-            store_bf16(actT, 32 + f, r, c);
-        }
-        fence_async_smem();
-        __syncthreads();
         // injected failure (tests): a bounded wait on drain_bar, on which nothing arrives before the
         // teardown, runs out like a product whose completion never came
         if (g.inject_wait_polls) ok = __syncthreads_and(mbar_wait_bounded(dbar, 0u, g.inject_wait_polls));
