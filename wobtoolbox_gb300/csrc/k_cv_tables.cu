@@ -506,7 +506,7 @@ __global__ void cv_parts_kernel(const double *__restrict__ part_sums, uint32_t p
 
 // Blocks of the same 32 points the potential's largest groups are split over: with one block per
 // 32 points there are too few blocks to fill the GPU for the slice-sized point sets.
-constexpr uint32_t kPotentialParts = 4;
+constexpr uint32_t kPotentialParts = 8;
 
 // The network's input at every stored element: (centroid, normal), 2D padded with zeros.
 template <int D>
