@@ -85,7 +85,7 @@ def fp32_roofline(bounces_per_s, clk):
 
 def build_scene_arrays():
     from wobtoolbox_gb300 import workloads as W
-    return W.config1_scene(subdiv=6, seed=SEED, alpha=2.0, source=(3.0, 0.5, 0.0))
+    return W.robin_sphere_scene(subdiv=6, seed=SEED, alpha=2.0, source=(3.0, 0.5, 0.0))
 
 
 def params():
@@ -297,7 +297,7 @@ def run_ours(args):
     wob.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     if args.workload == "dl2d":
-        sc = W.config0_scene()
+        sc = W.star_dirichlet_scene()
         scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
         pts = sc["points"]
         paths = 1024
@@ -1148,8 +1148,8 @@ def run_fmad(args):
     on both (CUDA events, L2 flushed between steps) and the two builds' per-point estimates, drawn
     with different seeds, are compared by z-scores (the fast build is not path-for-path identical
     to the oracle, so it is validated statistically against the exact one):
-      robin3d -- the headline step (timing only: the alpha = 2 series diverges, see DESIGN.md);
-      dl2d    -- configs[0] at 1024 paths x 8 bounces;
+      robin3d -- the headline step (timing only: the alpha = 2 series diverges);
+      dl2d    -- the 2D double-layer star at 1024 paths x 8 bounces;
       fwd3d   -- the 327,680-triangle forward walk, 256 paths;
       vpl2d   -- the VPL aggregation over the same VPLs (deterministic: relative difference)."""
     import ctypes as C
@@ -1235,7 +1235,7 @@ def run_fmad(args):
     tmp.close()
     results["robin3d"] = compare("robin3d", (sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"]),
                                  dataclasses.replace(params(), num_sample_paths=PATHS), pts, 2, True, z_test=False)
-    c0 = W.config0_scene()
+    c0 = W.star_dirichlet_scene()
     p0 = wob.EstimatorParams(bie_model=wob.IndirectDoubleLayer, domain=wob.InteriorDomain,
                              estimator=wob.BackwardEstimator, problem=wob.DirichletProblem, path_length=8,
                              num_sample_paths=1024, seed=SEED)
@@ -1284,7 +1284,8 @@ def run_fmad(args):
     out = {"metric": "time per step, bit-exact build (-fmad=false) vs contraction-enabled build (-fmad=true)",
            "value": results["robin3d"]["speedup"], "unit": "x (exact time / contracted time, headline step)",
            "n_gpus": world, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "headline robin3d, dl2d (configs[0]), fwd3d (configs[3]'s walk), VPL aggregation",
+           "config": {"workload": "headline robin3d, dl2d (2D double-layer star), fwd3d (327,680-triangle forward walk), "
+                                  "VPL aggregation",
                       "note": "per-point estimates of the two builds drawn with different seeds; z = difference / "
                               "combined standard error"},
            "results": results}
@@ -1379,7 +1380,7 @@ def run_wos(args):
     rank, world, local = dist_init(args)
     wob.load()
     dev = torch.device("cuda", torch.cuda.current_device())
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     scene = wob.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
     pts = sc["points"]
     n_pts = len(pts)

@@ -21,7 +21,7 @@ from wobtoolbox_gb300 import workloads as W  # noqa: E402
 
 
 def star_dl():
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = O.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     p = EstimatorParams(bie_model=1, path_length=8, num_sample_paths=16, seed=0)
     return O.lbvh_stats(el, p, sc["points"])

@@ -51,7 +51,7 @@ def _parity_inside(case, pts):
 def points_for(name, case):
     rng = np.random.default_rng(100)
     if name == "dl2d_star1024":
-        return W.config0_scene()["points"]
+        return W.star_dirichlet_scene()["points"]
     if name == "robin3d_sphere81920_alpha1":
         cand = W.slice_points_z0(512, 2.6)
         cand = cand[rng.choice(len(cand), 2000, replace=False)]

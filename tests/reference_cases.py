@@ -1,7 +1,7 @@
 """Scenes and estimator settings of the reference fixtures (tests/golden/reference_*.npz).
 
-Each case names a workload of the reference (its BASELINE configuration, or one of its shipped
-data/config_*.json files) at a size the reference's CPU build finishes in seconds. The scene is
+Each case names a workload of the reference (one of its benchmarked configurations, or one of its
+shipped data/config_*.json files) at a size the reference's CPU build finishes in seconds. The scene is
 rebuilt from seeded generators on both sides; the fixture stores the evaluation points, the
 reference's per-point statistics and, for a few points, every path value, plus a checksum of the
 scene arrays so that a change of the generators is caught instead of silently compared.
@@ -28,26 +28,26 @@ def _three_sources(seed: int, inside: bool):
 
 
 def dl2d_star1024():
-    """configs[0]: 2D interior Dirichlet, double layer, star r = 1 + 0.3 cos 5t with 1024
+    """2D interior Dirichlet, double layer, star r = 1 + 0.3 cos 5t with 1024
     segments, g = e^x cos y, the 7,960 interior points of the 128^2 grid, 8 bounces."""
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     params = EstimatorParams(bie_model=1, domain=0, estimator=0, problem=0, path_length=8, eps=FLT_EPS)
     return dict(verts=sc["verts"], normals=sc["normals"], bvals=sc["bvals"], types=sc["types"], alphas=None,
                 params=params, volume=None, n_paths=256, n_pp=8, pp_paths=4096)
 
 
 def robin3d_sphere81920_alpha1():
-    """configs[1]'s geometry and data with Robin alpha = 1 (the reference's shipped Robin value,
+    """The 3D Robin benchmark's geometry and data with alpha = 1 (the reference's shipped Robin value,
     for which the direct BIE's series converges; at alpha = 2 it diverges): displaced icosphere of
     81,920 triangles, u = 1/(4 pi |x - s|), s = (3, 0.5, 0), direct BIE, backward, 16 bounces."""
-    sc = W.config1_scene(subdiv=6, seed=0, alpha=1.0)
+    sc = W.robin_sphere_scene(subdiv=6, seed=0, alpha=1.0)
     params = EstimatorParams(bie_model=2, domain=0, estimator=0, problem=2, path_length=16, eps=FLT_EPS)
     return dict(verts=sc["verts"], normals=sc["normals"], bvals=sc["bvals"], types=sc["types"], alphas=sc["alphas"],
                 params=params, volume=None, n_paths=1024, n_pp=8, pp_paths=4096)
 
 
 def fwdsl3d_ext_neumann_sphere5120():
-    """configs[3]'s problem (data/config_general_3d_exterior_Neumann.json): exterior Neumann,
+    """The 3D exterior Neumann problem (data/config_general_3d_exterior_Neumann.json): exterior Neumann,
     forward single layer, 4 bounces, Neumann data of three interior point sources, on the displaced
     icosphere at 5,120 triangles."""
     V, F, _ = W.displaced_icosphere(4, 0.15, 4, 0)
@@ -61,7 +61,7 @@ def fwdsl3d_ext_neumann_sphere5120():
 
 
 def slris3d_mixed_sphere1280():
-    """configs[4]'s problem (data/config_general_3d_interior_Mixed.json: single layer, backward,
+    """The 3D interior mixed problem (data/config_general_3d_interior_Mixed.json: single layer, backward,
     64 resampling candidates, eps 1e-5, first-kind scaling 2, 4 bounces): Dirichlet on faces whose
     centroid has z > 0, Neumann elsewhere, data of three exterior point sources, icosphere at
     1,280 triangles."""

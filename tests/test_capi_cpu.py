@@ -70,7 +70,7 @@ def test_grid_points_match_reference_formula():
 
 def test_config0_interior_point_count():
     from wobtoolbox_gb300 import workloads as W
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     assert sc["mask"].sum() == 7960 and len(sc["verts"]) == 1024
     # clockwise star: outward normals
     mid = sc["verts"].mean(1)

@@ -67,7 +67,7 @@ def _run_and_compare(engine, oracle, cuda, scene, params, pts, accel=False):
 def test_robin3d_benchmark_scene_every_tuned_build(engine, oracle, cuda):
     """The headline workload's own scene (81,920 triangles, alpha = 2, 16 bounces), 64 inside
     points of its z = 0 slice including points close to the surface, 1024 paths each."""
-    sc = W.config1_scene(subdiv=6, seed=0, alpha=2.0)
+    sc = W.robin_sphere_scene(subdiv=6, seed=0, alpha=2.0)
     assert np.all(sc["alphas"] == 2.0)  # one alpha for every vertex: the records' scene-constant path
     scene = engine.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"], sc["alphas"])
     cand = W.slice_points_z0(512, 2.6)

@@ -134,7 +134,7 @@ def test_line_grid_walks_match_oracle(engine, oracle, cuda):
     """The 2D double-layer workload (1024 segments, line grid of 512 x 512 cells) walks exactly
     the oracle's paths."""
     torch = cuda
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     scene = engine.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     pts = np.ascontiguousarray(sc["points"][::40])
     p = engine.EstimatorParams(bie_model=1, path_length=8, num_sample_paths=64, seed=3)

@@ -1,9 +1,9 @@
 """The engine against the reference's own estimator (compiled from the reference tree; committed
 fixtures tests/golden/reference_*.npz): per-point estimates at equal sample count, the z-score
 distribution against an empirical null, and every path value at a few points
-(tests/reference_stats.py). Among the cases: configs[0] complete (all 7,960 points of the star),
-configs[1]'s 81,920-triangle geometry with the convergent alpha = 1, and the problems of
-configs[3] and configs[4] at reduced mesh size."""
+(tests/reference_stats.py). Among the cases: the 2D double-layer star complete (all 7,960
+interior points), the 81,920-triangle Robin geometry with the convergent alpha = 1, and the 3D
+exterior Neumann and interior mixed problems at reduced mesh size."""
 from __future__ import annotations
 
 import dataclasses

@@ -18,7 +18,7 @@ def _elems(oracle, scene):
 
 def test_closest_point_matches_scan(engine, oracle, cuda):
     torch = cuda
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     scene = engine.SceneHost(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     rng = np.random.default_rng(1)
     x = rng.uniform(-1.4, 1.4, (5000, 2)).astype(np.float32)

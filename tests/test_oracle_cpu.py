@@ -95,7 +95,7 @@ def _z_test(mean, ex, var, n):
 
 def test_double_layer_unbiased_2d(oracle):
     """The 2D star workload's walk: DL interior Dirichlet on a star, g = e^x cos y; z-test per point."""
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     import wobtoolbox_gb300 as wob
     pts = sc["points"][::97]
@@ -113,7 +113,7 @@ def test_double_layer_unbiased_2d(oracle):
 
 def test_closed_form_walk_matches_estimator(oracle):
     """apps/simple_wob_and_wos.cu:81-108 (closed-form DL walk) vs the general estimator."""
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     import wobtoolbox_gb300 as wob
     pts = sc["points"][::301]
@@ -190,7 +190,7 @@ def test_walk_on_spheres_oracle_unbiased(oracle):
     """apps/simple_wob_and_wos.cu:111-137 restated: WoS on the star with g = e^x cos y (harmonic)
     is unbiased up to the eps-shell error; per-point z-tests."""
     import wobtoolbox_gb300 as wob
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     pts = sc["points"][::397]
     n = 3000
@@ -204,7 +204,7 @@ def test_walk_on_spheres_oracle_unbiased(oracle):
 
 
 def test_closest_point_oracle_brute_force(oracle):
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     rng = np.random.default_rng(0)
     x = rng.uniform(-1.3, 1.3, (200, 2)).astype(np.float32)
@@ -223,7 +223,7 @@ def test_lbvh_work_counter(oracle):
     the primitives it hits and visits at least the root; a line far from the scene visits only
     the root."""
     import wobtoolbox_gb300 as wob
-    sc = W.config0_scene()
+    sc = W.star_dirichlet_scene()
     el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
     p = wob.EstimatorParams(bie_model=1, path_length=2, num_sample_paths=4, seed=0)
     pts = sc["points"][::50]
@@ -238,7 +238,7 @@ def test_oracle_bvh_filter_is_exact(oracle, dim):
     """The oracle's optional BVH filter for line queries (used by the CPU baseline) changes no path."""
     import wobtoolbox_gb300 as wob
     if dim == 2:
-        sc = W.config0_scene()
+        sc = W.star_dirichlet_scene()
         el = oracle.Elements(sc["verts"], sc["normals"], sc["bvals"], sc["types"])
         pts = sc["points"][::200]
         p = wob.EstimatorParams(bie_model=1, path_length=6, num_sample_paths=32, seed=3)

@@ -1,7 +1,8 @@
 """The oracle against the reference's own estimator (compiled from the reference tree; committed
 fixtures tests/golden/reference_*.npz written by tests/golden/make_reference_fixtures.py): the
 statistical agreement of tests/reference_stats.py at equal sample count, on the benchmark
-workloads (configs[0] complete: all 7,960 points) and on shipped reference configurations.
+workloads (the 2D double-layer star complete: all 7,960 points) and on shipped reference
+configurations.
 This pins the oracle, and through the engine's bit-identity with the oracle, the engine."""
 from __future__ import annotations
 

@@ -175,7 +175,7 @@ def point_sources(p: np.ndarray, sources: np.ndarray, q: np.ndarray) -> np.ndarr
 
 
 # ------------------------------------------------------------------ the benchmark scenes
-def config0_scene():
+def star_dirichlet_scene():
     """2D interior Dirichlet star (1024 segments, r = 1 + 0.3 cos 5 theta), g = e^x cos y at the
     vertices, linear along segments; 128^2 grid over [-1.3, 1.3]^2, interior points only."""
     verts, normals = star_polygon(1024, 5, 0.3)
@@ -188,7 +188,7 @@ def config0_scene():
                 points=np.ascontiguousarray(grid[mask]))
 
 
-def config1_scene(subdiv: int = 6, seed: int = 0, alpha: float = 2.0, source=(3.0, 0.5, 0.0)):
+def robin_sphere_scene(subdiv: int = 6, seed: int = 0, alpha: float = 2.0, source=(3.0, 0.5, 0.0)):
     """3D interior Robin (du/dn + alpha u = h) on a displaced icosphere, u = 1/(4 pi |x - s|)."""
     V, F, coeffs = displaced_icosphere(subdiv, 0.15, 4, seed)
     verts, normals = mesh_elements(V, F)
