@@ -3,14 +3,16 @@
 // every weight and activation in shared memory and writes the block's gradient; a second kernel
 // sums the blocks' gradients in a fixed order (so a step is deterministic), applies Adam, writes
 // the updated weights as a packed BF16 image in both operand layouts, and its last block advances
-// the step counter. wob_mlp_train replays the two as a CUDA graph. Each block of the next step
-// stages that image (74 KB) into shared memory with one TMA bulk copy (cp.async.bulk, completion
-// on an mbarrier, the wait bounded), instead of every block reading and converting the FP32
-// parameters itself.
+// the step counter. Both are programmatic dependent launches (each starts its set-up while the
+// previous kernel finishes and waits for it in griddepcontrol.wait); wob_mlp_train captures 16
+// steps into a CUDA graph and replays it. Each block of the next step stages that image (74 KB)
+// into shared memory with one TMA bulk copy (cp.async.bulk, completion on an mbarrier, the wait
+// bounded; the Fourier features are computed meanwhile), instead of every block reading and
+// converting the FP32 parameters itself.
 //
 // Network and parameter layout as in mlp.cu: phi = [sin, cos](2 pi B v) (32 frequencies of the
 // 6 inputs), 4 hidden layers 64 -> 64 with SiLU, a linear 64 -> out_dim head; FP32 parameters,
-// for each layer W [out][in] row-major then b [out]. pre-activations are kept as BF16 for the SiLU
+// for each layer W [out][in] row-major then b [out]. Pre-activations are kept as BF16 for the SiLU
 // derivative, bias gradients are summed in FP32 from the FP32 products. No atomics: every sum has
 // a fixed order, so training is deterministic.
 //
