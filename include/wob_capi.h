@@ -403,6 +403,7 @@ int wob_measure_gather_peak(uint32_t n_records, uint32_t n_guide, uint32_t iters
  * element records are copied, the device buffers that no entry point writes in place (BVH,
  * intersection records, sampling tables, volume cache, line grid) are shared by reference count,
  * so either scene may be destroyed first and a later change to one leaves the other as it was.
+ * Cloning only reads the source scene and may run beside other calls that read it.
  * wob_scene_add_boundary_offsets: adds delta_j to the vertex values of stored element j (delta on
  * the device when delta_on_device != 0, else on the host) and rebuilds the |g| sampling tables;
  * synchronises the stream. The plain forward estimator on such a clone, plus S sigma~ from

@@ -64,9 +64,13 @@ struct DevBuf {
 };
 
 // dst holds src's allocation too (for buffers that no entry point writes after the scene is built).
+// The first share converts src to counted ownership; a process-wide lock makes concurrent clones of
+// one scene convert it once.
+std::mutex g_share_mutex;
 void share(DevBuf &dst, DevBuf &src) {
     dst.release();
     if (!src.ptr) return;
+    std::lock_guard<std::mutex> lock(g_share_mutex);
     if (!src.shared) src.shared = std::shared_ptr<void>(src.ptr, [](void *p) { cudaFree(p); });
     dst.ptr = src.ptr;
     dst.bytes = src.bytes;
