@@ -167,14 +167,17 @@ def _morton_order(points):
     return np.lexsort((np.arange(len(p)), code))
 
 
-def _cluster_split(tx, cen, w, near2, theta, size=32, order=None, fan=8):
+def _cluster_split(tx, cen, w, near2, theta, size=32, order=None, fan=8, return_cover=False):
     """Per target: the far records' expansion (phi, grad) and the mask [targets, sources] of the
     sources still summed pair by pair, for targets tx in warps of 32 consecutive ones. Records of
     three sizes (size, size * fan, size * fan^2 consecutive sources); one is taken when it is far
-    and none of its ancestors is (k_cv_tables.cu's cv_sum_kernel)."""
+    and none of its ancestors is (k_cv_tables.cu's cv_sum_kernel). With return_cover, also the
+    number of sources inside the records taken for each target (each source must be counted once:
+    inside one taken record or summed pair by pair)."""
     levels = [_clusters(cen, w, near2, theta, size * fan ** L) for L in range(3)]
     phi = np.zeros(len(tx)); g = np.zeros((len(tx), 3))
     pair = np.ones((len(tx), len(cen)), bool)
+    cover = np.zeros(len(tx), np.int64)
     order = np.arange(len(tx)) if order is None else order
     for g0 in range(0, len(tx), 32):
         grp = order[g0:g0 + 32]
@@ -190,8 +193,12 @@ def _cluster_split(tx, cen, w, near2, theta, size=32, order=None, fan=8):
                 g[grp] += gr
                 span = size * fan ** L
                 for k in np.nonzero(far)[0]:
-                    pair[np.ix_(grp, np.arange(k * span, min(len(cen), (k + 1) * span)))] = False
+                    members = np.arange(k * span, min(len(cen), (k + 1) * span))
+                    pair[np.ix_(grp, members)] = False
+                    cover[grp] += len(members)
             covered = far if covered is None else (far | covered[np.arange(len(z)) // fan])
+    if return_cover:
+        return phi, g, pair, cover
     return phi, g, pair
 
 

@@ -70,3 +70,25 @@ def test_cluster_expansion_close_to_pairwise():
     pg = T.potential(v, sig, pts, 3.0, theta=0.3)
     scale = np.abs(pr).max(0)
     assert np.all(np.abs(pg - pr) <= 2e-4 * scale), (np.abs(pg - pr) / scale).max()
+
+
+def test_treecode_counts_every_source_once():
+    """The three-level decisions partition the sources for every target: each source lies in
+    exactly one record taken by its expansion or is summed pair by pair (no record taken together
+    with an ancestor, none left out). Targets in compact tiles of 32, as the engine takes them:
+    the 5,120 centroids of the surface in storage order, a small ball of points just off the
+    surface and one far away; several theta."""
+    from wobtoolbox_gb300 import workloads as W
+    V, F, _ = W.displaced_icosphere(4, 0.15, 4, 0)
+    verts, _ = W.mesh_elements(V, F)
+    verts = verts[np.array(_median_order(verts.astype(np.float64).mean(1)))]  # spatially compact order
+    cen = verts.astype(np.float64).mean(1)
+    h2 = np.max(np.stack([((verts[:, 1] - verts[:, 0]) ** 2).sum(1), ((verts[:, 2] - verts[:, 1]) ** 2).sum(1),
+                          ((verts[:, 0] - verts[:, 2]) ** 2).sum(1)], 1), 1).astype(np.float64)
+    rng = np.random.default_rng(7)
+    ball = rng.uniform(-0.05, 0.05, (64, 3))
+    tx = np.concatenate([cen, ball + [1.4, 0.0, 0.0], ball + [6.0, 0.0, 0.0]])
+    for theta in (0.1, 0.3, 0.6):
+        _, _, pair, cover = T._cluster_split(tx, cen, np.ones(len(cen)), 9.0 * h2, theta, return_cover=True)
+        assert np.array_equal(cover + pair.sum(1), np.full(len(tx), len(cen))), theta
+        assert cover[:len(cen)].max() > 0 and cover[-64:].min() > 2048, (theta, cover.max())
